@@ -1,0 +1,51 @@
+// hyc_args.h -- plain-C++ layout of the kernel arguments, shared by the CUDA
+// translation units and the host layer.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace hyc {
+
+constexpr uint8_t kIP = 1, kIU = 2, kIV = 4;  // mask bits: ip, iu, iv
+
+constexpr int kMaxFields = 16;
+enum Scheme { kPCM = 0, kMPDATA = 1, kFCT2 = 2, kFCT4 = 4 };
+
+struct FieldDesc {
+  double *nbase;        // first slice of time level n (old in, new out)
+  const double *mbase;  // first slice of time level m (center)
+  int k_off;            // slice index of layer k=1 (1 for q2/q2l, whose k starts at 0)
+  int kmin, kmax;       // the field is advected for kmin <= k <= kmax (1-based)
+  int pad;
+  double posdef;        // MPDATA offset, mod_tsadvc.F90:1761-1763
+};
+
+struct TileArgs {
+  int ii, jj, nbdy, ld1, ld2;
+  long long slice;  // ld1*ld2
+  int ntx, nty;     // tiles in x and y
+  int mode;         // 0: tsadvc (fco/fcn from dp, uflx, vflx); 1: advem (fco/fcn given)
+  const uint8_t *msk;
+  const double *scal, *scali;
+  // tsadvc mode, per layer k (0-based): uflx + k*slice, vflx + k*slice, dpn + k*slice
+  const double *uflx, *vflx, *dpn;
+  const double *oneta_n;  // onetamas(:,:,m) when btrmas (mod_tsadvc.F90:1806), else null
+  // advem mode (single slice)
+  const double *fco, *fcn;
+  double dt2;
+  int nfld;
+  FieldDesc f[kMaxFields];
+  // output: out + (fi*kdm + k)*slice ; every interior cell written
+  double *out;
+  int kdm;
+};
+
+template <int TX, int TY>
+struct TileGeom {
+  static constexpr int RX = TX + 6, RY = TY + 6, N = RX * RY;
+  // per-layer arrays: U V FCO FCN HN RH SCAL SCALI ; per-field: FLD FLDC FX FY FLO FXL FNL RP RM QX QN
+  static constexpr int NLAYER = 8, NFIELD = 11;
+  static constexpr size_t smem_bytes = (size_t)(NLAYER + NFIELD) * N * sizeof(double) + ((N + 15) / 16) * 16;
+};
+
+}  // namespace hyc

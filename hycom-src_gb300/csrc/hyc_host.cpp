@@ -1,0 +1,606 @@
+// hyc_host.cpp -- host side of libhycadv: contexts, resident fields, the
+// tsadvc/advem/xctilr drivers and the C ABI declared in include/hycom_adv.h.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/hycom_adv.h"
+#include "hyc_internal.h"
+#include "hyc_args.h"
+
+using hyc::FieldDesc;
+using hyc::TileArgs;
+
+namespace {
+
+thread_local std::string g_lib_error;
+
+struct Field {
+  double *dev = nullptr;   // device data used by the kernels
+  double *host = nullptr;  // caller's host array (HYC_HOST binding)
+  int64_t nelem = 0;
+  bool owned = false;      // dev allocated by the library
+};
+
+}  // namespace
+
+struct hyc_ctx {
+  int idm = 0, jdm = 0, kdm = 0, nbdy = 0, nreg = 0, ld1 = 0, ld2 = 0;
+  long long slice = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  uint8_t *d_msk = nullptr;
+  double *d_scp2 = nullptr, *d_scp2i = nullptr;
+  Field fields[HYC_NFIELDS];
+  double *d_scratch = nullptr;  // advem output slices (fields x layers)
+  size_t scratch_elems = 0;
+  double *d_tmp = nullptr;      // staging for host-pointer advem/xctilr (8 slices)
+  long long *d_keys = nullptr;  // salinity range keys (2*kdm)
+  long long *h_keys = nullptr;  // pinned
+  double *d_sum = nullptr;      // mass-sum partials + result
+  double *h_sum = nullptr;      // pinned
+  hyc::TileShape shape{32, 16};
+  std::string err;
+};
+
+namespace {
+
+int fail(hyc_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  g_lib_error = buf;
+  return code;
+}
+
+int cuda_fail(hyc_ctx *c, cudaError_t e, const char *what) {
+  return fail(c, HYC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                          \
+  do {                                          \
+    cudaError_t e_ = (call);                    \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+  } while (0)
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int d) {
+    cudaGetDevice(&prev);
+    if (prev != d) cudaSetDevice(d);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+inline long long off(const hyc_ctx *c, int i, int j) {
+  return (long long)(i + c->nbdy - 1) + (long long)(j + c->nbdy - 1) * c->ld1;
+}
+
+const int kMbdy[5] = {2, 5, 5, 0, 5};  // mbdy_advtyp, mod_tsadvc.F90:24-29
+
+bool valid_advtyp(int a) { return a == 0 || a == 1 || a == 2 || a == 4; }
+
+hyc::TileShape env_shape(hyc::TileShape def) {
+  const char *s = getenv("HYC_TILE");
+  if (!s) return def;
+  hyc::TileShape t{0, 0};
+  if (sscanf(s, "%dx%d", &t.tx, &t.ty) == 2 && hyc::advect_tile_shape_ok(t)) return t;
+  return def;
+}
+
+int ensure_scratch(hyc_ctx *c, size_t elems) {
+  if (c->scratch_elems >= elems) return HYC_OK;
+  if (c->d_scratch) cudaFree(c->d_scratch);
+  c->d_scratch = nullptr;
+  c->scratch_elems = 0;
+  cudaError_t e = cudaMalloc(&c->d_scratch, elems * sizeof(double));
+  if (e != cudaSuccess) return fail(c, HYC_ERR_NOMEM, "cannot allocate %zu bytes of scratch", elems * 8);
+  c->scratch_elems = elems;
+  return HYC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host xctilr used by bigrid (same halo rule as the device kernel)
+// ---------------------------------------------------------------------------
+template <class T>
+void host_halo(T *a, int ii, int jj, int nb, int ld1, int nreg) {
+  auto at = [&](int i, int j) -> T & { return a[(i + nb - 1) + (long long)(j + nb - 1) * ld1]; };
+  const bool closed_y = nreg <= 2, closed_x = (nreg == 0 || nreg == 4);
+  for (int j = 1; j <= nb; j++)
+    for (int i = 1; i <= ii; i++) {
+      at(i, 1 - j) = closed_y ? T(0) : at(i, jj + 1 - j);
+      at(i, jj + j) = closed_y ? T(0) : at(i, j);
+    }
+  for (int j = 1 - nb; j <= jj + nb; j++)
+    for (int i = 1; i <= nb; i++) {
+      at(1 - i, j) = closed_x ? T(0) : at(ii + 1 - i, j);
+      at(ii + i, j) = closed_x ? T(0) : at(i, j);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *hyc_version(void) { return "hycadv 0.1 sm_103a"; }
+
+int hyc_last_error(const hyc_ctx *ctx, char *buf, size_t n) {
+  if (!buf || n == 0) return HYC_ERR_ARG;
+  const std::string &s = ctx ? ctx->err : g_lib_error;
+  snprintf(buf, n, "%s", s.c_str());
+  return HYC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// bigrid.F90:1-415 for one tile (i0=j0=0), mapflg != 4.  The land/sea
+// masks: ip where depth>0 (over the halo after the halo fill and land
+// borders), iu/iv where both neighbouring p-points are sea (interior, then
+// halo-filled), iq for interior and promontory vorticity points, and the
+// sea-only neighbour indices (W,E,S,N if sea, else the point itself).
+// ---------------------------------------------------------------------------
+int hyc_bigrid(int32_t idm, int32_t jdm, int32_t nbdy, double *depth, int32_t *ip, int32_t *iu, int32_t *iv,
+               int32_t *iq, int32_t *ipim1, int32_t *ipip1, int32_t *ipjm1, int32_t *ipjp1, int32_t *nreg) {
+  if (idm < 1 || jdm < 1 || nbdy < 1 || !depth || !ip || !iu || !iv || !nreg)
+    return fail(nullptr, HYC_ERR_ARG, "hyc_bigrid: bad arguments");
+  const int ii = idm, jj = jdm, nb = nbdy, ld1 = idm + 2 * nbdy, ld2 = jdm + 2 * nbdy;
+  auto D = [&](int i, int j) -> double & { return depth[(i + nb - 1) + (long long)(j + nb - 1) * ld1]; };
+  // periodicity from sea in the last column / last row (bigrid.F90:25-45)
+  bool lperiod = false, larctic = false;
+  for (int j = 1; j <= jj; j++) lperiod |= D(ii, j) > 0.0;
+  for (int i = 1; i <= ii; i++) larctic |= D(i, jj) > 0.0;
+  if (larctic) return fail(nullptr, HYC_ERR_GRID, "hyc_bigrid: sea in row jdm (arctic/f-plane grids unsupported)");
+  const int nr = lperiod ? 1 : 0;
+  host_halo(depth, ii, jj, nb, ld1, nr);
+  for (int j = 1 - nb; j <= jj + nb; j++)
+    for (int i = 1 - nb; i <= ii + nb; i++) {
+      bool border = j <= 0 || j > jj || (!lperiod && (i <= 0 || i > ii));
+      if (border) D(i, j) = 0.0;
+    }
+  for (int j = 1; j <= jj; j++)  // 1-point seas (bigrid.F90:156-191)
+    for (int i = 1; i <= ii; i++)
+      if (D(i, j) > 0.0 && D(i - 1, j) <= 0.0 && D(i + 1, j) <= 0.0 && D(i, j - 1) <= 0.0 && D(i, j + 1) <= 0.0)
+        return fail(nullptr, HYC_ERR_GRID, "hyc_bigrid: 1-point sea at i=%d j=%d", i, j);
+  const size_t n2 = (size_t)ld1 * ld2;
+  std::vector<int32_t> p(n2, 0), u(n2, 0), v(n2, 0), q(n2, 0);
+  auto at = [&](std::vector<int32_t> &a, int i, int j) -> int32_t & {
+    return a[(i + nb - 1) + (size_t)(j + nb - 1) * ld1];
+  };
+  for (int j = 1 - nb; j <= jj + nb; j++)
+    for (int i = 1 - nb; i <= ii + nb; i++) at(p, i, j) = D(i, j) > 0.0 ? 1 : 0;
+  for (int j = 1; j <= jj; j++)
+    for (int i = 1; i <= ii; i++) {
+      int c = at(p, i, j), w = at(p, i - 1, j), s = at(p, i, j - 1), sw = at(p, i - 1, j - 1);
+      at(u, i, j) = (w > 0 && c > 0) ? 1 : 0;
+      at(v, i, j) = (s > 0 && c > 0) ? 1 : 0;
+      at(q, i, j) = ((c > 0 && w > 0 && s > 0 && sw > 0) || (c > 0 && sw > 0) || (w > 0 && s > 0)) ? 1 : 0;
+    }
+  host_halo(u.data(), ii, jj, nb, ld1, nr);
+  host_halo(v.data(), ii, jj, nb, ld1, nr);
+  host_halo(q.data(), ii, jj, nb, ld1, nr);
+  for (int j = 1 - nb; j <= jj + nb; j++)  // land borders, part II
+    for (int i = 1 - nb; i <= ii + nb; i++) {
+      bool border = j <= 0 || j > jj || (!lperiod && (i <= 0 || i > ii));
+      if (border) at(u, i, j) = at(v, i, j) = at(q, i, j) = 0;
+    }
+  memcpy(ip, p.data(), n2 * 4);
+  memcpy(iu, u.data(), n2 * 4);
+  memcpy(iv, v.data(), n2 * 4);
+  if (iq) memcpy(iq, q.data(), n2 * 4);
+  for (int j = 1 - nb; j <= jj + nb; j++)
+    for (int i = 1 - nb; i <= ii + nb; i++) {
+      size_t o = (i + nb - 1) + (size_t)(j + nb - 1) * ld1;
+      bool edge = i == 1 - nb || i == ii + nb || j == 1 - nb || j == jj + nb;
+      if (ipim1) ipim1[o] = (!edge && at(p, i - 1, j) != 0) ? i - 1 : i;
+      if (ipip1) ipip1[o] = (!edge && at(p, i + 1, j) != 0) ? i + 1 : i;
+      if (ipjm1) ipjm1[o] = (!edge && at(p, i, j - 1) != 0) ? j - 1 : j;
+      if (ipjp1) ipjp1[o] = (!edge && at(p, i, j + 1) != 0) ? j + 1 : j;
+    }
+  *nreg = nr;
+  return HYC_OK;
+}
+
+int hyc_adv_init(hyc_ctx **out, int32_t idm, int32_t jdm, int32_t kdm, int32_t nbdy, int32_t nreg, const int32_t *ip,
+                 const int32_t *iu, const int32_t *iv, const double *scp2, const double *scp2i, int32_t device) {
+  if (!out) return fail(nullptr, HYC_ERR_ARG, "hyc_adv_init: ctx is null");
+  *out = nullptr;
+  if (idm < 1 || jdm < 1 || kdm < 1 || nbdy < 3 || !ip || !iu || !iv || !scp2 || !scp2i)
+    return fail(nullptr, HYC_ERR_ARG, "hyc_adv_init: bad sizes or null arrays (need nbdy >= 3)");
+  if (!(nreg == 0 || nreg == 1 || nreg == 3 || nreg == 4))
+    return fail(nullptr, HYC_ERR_ARG, "hyc_adv_init: nreg %d unsupported (0, 1, 3 or 4)", nreg);
+  hyc_ctx *c = new hyc_ctx;
+  c->idm = idm;
+  c->jdm = jdm;
+  c->kdm = kdm;
+  c->nbdy = nbdy;
+  c->nreg = nreg;
+  c->ld1 = idm + 2 * nbdy;
+  c->ld2 = jdm + 2 * nbdy;
+  c->slice = (long long)c->ld1 * c->ld2;
+  c->device = device;
+  c->shape = env_shape(c->shape);
+  // masks: iu/iv must be the bigrid ones (iu = ip(i-1)*ip(i), iv = ip(j-1)*ip(j))
+  const int nb = nbdy, ii = idm, jj = jdm;
+  std::vector<uint8_t> m((size_t)c->slice, 0);
+  for (int j = 1 - nb; j <= jj + nb; j++)
+    for (int i = 1 - nb; i <= ii + nb; i++) {
+      long long o = off(c, i, j);
+      bool p = ip[o] != 0, u = iu[o] != 0, v = iv[o] != 0;
+      if (i > 1 - nb) {
+        bool want = p && ip[o - 1] != 0;
+        if (u != want) {
+          int rc = fail(nullptr, HYC_ERR_MASK, "iu(%d,%d)=%d but ip(i-1)*ip(i)=%d", i, j, (int)u, (int)want);
+          delete c;
+          return rc;
+        }
+      } else if (u) {
+        int rc = fail(nullptr, HYC_ERR_MASK, "iu(%d,%d) set on the outer halo column", i, j);
+        delete c;
+        return rc;
+      }
+      if (j > 1 - nb) {
+        bool want = p && ip[o - c->ld1] != 0;
+        if (v != want) {
+          int rc = fail(nullptr, HYC_ERR_MASK, "iv(%d,%d)=%d but ip(j-1)*ip(j)=%d", i, j, (int)v, (int)want);
+          delete c;
+          return rc;
+        }
+      } else if (v) {
+        int rc = fail(nullptr, HYC_ERR_MASK, "iv(%d,%d) set on the outer halo row", i, j);
+        delete c;
+        return rc;
+      }
+      m[o] = (p ? hyc::kIP : 0) | (u ? hyc::kIU : 0) | (v ? hyc::kIV : 0);
+    }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) {
+    int rc = fail(nullptr, HYC_ERR_CUDA, "hyc_adv_init: CUDA device %d not available", device);
+    delete c;
+    return rc;
+  }
+  DeviceGuard g(device);
+  auto bail = [&](cudaError_t e, const char *w) {
+    int rc = cuda_fail(nullptr, e, w);
+    hyc_adv_finalize(c);
+    return rc;
+  };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
+  c->own_stream = true;
+  if ((e = cudaMalloc(&c->d_msk, c->slice)) != cudaSuccess) return bail(e, "malloc msk");
+  if ((e = cudaMalloc(&c->d_scp2, c->slice * 8)) != cudaSuccess) return bail(e, "malloc scp2");
+  if ((e = cudaMalloc(&c->d_scp2i, c->slice * 8)) != cudaSuccess) return bail(e, "malloc scp2i");
+  if ((e = cudaMalloc(&c->d_keys, 2 * kdm * sizeof(long long))) != cudaSuccess) return bail(e, "malloc keys");
+  if ((e = cudaMallocHost(&c->h_keys, 2 * kdm * sizeof(long long))) != cudaSuccess) return bail(e, "host keys");
+  if ((e = cudaMalloc(&c->d_sum, (2 * hyc::mass_sum_partials() + 2) * sizeof(double))) != cudaSuccess)
+    return bail(e, "malloc sum");
+  if ((e = cudaMallocHost(&c->h_sum, 2 * sizeof(double))) != cudaSuccess) return bail(e, "host sum");
+  if ((e = cudaMemcpy(c->d_msk, m.data(), c->slice, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e, "msk");
+  if ((e = cudaMemcpy(c->d_scp2, scp2, c->slice * 8, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e, "scp2");
+  if ((e = cudaMemcpy(c->d_scp2i, scp2i, c->slice * 8, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return bail(e, "scp2i");
+  *out = c;
+  return HYC_OK;
+}
+
+int hyc_adv_finalize(hyc_ctx *c) {
+  if (!c) return HYC_OK;
+  {
+    DeviceGuard g(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &f : c->fields)
+      if (f.owned && f.dev) cudaFree(f.dev);
+    cudaFree(c->d_msk);
+    cudaFree(c->d_scp2);
+    cudaFree(c->d_scp2i);
+    cudaFree(c->d_scratch);
+    cudaFree(c->d_tmp);
+    cudaFree(c->d_keys);
+    cudaFree(c->d_sum);
+    if (c->h_keys) cudaFreeHost(c->h_keys);
+    if (c->h_sum) cudaFreeHost(c->h_sum);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  }
+  delete c;
+  return HYC_OK;
+}
+
+int hyc_set_stream(hyc_ctx *c, void *stream) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  DeviceGuard g(c->device);
+  if (c->own_stream && c->stream) {
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+  }
+  c->stream = (cudaStream_t)stream;
+  c->own_stream = false;
+  return HYC_OK;
+}
+
+int hyc_synchronize(hyc_ctx *c) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  DeviceGuard g(c->device);
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  return HYC_OK;
+}
+
+int hyc_bind_field(hyc_ctx *c, int32_t field, void *ptr, int64_t nelem, int32_t where) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (field < 0 || field >= HYC_NFIELDS || !ptr || nelem <= 0 || (where != HYC_HOST && where != HYC_DEVICE))
+    return fail(c, HYC_ERR_ARG, "hyc_bind_field: bad arguments (field %d)", field);
+  DeviceGuard g(c->device);
+  Field &f = c->fields[field];
+  if (f.owned && f.dev) cudaFree(f.dev);
+  f = Field{};
+  f.nelem = nelem;
+  if (where == HYC_DEVICE) {
+    f.dev = (double *)ptr;
+  } else {
+    f.host = (double *)ptr;
+    CK(cudaMalloc(&f.dev, (size_t)nelem * sizeof(double)), "malloc field mirror");
+    f.owned = true;
+  }
+  return HYC_OK;
+}
+
+int hyc_sync_field(hyc_ctx *c, int32_t field, int32_t to_device) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (field < 0 || field >= HYC_NFIELDS) return fail(c, HYC_ERR_ARG, "bad field %d", field);
+  Field &f = c->fields[field];
+  if (!f.dev) return fail(c, HYC_ERR_FIELD, "field %d not bound", field);
+  if (!f.host) return HYC_OK;  // device-bound: nothing to move
+  DeviceGuard g(c->device);
+  size_t bytes = (size_t)f.nelem * sizeof(double);
+  if (to_device)
+    CK(cudaMemcpyAsync(f.dev, f.host, bytes, cudaMemcpyHostToDevice, c->stream), "sync h2d");
+  else
+    CK(cudaMemcpyAsync(f.host, f.dev, bytes, cudaMemcpyDeviceToHost, c->stream), "sync d2h");
+  return HYC_OK;
+}
+
+int hyc_xctilr(hyc_ctx *c, double *a, int32_t nlev, int32_t mh, int32_t nh, int32_t where) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (!a || nlev < 1) return fail(c, HYC_ERR_ARG, "hyc_xctilr: bad arguments");
+  DeviceGuard g(c->device);
+  if (where == HYC_DEVICE) {
+    CK(hyc::launch_xctilr(a, c->slice, nlev, c->idm, c->jdm, c->nbdy, c->ld1, mh, nh, c->nreg, c->stream), "xctilr");
+    return HYC_OK;
+  }
+  // host array: stage one slice at a time through the staging buffer
+  if (!c->d_tmp) CK(cudaMalloc(&c->d_tmp, 8 * c->slice * sizeof(double)), "malloc staging");
+  for (int l = 0; l < nlev; l++) {
+    double *h = a + (long long)l * c->slice;
+    CK(cudaMemcpyAsync(c->d_tmp, h, c->slice * 8, cudaMemcpyHostToDevice, c->stream), "h2d");
+    CK(hyc::launch_xctilr(c->d_tmp, c->slice, 1, c->idm, c->jdm, c->nbdy, c->ld1, mh, nh, c->nreg, c->stream),
+       "xctilr");
+    CK(cudaMemcpyAsync(h, c->d_tmp, c->slice * 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
+  }
+  CK(cudaStreamSynchronize(c->stream), "xctilr sync");
+  return HYC_OK;
+}
+
+int hyc_advem(hyc_ctx *c, int32_t advtyp, double *fld, const double *fldc, const double *u, const double *v,
+              const double *fco, const double *fcn, double posdef, const double *scal, const double *scali, double dt2,
+              int32_t btrmas, int32_t where) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (!valid_advtyp(advtyp)) return fail(c, HYC_ERR_ADVTYP, "advem called with advtyp = %d", advtyp);
+  if (advtyp == 2 && btrmas) return fail(c, HYC_ERR_UNSUPPORTED, "advem_fct2c (btrmas) not available");
+  if (c->nbdy < kMbdy[advtyp]) return fail(c, HYC_ERR_NBDY, "nbdy must be at least %d", kMbdy[advtyp]);
+  if (!fld || !u || !v || !fco || !fcn || !scal || !scali || (advtyp >= 2 && !fldc))
+    return fail(c, HYC_ERR_ARG, "hyc_advem: null array");
+  if (where != HYC_HOST && where != HYC_DEVICE) return fail(c, HYC_ERR_ARG, "bad where");
+  DeviceGuard g(c->device);
+  const long long sl = c->slice;
+  double *dfld = fld;
+  const double *dfldc = fldc, *du = u, *dv = v, *dfco = fco, *dfcn = fcn, *dscal = scal, *dscali = scali;
+  if (where == HYC_HOST) {
+    if (!c->d_tmp) CK(cudaMalloc(&c->d_tmp, 8 * sl * sizeof(double)), "malloc staging");
+    const double *src[8] = {fld, fldc ? fldc : fld, u, v, fco, fcn, scal, scali};
+    for (int q = 0; q < 8; q++)
+      CK(cudaMemcpyAsync(c->d_tmp + q * sl, src[q], sl * 8, cudaMemcpyHostToDevice, c->stream), "advem h2d");
+    dfld = c->d_tmp;
+    dfldc = c->d_tmp + sl;
+    du = c->d_tmp + 2 * sl;
+    dv = c->d_tmp + 3 * sl;
+    dfco = c->d_tmp + 4 * sl;
+    dfcn = c->d_tmp + 5 * sl;
+    dscal = c->d_tmp + 6 * sl;
+    dscali = c->d_tmp + 7 * sl;
+  }
+  int rc = ensure_scratch(c, (size_t)sl);
+  if (rc) return rc;
+  TileArgs a;
+  memset(&a, 0, sizeof a);
+  a.ii = c->idm;
+  a.jj = c->jdm;
+  a.nbdy = c->nbdy;
+  a.ld1 = c->ld1;
+  a.ld2 = c->ld2;
+  a.slice = sl;
+  a.ntx = (c->idm + c->shape.tx - 1) / c->shape.tx;
+  a.nty = (c->jdm + c->shape.ty - 1) / c->shape.ty;
+  a.mode = 1;
+  a.msk = c->d_msk;
+  a.scal = dscal;
+  a.scali = dscali;
+  a.uflx = du;
+  a.vflx = dv;
+  a.fco = dfco;
+  a.fcn = dfcn;
+  a.dt2 = dt2;
+  a.nfld = 1;
+  a.f[0].nbase = dfld;
+  a.f[0].mbase = dfldc ? dfldc : dfld;
+  a.f[0].k_off = 0;
+  a.f[0].kmin = 1;
+  a.f[0].kmax = 1;
+  a.f[0].posdef = posdef;
+  a.out = c->d_scratch;
+  a.kdm = 1;
+  CK(hyc::launch_advect_tiles(advtyp, a, 1, c->shape, c->stream), "advem kernel");
+  CK(hyc::launch_copy_back(a, 1, c->stream), "advem copy");
+  if (where == HYC_HOST)
+    CK(cudaMemcpyAsync(fld, c->d_tmp, sl * 8, cudaMemcpyDeviceToHost, c->stream), "advem d2h");
+  CK(cudaStreamSynchronize(c->stream), "advem");
+  return HYC_OK;
+}
+
+int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, double *xmin, double *xmax) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (!p || m < 1 || m > 2 || n < 1 || n > 2) return fail(c, HYC_ERR_ARG, "hyc_tsadvc: bad m/n/params");
+  const int at = p->advtyp < 0 ? -p->advtyp : p->advtyp;
+  if (!valid_advtyp(at)) return fail(c, HYC_ERR_ADVTYP, "advem called with advtyp = %d", p->advtyp);
+  if (c->nbdy < kMbdy[at])
+    return fail(c, HYC_ERR_NBDY, "nbdy (dimensions.h) must be at least %d for advtyp %d", kMbdy[at], at);
+  if (p->isopyc) return fail(c, HYC_ERR_UNSUPPORTED, "isopycnic (nhybrd=0) mode is not supported");
+  if (at == 2 && p->btrmas) return fail(c, HYC_ERR_UNSUPPORTED, "advem_fct2c (btrmas) not available");
+  if (p->ntracr < 0 || (p->ntracr > 0 && !p->trcflg)) return fail(c, HYC_ERR_ARG, "ntracr/trcflg");
+  const int kk = c->kdm;
+  const long long sl = c->slice;
+  Field *F = c->fields;
+  auto need = [&](int id, int64_t nel, const char *name) -> int {
+    if (!F[id].dev) return fail(c, HYC_ERR_FIELD, "field %s is not bound", name);
+    if (F[id].nelem < nel) return fail(c, HYC_ERR_FIELD, "field %s has %lld elements, needs %lld", name,
+                                       (long long)F[id].nelem, (long long)nel);
+    return HYC_OK;
+  };
+  const bool use_temp = p->advflg == 0 && p->nhybrd >= 1;
+  const bool use_th3d = p->advflg == 1 && p->hybrid && p->nhybrd >= 1;
+  int rc;
+  if ((rc = need(HYC_F_SALN, 2LL * kk * sl, "saln"))) return rc;
+  if ((rc = need(HYC_F_UFLX, (long long)kk * sl, "uflx"))) return rc;
+  if ((rc = need(HYC_F_VFLX, (long long)kk * sl, "vflx"))) return rc;
+  if ((rc = need(HYC_F_DP, 2LL * kk * sl, "dp"))) return rc;
+  if (use_temp && (rc = need(HYC_F_TEMP, 2LL * kk * sl, "temp"))) return rc;
+  if (use_th3d && (rc = need(HYC_F_TH3D, 2LL * kk * sl, "th3d"))) return rc;
+  if (p->ntracr > 0 && (rc = need(HYC_F_TRACER, 2LL * kk * sl * p->ntracr, "tracer"))) return rc;
+  if (p->mxlmy && ((rc = need(HYC_F_Q2, 2LL * (kk + 2) * sl, "q2")) || (rc = need(HYC_F_Q2L, 2LL * (kk + 2) * sl, "q2l"))))
+    return rc;
+  if (p->btrmas && (rc = need(HYC_F_ONETA, 2LL * sl, "oneta"))) return rc;
+  DeviceGuard g(c->device);
+  cudaStream_t s = c->stream;
+  const int mm = m - 1, nn = n - 1;
+
+  // halo refresh, mod_tsadvc.F90:1827-1840 (dp halo is up to date on entry)
+  const int l = kMbdy[at];
+  auto halo = [&](int id, int nlev) -> cudaError_t {
+    if (!F[id].dev) return cudaSuccess;
+    return hyc::launch_xctilr(F[id].dev, sl, nlev, c->idm, c->jdm, c->nbdy, c->ld1, l, l, c->nreg, s);
+  };
+  CK(halo(HYC_F_SALN, 2 * kk), "xctilr saln");
+  CK(halo(HYC_F_TEMP, 2 * kk), "xctilr temp");
+  CK(halo(HYC_F_TH3D, 2 * kk), "xctilr th3d");
+  CK(halo(HYC_F_UFLX, kk), "xctilr uflx");
+  CK(halo(HYC_F_VFLX, kk), "xctilr vflx");
+  if (p->ntracr > 0)
+    CK(hyc::launch_xctilr(F[HYC_F_TRACER].dev, sl, 2 * kk * p->ntracr, c->idm, c->jdm, c->nbdy, c->ld1, l, l,
+                          c->nreg, s), "xctilr tracer");
+  if (p->mxlmy) {
+    CK(halo(HYC_F_Q2, 2 * kk + 4), "xctilr q2");
+    CK(halo(HYC_F_Q2L, 2 * kk + 4), "xctilr q2l");
+  }
+
+  // field list in the reference's call order (mod_tsadvc.F90:1969-2048)
+  std::vector<FieldDesc> fl;
+  auto add = [&](double *base, long long lev, int koff, int kmin, int kmax, double posdef) {
+    FieldDesc d;
+    memset(&d, 0, sizeof d);
+    d.nbase = base + (long long)nn * lev;
+    d.mbase = base + (long long)mm * lev;
+    d.k_off = koff;
+    d.kmin = kmin;
+    d.kmax = kmax;
+    d.posdef = posdef;
+    fl.push_back(d);
+  };
+  const double pdzero = 0.0, pdtemp = 256.0, pdth3d = 32.0, pdq2 = 1.0;  // :1761-1763
+  const int nh = p->nhybrd < kk ? p->nhybrd : kk;
+  if (use_temp) add(F[HYC_F_TEMP].dev, (long long)kk * sl, 0, 1, nh, pdtemp);
+  if (use_th3d) add(F[HYC_F_TH3D].dev, (long long)kk * sl, 0, 1, nh, pdth3d);
+  add(F[HYC_F_SALN].dev, (long long)kk * sl, 0, 1, kk, pdzero);
+  for (int t = 0; t < p->ntracr; t++)
+    add(F[HYC_F_TRACER].dev + (long long)t * 2 * kk * sl, (long long)kk * sl, 0, 1, kk,
+        p->trcflg[t] == 2 ? pdtemp : pdzero);
+  if (p->mxlmy) {
+    add(F[HYC_F_Q2].dev, (long long)(kk + 2) * sl, 1, 1, kk, pdq2);
+    add(F[HYC_F_Q2L].dev, (long long)(kk + 2) * sl, 1, 1, kk, pdq2);
+  }
+
+  TileArgs a;
+  memset(&a, 0, sizeof a);
+  a.ii = c->idm;
+  a.jj = c->jdm;
+  a.nbdy = c->nbdy;
+  a.ld1 = c->ld1;
+  a.ld2 = c->ld2;
+  a.slice = sl;
+  a.ntx = (c->idm + c->shape.tx - 1) / c->shape.tx;
+  a.nty = (c->jdm + c->shape.ty - 1) / c->shape.ty;
+  a.mode = 0;
+  a.msk = c->d_msk;
+  a.scal = c->d_scp2;
+  a.scali = c->d_scp2i;
+  a.uflx = F[HYC_F_UFLX].dev;
+  a.vflx = F[HYC_F_VFLX].dev;
+  a.dpn = F[HYC_F_DP].dev + (long long)nn * kk * sl;
+  a.oneta_n = p->btrmas ? F[HYC_F_ONETA].dev + (long long)nn * sl : nullptr;
+  a.dt2 = p->delt1;
+  a.kdm = kk;
+  const int chunk = hyc::kMaxFields;
+  const int nchunk0 = (int)fl.size() < chunk ? (int)fl.size() : chunk;
+  if ((rc = ensure_scratch(c, (size_t)nchunk0 * kk * sl))) return rc;
+  a.out = c->d_scratch;
+  for (size_t f0 = 0; f0 < fl.size(); f0 += chunk) {
+    int nf = (int)(fl.size() - f0) < chunk ? (int)(fl.size() - f0) : chunk;
+    a.nfld = nf;
+    for (int q = 0; q < nf; q++) a.f[q] = fl[f0 + q];
+    CK(hyc::launch_advect_tiles(at, a, kk, c->shape, s), "advect kernel");
+    CK(hyc::launch_copy_back(a, kk, s), "copy back");
+  }
+
+  // salinity range diagnostic, mod_tsadvc.F90:2065-2084
+  if (xmin && xmax && (p->nstep % 3 == 0 || p->diagno)) {
+    for (int k = 0; k < kk; k++) {
+      c->h_keys[k] = hyc::double_to_key(999.);
+      c->h_keys[kk + k] = hyc::double_to_key(-999.);
+    }
+    CK(cudaMemcpyAsync(c->d_keys, c->h_keys, 2 * kk * sizeof(long long), cudaMemcpyHostToDevice, s), "keys h2d");
+    CK(hyc::launch_saln_range(F[HYC_F_SALN].dev + (long long)nn * kk * sl, a.dpn, c->d_msk, sl, kk, c->idm, c->jdm,
+                              c->nbdy, c->ld1, c->d_keys, s), "saln range");
+    CK(cudaMemcpyAsync(c->h_keys, c->d_keys, 2 * kk * sizeof(long long), cudaMemcpyDeviceToHost, s), "keys d2h");
+    CK(cudaStreamSynchronize(s), "saln range sync");
+    for (int k = 0; k < kk; k++) {
+      xmin[k] = hyc::key_to_double(c->h_keys[k]);
+      xmax[k] = hyc::key_to_double(c->h_keys[kk + k]);
+    }
+  }
+  return HYC_OK;
+}
+
+int hyc_mass_sum(hyc_ctx *c, const double *fld, const double *fc, double *sum) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (!fld || !fc || !sum) return fail(c, HYC_ERR_ARG, "hyc_mass_sum: null pointer");
+  DeviceGuard g(c->device);
+  double *partial = c->d_sum, *res = c->d_sum + 2 * hyc::mass_sum_partials();
+  CK(hyc::launch_mass_sum(fld, fc, c->d_scp2, c->d_msk, c->idm, c->jdm, c->nbdy, c->ld1, partial, res, c->stream),
+     "mass sum");
+  CK(cudaMemcpyAsync(c->h_sum, res, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "mass sum d2h");
+  CK(cudaStreamSynchronize(c->stream), "mass sum sync");
+  *sum = c->h_sum[0];
+  return HYC_OK;
+}
+
+}  // extern "C"

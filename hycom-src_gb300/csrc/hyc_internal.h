@@ -1,0 +1,48 @@
+// hyc_internal.h -- launchers shared between the CUDA translation units and
+// the host layer (hyc_host.cpp).  Not part of the public C ABI.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hyc {
+
+struct FieldDesc;
+struct TileArgs;
+
+// Geometry of a tile launch (chosen by the host, see hyc_host.cpp).
+struct TileShape {
+  int tx, ty;
+};
+
+// Fused advem/tsadvc tile kernel; scheme in {0,1,2,4}.  out receives every
+// interior cell of each (field, layer) slice it processes.
+cudaError_t launch_advect_tiles(int scheme, const TileArgs &a, int nlayers, TileShape shape,
+                                cudaStream_t s);
+size_t advect_tiles_smem(TileShape shape);
+bool advect_tile_shape_ok(TileShape shape);
+
+// Copy the interior of out[(fi*kdm+k)] back into field level n for every
+// (field, layer) the launch processed.
+cudaError_t launch_copy_back(const TileArgs &a, int nlayers, cudaStream_t s);
+
+// xctilr on nlev slices (mod_xc_sm.h:1337-1428).
+cudaError_t launch_xctilr(double *a, long long slice, int nlev, int ii, int jj, int nbdy, int ld1, int mh,
+                          int nh, int nreg, cudaStream_t s);
+
+// Salinity range diagnostic (mod_tsadvc.F90:2065-2084): per layer min/max of
+// saln(:,:,k,n) over interior sea cells with dp(:,:,k,n) > onemm.  keys is
+// a device array of 2*kdm int64 (min keys then max keys).
+cudaError_t launch_saln_range(const double *saln_n, const double *dp_n, const uint8_t *msk, long long slice,
+                              int kdm, int ii, int jj, int nbdy, int ld1, long long *keys, cudaStream_t s);
+double key_to_double(long long k);
+long long double_to_key(double d);
+
+// sum over interior sea cells of fld*(fc+onemu)*scal, two-sum compensated,
+// fixed order.  partial: device scratch of at least mass_sum_partials()
+// doubles*2; result written to *dres (device).
+int mass_sum_partials();
+cudaError_t launch_mass_sum(const double *fld, const double *fc, const double *scal, const uint8_t *msk,
+                            int ii, int jj, int nbdy, int ld1, double *partial, double *dres, cudaStream_t s);
+
+}  // namespace hyc

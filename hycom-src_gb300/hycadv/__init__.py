@@ -1,0 +1,245 @@
+"""hycadv -- Python mirror of HYCOM's tracer-advection interface over libhycadv.
+
+The reference routines and the functions here that stand in for them
+(same names, argument meaning and order):
+
+=====================================  ==========================================
+reference (HYCOM-src)                  here
+=====================================  ==========================================
+``tsadvc(m,n)``  mod_tsadvc.F90:1708   :meth:`Context.tsadvc`
+``advem(...)``   mod_tsadvc.F90:69     :meth:`Context.advem`
+``xctilr(...)``  mod_xc_sm.h:1337      :meth:`Context.xctilr`
+``bigrid(...)``  bigrid.F90:1          :func:`bigrid`
+=====================================  ==========================================
+
+Everything calls the CUDA library through its C ABI (include/hycom_adv.h)
+with ctypes; there is no CPU implementation behind these functions, and a
+missing or unloadable library raises :class:`HycError`.
+
+Array layout is the reference's: a 2-D slice is a C-contiguous array of
+shape (jdm+2*nbdy, idm+2*nbdy) (Fortran column-major (ld1, ld2)).  Arrays on
+the host are numpy float64; arrays on the GPU are torch float64 CUDA tensors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libhycadv.so")
+
+HYC_OK = 0
+ERRORS = {-1: "HYC_ERR_ARG", -2: "HYC_ERR_ADVTYP", -3: "HYC_ERR_NBDY", -4: "HYC_ERR_MASK", -5: "HYC_ERR_CUDA",
+          -6: "HYC_ERR_FIELD", -7: "HYC_ERR_GRID", -8: "HYC_ERR_UNSUPPORTED", -9: "HYC_ERR_NOMEM"}
+HYC_HOST, HYC_DEVICE = 0, 1
+FIELDS = {"temp": 0, "saln": 1, "th3d": 2, "tracer": 3, "uflx": 4, "vflx": 5, "dp": 6, "oneta": 7, "q2": 8,
+          "q2l": 9}
+
+# every symbol the header declares (checked by the CPU tests)
+EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "hyc_set_stream", "hyc_bind_field",
+           "hyc_sync_field", "hyc_synchronize", "hyc_tsadvc", "hyc_advem", "hyc_xctilr", "hyc_mass_sum",
+           "hyc_version")
+
+
+class HycError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class TsadvcParams(C.Structure):
+    _fields_ = [("advtyp", C.c_int32), ("advflg", C.c_int32), ("btrmas", C.c_int32), ("ntracr", C.c_int32),
+                ("nhybrd", C.c_int32), ("isopyc", C.c_int32), ("hybrid", C.c_int32), ("mxlmy", C.c_int32),
+                ("nstep", C.c_int32), ("diagno", C.c_int32), ("delt1", C.c_double),
+                ("trcflg", C.POINTER(C.c_int32))]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libhycadv.so; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise HycError(-5, f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32)
+        L.hyc_version.restype = C.c_char_p
+        L.hyc_bigrid.argtypes = [C.c_int32, C.c_int32, C.c_int32, dp] + [ip] * 8 + [ip]
+        L.hyc_adv_init.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, ip, ip, ip,
+                                   dp, dp, C.c_int32]
+        L.hyc_adv_finalize.argtypes = [vp]
+        L.hyc_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+        L.hyc_set_stream.argtypes = [vp, vp]
+        L.hyc_bind_field.argtypes = [vp, C.c_int32, vp, C.c_int64, C.c_int32]
+        L.hyc_sync_field.argtypes = [vp, C.c_int32, C.c_int32]
+        L.hyc_synchronize.argtypes = [vp]
+        L.hyc_tsadvc.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(TsadvcParams), dp, dp]
+        L.hyc_advem.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp, vp, C.c_double, vp, vp, C.c_double, C.c_int32,
+                                C.c_int32]
+        L.hyc_xctilr.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+        L.hyc_mass_sum.argtypes = [vp, vp, vp, dp]
+        _lib = L
+    return _lib
+
+
+def version() -> str:
+    return lib().hyc_version().decode()
+
+
+def _err(h=None) -> str:
+    buf = C.create_string_buffer(512)
+    lib().hyc_last_error(h, buf, 512)
+    return buf.value.decode(errors="replace")
+
+
+def _check(rc: int, h=None):
+    if rc != HYC_OK:
+        raise HycError(rc, _err(h))
+
+
+def _i32(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def _f64(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ptr(a):
+    """(pointer, where) of a numpy array (host) or a torch CUDA tensor (device)."""
+    if a is None:
+        return None, HYC_HOST
+    if isinstance(a, np.ndarray):
+        if not (a.flags["C_CONTIGUOUS"] and a.dtype == np.float64):
+            raise HycError(-1, "host arrays must be C-contiguous float64")
+        return a.ctypes.data, HYC_HOST
+    import torch
+
+    if isinstance(a, torch.Tensor):
+        if not (a.is_contiguous() and a.dtype == torch.float64):
+            raise HycError(-1, "tensors must be contiguous float64")
+        return a.data_ptr(), (HYC_DEVICE if a.is_cuda else HYC_HOST)
+    raise TypeError(type(a))
+
+
+def bigrid(depth: np.ndarray, nbdy: int = 6):
+    """bigrid.F90 for one tile: returns (depth_after, masks, nreg).
+
+    masks has ip, iu, iv, iq, ipim1, ipip1, ipjm1, ipjp1 (int32, (ld2, ld1)).
+    """
+    d, dptr = _f64(np.array(depth, dtype=np.float64, copy=True))
+    ld2, ld1 = d.shape
+    idm, jdm = ld1 - 2 * nbdy, ld2 - 2 * nbdy
+    names = ("ip", "iu", "iv", "iq", "ipim1", "ipip1", "ipjm1", "ipjp1")
+    masks = {k: np.zeros((ld2, ld1), np.int32) for k in names}
+    nreg = C.c_int32(-1)
+    _check(lib().hyc_bigrid(idm, jdm, nbdy, dptr, *[_i32(masks[k])[1] for k in names], C.byref(nreg)))
+    return d, masks, nreg.value
+
+
+class Context:
+    """One basin on one GPU: the state tsadvc reads from mod_dimensions/mod_cb_arrays."""
+
+    def __init__(self, idm, jdm, kdm, nbdy, nreg, ip, iu, iv, scp2, scp2i, device: int = 0):
+        L = lib()
+        self.idm, self.jdm, self.kdm, self.nbdy, self.nreg = idm, jdm, kdm, nbdy, nreg
+        self.ld1, self.ld2 = idm + 2 * nbdy, jdm + 2 * nbdy
+        self.slice = self.ld1 * self.ld2
+        h = C.c_void_p()
+        keep = [_i32(ip), _i32(iu), _i32(iv), _f64(scp2), _f64(scp2i)]
+        _check(L.hyc_adv_init(C.byref(h), idm, jdm, kdm, nbdy, nreg, keep[0][1], keep[1][1], keep[2][1], keep[3][1],
+                              keep[4][1], device))
+        self._h = h
+        self._bound = {}
+
+    @classmethod
+    def from_masks(cls, masks: dict, scp2, scp2i, kdm: int, nreg: int, nbdy: int = 6, device: int = 0):
+        ld2, ld1 = masks["ip"].shape
+        return cls(ld1 - 2 * nbdy, ld2 - 2 * nbdy, kdm, nbdy, nreg, masks["ip"], masks["iu"], masks["iv"], scp2,
+                   scp2i, device)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().hyc_adv_finalize(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- fields -------------------------------------------------------------
+    def bind(self, name: str, array):
+        """Bind a model field: a torch CUDA tensor is used in place; a numpy
+        array gets a resident device mirror (move data with :meth:`sync`)."""
+        p, where = _ptr(array)
+        n = array.size if isinstance(array, np.ndarray) else array.numel()
+        _check(lib().hyc_bind_field(self._h, FIELDS[name], p, n, where), self._h)
+        self._bound[name] = array
+
+    def sync(self, name: str, to_device: bool):
+        _check(lib().hyc_sync_field(self._h, FIELDS[name], int(bool(to_device))), self._h)
+
+    def synchronize(self):
+        _check(lib().hyc_synchronize(self._h), self._h)
+
+    def set_stream(self, stream):
+        """Queue later work on a torch.cuda.Stream (or a raw cudaStream_t int)."""
+        ptr = stream if isinstance(stream, int) else stream.cuda_stream
+        _check(lib().hyc_set_stream(self._h, C.c_void_p(ptr)), self._h)
+
+    # -- the reference's routines --------------------------------------------
+    def tsadvc(self, m: int, n: int, *, delt1: float, advtyp: int = 2, advflg: int = 0, btrmas: bool = False,
+               ntracr: int = 0, trcflg=None, nhybrd: int | None = None, isopyc: bool = False, mxlmy: bool = False,
+               nstep: int = 1, diagno: bool = False, range_diag: bool = False):
+        """tsadvc(m,n) on the bound fields.  Returns (xmin, xmax) of salinity
+        per layer when range_diag and the diagnostic runs, else None."""
+        nh = self.kdm if nhybrd is None else nhybrd
+        tf = np.ascontiguousarray(trcflg if trcflg is not None else np.zeros(max(ntracr, 1)), np.int32)
+        p = TsadvcParams(advtyp=advtyp, advflg=advflg, btrmas=int(btrmas), ntracr=ntracr, nhybrd=nh,
+                         isopyc=int(isopyc), hybrid=int(nh > 0), mxlmy=int(mxlmy), nstep=nstep, diagno=int(diagno),
+                         delt1=float(delt1), trcflg=tf.ctypes.data_as(C.POINTER(C.c_int32)))
+        if range_diag:
+            xmin = np.zeros(self.kdm)
+            xmax = np.zeros(self.kdm)
+            _check(lib().hyc_tsadvc(self._h, m, n, C.byref(p), xmin.ctypes.data_as(C.POINTER(C.c_double)),
+                                    xmax.ctypes.data_as(C.POINTER(C.c_double))), self._h)
+            return xmin, xmax
+        _check(lib().hyc_tsadvc(self._h, m, n, C.byref(p), None, None), self._h)
+        return None
+
+    def advem(self, advtyp, fld, fldc, u, v, fco, fcn, posdef, scal, scali, dt2, btrmas=False):
+        """advem on one slice; all arrays numpy (host) or all torch CUDA (device)."""
+        arrs = [fld, fldc, u, v, fco, fcn, scal, scali]
+        ptrs = [_ptr(a) for a in arrs]
+        wheres = {w for (p, w), a in zip(ptrs, arrs) if a is not None}
+        if len(wheres) != 1:
+            raise HycError(-1, "advem arrays must all be host or all device")
+        where = wheres.pop()
+        p = [pp for pp, _ in ptrs]
+        _check(lib().hyc_advem(self._h, int(advtyp), p[0], p[1], p[2], p[3], p[4], p[5], float(posdef), p[6], p[7],
+                               float(dt2), int(bool(btrmas)), where), self._h)
+
+    def xctilr(self, a, mh: int, nh: int):
+        p, where = _ptr(a)
+        nlev = int(np.prod(a.shape[:-2])) if len(a.shape) > 2 else 1
+        _check(lib().hyc_xctilr(self._h, p, nlev, mh, nh, where), self._h)
+
+    def mass_sum(self, fld, fc) -> float:
+        """sum over interior sea cells of fld*(fc+onemu)*scp2 (device tensors)."""
+        out = C.c_double(0.0)
+        _check(lib().hyc_mass_sum(self._h, _ptr(fld)[0], _ptr(fc)[0], C.byref(out)), self._h)
+        return out.value

@@ -1,0 +1,181 @@
+/*
+ * hycom_adv.h -- C ABI of the GB300 tracer-advection library (libhycadv.so).
+ *
+ * Drop-in for HYCOM's layered tracer advection, module mod_tsadvc:
+ *   tsadvc(m,n)                         mod_tsadvc.F90:1708  (public entry)
+ *   advem(advtyp,fld,fldc,u,v,fco,fcn,  mod_tsadvc.F90:69-79 (module-private
+ *         posdef,scal,scali,dt2,btrmas)                      scheme driver)
+ *   xctilr(a,l1,ld,mh,nh,itype)         mod_xc_sm.h:1337      (halo fill)
+ *   bigrid / indxi / indxj              bigrid.F90:1,417,475  (masks)
+ *
+ * Every array uses the reference's memory layout: a 2-D slice is the
+ * Fortran array a(1-nbdy:idm+nbdy, 1-nbdy:jdm+nbdy) stored column-major
+ * (i fastest), ld1 = idm+2*nbdy, ld2 = jdm+2*nbdy, and the pointer passed
+ * points at element (1-nbdy,1-nbdy).  3-D/4-D fields are slices stacked as
+ * in mod_cb_arrays.F90 (e.g. temp(:,:,k,t) at slice index (k-1)+(t-1)*kdm).
+ * Time levels m, n are the reference's 1-based indices.
+ *
+ * All functions return HYC_OK (0) or a negative HYC_ERR_* code; the text of
+ * the last error of a context is available from hyc_last_error().  Where
+ * the reference would stop the model (xcstop for a bad advtyp,
+ * mod_tsadvc.F90:160-165, or nbdy < mbdy, :1817-1825) the library returns
+ * an error instead.  No CPU fallback exists: without a usable GPU every
+ * compute call fails with HYC_ERR_CUDA.
+ */
+#ifndef HYCOM_ADV_H
+#define HYCOM_ADV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HYC_OK 0
+#define HYC_ERR_ARG -1         /* bad argument (null pointer, size, level) */
+#define HYC_ERR_ADVTYP -2      /* advtyp not in {0,1,2,4}, mod_tsadvc.F90:149-166 */
+#define HYC_ERR_NBDY -3        /* nbdy < mbdy_advtyp(advtyp), mod_tsadvc.F90:1817 */
+#define HYC_ERR_MASK -4        /* iu/iv inconsistent with ip (bigrid.F90:216-252) */
+#define HYC_ERR_CUDA -5        /* CUDA runtime error or no device */
+#define HYC_ERR_FIELD -6       /* a field tsadvc needs is not bound */
+#define HYC_ERR_GRID -7        /* bigrid: 1-point sea, arctic row, ms overflow */
+#define HYC_ERR_UNSUPPORTED -8 /* option outside this library's scope */
+#define HYC_ERR_NOMEM -9       /* device allocation failed */
+
+/* where a pointer lives */
+#define HYC_HOST 0
+#define HYC_DEVICE 1
+
+/* field identifiers for hyc_bind_field (mod_cb_arrays.F90 names) */
+#define HYC_F_TEMP 0   /* temp(ld1,ld2,kdm,2)              */
+#define HYC_F_SALN 1   /* saln(ld1,ld2,kdm,2)              */
+#define HYC_F_TH3D 2   /* th3d(ld1,ld2,kdm,2)              */
+#define HYC_F_TRACER 3 /* tracer(ld1,ld2,kdm,2,ntracr)     */
+#define HYC_F_UFLX 4   /* uflx(ld1,ld2,kdm)                */
+#define HYC_F_VFLX 5   /* vflx(ld1,ld2,kdm)                */
+#define HYC_F_DP 6     /* dp(ld1,ld2,kdm,2)                */
+#define HYC_F_ONETA 7  /* oneta(ld1,ld2,2), read if btrmas */
+#define HYC_F_Q2 8     /* q2(ld1,ld2,0:kdm+1,2), if mxlmy  */
+#define HYC_F_Q2L 9    /* q2l(ld1,ld2,0:kdm+1,2), if mxlmy */
+#define HYC_NFIELDS 10
+
+typedef struct hyc_ctx hyc_ctx;
+
+/* Run-time switches of tsadvc (blkdat.F90:865-911, :1260-1300, :1485). */
+typedef struct hyc_tsadvc_params {
+  int32_t advtyp;  /* 0 PCM, 1 MPDATA, 2 FCT2, 4 FCT4                  */
+  int32_t advflg;  /* 0 advect temp and saln, 1 advect th3d and saln    */
+  int32_t btrmas;  /* barotropic mass flag (FCT2 becomes fct2c)        */
+  int32_t ntracr;  /* number of tracers in the bound tracer array       */
+  int32_t nhybrd;  /* number of hybrid layers                           */
+  int32_t isopyc;  /* isopycnic mode (nhybrd==0): unsupported, must be 0 */
+  int32_t hybrid;  /* nhybrd > 0                                        */
+  int32_t mxlmy;   /* Mellor-Yamada mixed layer: also advect q2, q2l   */
+  int32_t nstep;   /* model step; the salinity range diagnostic runs when
+                      mod(nstep,3)==0 or diagno (mod_tsadvc.F90:2065)   */
+  int32_t diagno;
+  double delt1;    /* leapfrog time step (2*baclin), passed as dt2      */
+  const int32_t *trcflg; /* host array of ntracr flags; 2 = temperature-like */
+} hyc_tsadvc_params;
+
+/*
+ * Build the land/sea masks from depth, as bigrid does for a single tile
+ * (bigrid.F90:1-415; no arctic fold, no f-plane).  depth (ld1*ld2, metres,
+ * >0 is sea) is modified in place exactly like bigrid (halo filled, land
+ * borders).  Outputs (each ld1*ld2 int32, any may be NULL except ip/iu/iv):
+ * ip, iu, iv, iq and the sea-only neighbour indices ipim1/ipip1/ipjm1/ipjp1
+ * (Fortran index values).  *nreg receives 0 (closed) or 1 (periodic in x).
+ * Replaces: bigrid.F90:1 (subroutine bigrid) plus geopar.F90:256 call site.
+ */
+int hyc_bigrid(int32_t idm, int32_t jdm, int32_t nbdy, double *depth, int32_t *ip, int32_t *iu,
+               int32_t *iv, int32_t *iq, int32_t *ipim1, int32_t *ipip1, int32_t *ipjm1, int32_t *ipjp1,
+               int32_t *nreg);
+
+/*
+ * Create a context bound to one GPU: grid sizes, nreg (mod_xc: 0 closed,
+ * 1 periodic-x/closed-y, 3 periodic in both), masks ip/iu/iv and the grid
+ * metrics scp2/scp2i (all host arrays of ld1*ld2).  The masks and metrics
+ * are copied to the device and stay resident.  Replaces the module state
+ * that tsadvc reads through `use mod_dimensions, mod_cb_arrays`
+ * (mod_tsadvc.F90:15, :1709).
+ */
+int hyc_adv_init(hyc_ctx **ctx, int32_t idm, int32_t jdm, int32_t kdm, int32_t nbdy, int32_t nreg,
+                 const int32_t *ip, const int32_t *iu, const int32_t *iv, const double *scp2,
+                 const double *scp2i, int32_t device);
+
+/* Release everything the context owns. */
+int hyc_adv_finalize(hyc_ctx *ctx);
+
+/* Copy the last error message of ctx (or of the library when ctx is NULL). */
+int hyc_last_error(const hyc_ctx *ctx, char *buf, size_t n);
+
+/* Use this CUDA stream (a cudaStream_t passed as void*) for later calls. */
+int hyc_set_stream(hyc_ctx *ctx, void *stream);
+
+/*
+ * Bind a model field (HYC_F_*) of nelem doubles.  where = HYC_DEVICE: ptr
+ * is device memory owned by the caller and is used in place.  where =
+ * HYC_HOST: ptr is the caller's host array; the library allocates a
+ * resident device mirror, and hyc_sync_field moves data between them.
+ */
+int hyc_bind_field(hyc_ctx *ctx, int32_t field, void *ptr, int64_t nelem, int32_t where);
+
+/* Copy a host-bound field: to_device=1 host->device mirror, 0 back. */
+int hyc_sync_field(hyc_ctx *ctx, int32_t field, int32_t to_device);
+
+/* Wait for all work queued on the context's stream. */
+int hyc_synchronize(hyc_ctx *ctx);
+
+/*
+ * tsadvc(m,n), advection part (mod_tsadvc.F90:1708-2132 with temdf2=0):
+ * halo fill of the advected fields (as :1829-1840), thickness prep
+ * (:1905-1942), advem on every active field of every layer, and the
+ * salinity range diagnostic.  Works on the bound (device-resident) fields;
+ * xmin/xmax (host, kdm each, may be NULL) receive the per-layer salinity
+ * minimum/maximum when the diagnostic runs (mod_tsadvc.F90:2065-2084).
+ * Asynchronous on the context stream unless xmin/xmax are requested.
+ * Replaces: mod_tsadvc.F90:1708 (subroutine tsadvc), call site
+ * mod_hycom.F90:2536.
+ */
+int hyc_tsadvc(hyc_ctx *ctx, int32_t m, int32_t n, const hyc_tsadvc_params *p, double *xmin,
+               double *xmax);
+
+/*
+ * advem on one 2-D slice (mod_tsadvc.F90:69-79, same argument meaning):
+ * fld (in/out, old level in, new level out on sea points of the interior),
+ * fldc (center level), u, v (mass fluxes), fco, fcn (old/new thickness),
+ * posdef, scal, scali (metrics), dt2, btrmas.  All pointers are host
+ * (where = HYC_HOST) or device (where = HYC_DEVICE) arrays of ld1*ld2
+ * doubles.  The grid and masks are those of ctx.  Synchronous.
+ * Replaces: mod_tsadvc.F90:69 (subroutine advem).
+ */
+int hyc_advem(hyc_ctx *ctx, int32_t advtyp, double *fld, const double *fldc, const double *u,
+              const double *v, const double *fco, const double *fcn, double posdef, const double *scal,
+              const double *scali, double dt2, int32_t btrmas, int32_t where);
+
+/*
+ * xctilr on nlev consecutive slices of a (mod_xc_sm.h:1337-1428): fill the
+ * halo mh wide in i and nh wide in j with vland=0 (closed) or a periodic
+ * copy, according to the context's nreg.  where = HYC_HOST or HYC_DEVICE.
+ * Replaces: mod_xc_sm.h:1337 (subroutine xctilr), single-tile form.
+ */
+int hyc_xctilr(hyc_ctx *ctx, double *a, int32_t nlev, int32_t mh, int32_t nh, int32_t where);
+
+/*
+ * Tracer content sum over sea points of the interior,
+ *   sum_{i,j} fld(i,j) * (fc(i,j) + onemu) * scp2(i,j),
+ * accumulated on the device in FP64 with compensated (two-sum) partials
+ * and a fixed reduction order, so the result is reproducible run to run.
+ * This is the quantity FCT/PCM conserve (mod_tsadvc.F90:788, :976).
+ * fld, fc: device arrays of one slice.  Result in *sum.  Synchronous.
+ */
+int hyc_mass_sum(hyc_ctx *ctx, const double *fld, const double *fc, double *sum);
+
+/* Library build identification, e.g. "hycadv 0.1 sm_103a". */
+const char *hyc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYCOM_ADV_H */

@@ -1,0 +1,154 @@
+"""ctypes front end of the CPU oracle (oracle/hyc_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
+benchmark's CPU-baseline leg.  The product path never imports it.
+
+Arrays follow the reference layout (see hyc_oracle.c): numpy float64 / int32,
+C-contiguous, a 2-D slice has shape (ld2, ld1) = (jdm+2*nbdy, idm+2*nbdy).
+Parity unpinned: there are no reference golden vectors for this path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libhyc_oracle.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (see oracle/Makefile)."""
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
+            os.path.join(_HERE, "hyc_oracle.c")):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        dp = C.POINTER(C.c_double)
+        ip = C.POINTER(C.c_int32)
+        L.hyo_grid_create.restype = C.c_void_p
+        L.hyo_grid_create.argtypes = [C.c_int, C.c_int, C.c_int, dp, dp, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.hyo_grid_free.argtypes = [C.c_void_p]
+        L.hyo_grid_nreg.argtypes = [C.c_void_p]
+        L.hyo_grid_masks.argtypes = [C.c_void_p] + [ip] * 7
+        L.hyo_grid_work.argtypes = [C.c_void_p, C.c_char_p, dp]
+        L.hyo_set_threads.argtypes = [C.c_void_p, C.c_int]
+        L.hyo_max_threads.restype = C.c_int
+        L.hyo_xctilr.argtypes = [C.c_void_p, dp, C.c_int, C.c_int, C.c_int]
+        L.hyo_advem.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp, dp, C.c_double, dp, dp, C.c_double, C.c_int]
+        L.hyo_tsadvc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int] + [dp] * 12
+        L.hyo_xcsum.restype = C.c_double
+        L.hyo_xcsum.argtypes = [C.c_void_p, dp, ip]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "oracle arrays must be C-contiguous"
+    if a.dtype == np.float64:
+        return a.ctypes.data_as(C.POINTER(C.c_double))
+    if a.dtype == np.int32:
+        return a.ctypes.data_as(C.POINTER(C.c_int32))
+    raise TypeError(a.dtype)
+
+
+class _TsParams(C.Structure):
+    _fields_ = [("kdm", C.c_int), ("advtyp", C.c_int), ("advflg", C.c_int), ("btrmas", C.c_int),
+                ("ntracr", C.c_int), ("nhybrd", C.c_int), ("isopyc", C.c_int), ("hybrid", C.c_int),
+                ("mxlmy", C.c_int), ("nstep", C.c_int), ("diagno", C.c_int), ("delt1", C.c_double),
+                ("trcflg", C.POINTER(C.c_int32))]
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class Grid:
+    """bigrid + the module work arrays of mod_tsadvc for one basin."""
+
+    def __init__(self, depth: np.ndarray, scp2: np.ndarray, scp2i: np.ndarray, nbdy: int = 6,
+                 threads: int = 0):
+        L = lib()
+        self.nbdy = nbdy
+        self.ld2, self.ld1 = depth.shape
+        self.idm = self.ld1 - 2 * nbdy
+        self.jdm = self.ld2 - 2 * nbdy
+        self.depth = np.ascontiguousarray(depth, dtype=np.float64).copy()
+        err = C.c_int(0)
+        nfill = C.c_int(0)
+        h = L.hyo_grid_create(self.idm, self.jdm, nbdy, _p(self.depth),
+                              _p(np.ascontiguousarray(scp2, np.float64)),
+                              _p(np.ascontiguousarray(scp2i, np.float64)), C.byref(err), C.byref(nfill))
+        if not h:
+            raise OracleError(f"hyo_grid_create failed: err={err.value} one-point seas={nfill.value}")
+        self._h = C.c_void_p(h)
+        self.scp2 = np.ascontiguousarray(scp2, np.float64)
+        self.scp2i = np.ascontiguousarray(scp2i, np.float64)
+        self.nreg = L.hyo_grid_nreg(self._h)
+        shp = (self.ld2, self.ld1)
+        m = {k: np.zeros(shp, np.int32) for k in ("ip", "iu", "iv", "ipim1", "ipip1", "ipjm1", "ipjp1")}
+        L.hyo_grid_masks(self._h, *[_p(m[k]) for k in ("ip", "iu", "iv", "ipim1", "ipip1", "ipjm1", "ipjp1")])
+        self.masks = m
+        if threads:
+            self.set_threads(threads)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib is not None:
+            _lib.hyo_grid_free(h)
+            self._h = None
+
+    def set_threads(self, n: int):
+        lib().hyo_set_threads(self._h, int(n))
+
+    def xctilr(self, a: np.ndarray, mh: int, nh: int):
+        nlev = int(np.prod(a.shape[:-2])) if a.ndim > 2 else 1
+        lib().hyo_xctilr(self._h, _p(a), nlev, mh, nh)
+
+    def advem(self, advtyp, fld, fldc, u, v, fco, fcn, posdef, scal, scali, dt2, btrmas=False):
+        rc = lib().hyo_advem(self._h, int(advtyp), _p(fld), _p(fldc), _p(u), _p(v), _p(fco), _p(fcn),
+                             float(posdef), _p(scal), _p(scali), float(dt2), int(bool(btrmas)))
+        if rc != 0:
+            raise OracleError(f"advem rc={rc}")
+
+    def work(self, name: str) -> np.ndarray:
+        out = np.empty((self.ld2, self.ld1), np.float64)
+        if lib().hyo_grid_work(self._h, name.encode(), _p(out)) != 0:
+            raise KeyError(name)
+        return out
+
+    def xcsum(self, a: np.ndarray, mask: np.ndarray) -> float:
+        return lib().hyo_xcsum(self._h, _p(a), _p(np.ascontiguousarray(mask, np.int32)))
+
+    def tsadvc(self, m: int, n: int, *, temp, saln, th3d, uflx, vflx, dp, delt1, advtyp=2, advflg=0,
+               btrmas=False, tracer=None, trcflg=None, nhybrd=None, isopyc=False, mxlmy=False, q2=None,
+               q2l=None, oneta=None, nstep=1, diagno=False):
+        kdm = temp.shape[1]
+        ntr = 0 if tracer is None else tracer.shape[0]
+        tf = np.ascontiguousarray(trcflg if trcflg is not None else np.zeros(max(ntr, 1)), np.int32)
+        p = _TsParams(kdm=kdm, advtyp=advtyp, advflg=advflg, btrmas=int(btrmas), ntracr=ntr,
+                      nhybrd=kdm if nhybrd is None else nhybrd, isopyc=int(isopyc),
+                      hybrid=int((kdm if nhybrd is None else nhybrd) > 0), mxlmy=int(mxlmy), nstep=nstep,
+                      diagno=int(diagno), delt1=float(delt1), trcflg=_p(tf))
+        xmin = np.zeros(kdm)
+        xmax = np.zeros(kdm)
+        rc = lib().hyo_tsadvc(self._h, C.byref(p), m, n, _p(temp), _p(saln), _p(th3d), _p(tracer), _p(uflx),
+                              _p(vflx), _p(dp), _p(oneta), _p(q2), _p(q2l), _p(xmin), _p(xmax))
+        if rc != 0:
+            raise OracleError(f"tsadvc rc={rc}")
+        return xmin, xmax
+
+
+def max_threads() -> int:
+    return lib().hyo_max_threads()

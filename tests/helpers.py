@@ -1,0 +1,52 @@
+"""Shared builders for the tests: synthetic basins, oracle grids, cases."""
+from __future__ import annotations
+
+import numpy as np
+
+from hycadv import synth
+from oracle import oracle as O
+
+
+def basin(nx, ny, periodic, seed):
+    return synth.make_basin(nx, ny, periodic, seed)
+
+
+def oracle_grid(b, threads=0):
+    scp2, scp2i = b.metrics()
+    return O.Grid(b.depth, scp2, scp2i, nbdy=b.nbdy, threads=threads)
+
+
+def np_case(b, g, kdm, ntracr, seed, courant, delt1, passive=True):
+    """Case as numpy arrays (CPU), keyed like the oracle's tsadvc arguments."""
+    c = synth.build_case(b, g.masks, kdm=kdm, ntracr=ntracr, seed=seed, courant=courant, delt1=delt1,
+                         device="cpu", passive=passive)
+    out = {k: getattr(c, k).numpy().copy() for k in ("temp", "saln", "th3d", "uflx", "vflx", "dp")}
+    out["tracer"] = c.tracer.numpy().copy() if ntracr > 0 else None
+    out["scp2"] = c.scp2.numpy().copy()
+    out["scp2i"] = c.scp2i.numpy().copy()
+    return out
+
+
+def levels(step):
+    """(m, n) of HYCOM_Run for a step counted from 1 (mod_hycom.F90:2254-2255),
+    shifted so that the first step reads level 1 as time t."""
+    m = ((step + 1) % 2) + 1
+    n = (step % 2) + 1
+    return m, n
+
+
+def same(a, b):
+    """Bitwise-equal values (treating -0.0 == +0.0) and identical NaN positions."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return bool(np.array_equal(np.isnan(a), np.isnan(b)) and np.all((a == b) | (np.isnan(a) & np.isnan(b))))
+
+
+def max_rel(a, b, mask=None):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if mask is not None:
+        a = a[..., mask]
+        b = b[..., mask]
+    den = max(np.abs(b).max(), 1e-300)
+    return float(np.abs(a - b).max() / den)
