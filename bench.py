@@ -1,0 +1,398 @@
+#!/usr/bin/env python
+"""Benchmark of the tracer-advection hot path (tsadvc/advem) on GB300.
+
+Workload (default): periodic-in-x ocean basin 4500 x 3298 x 41 layers,
+temperature and salinity, FCT2 (advtyp=2), plain FP64, max Courant 0.8,
+delt1 = 240 s -- seeded synthetic fields with HYCOM's units and layouts
+(no real region data exists here).  One step = one tsadvc(m,n) call over
+all layers and both fields (leapfrog levels alternate).  The metric counts
+dense interior cell*layer*tracer updates per step.
+
+Arms:
+  default            the CUDA library through its C ABI, fields resident on
+                     the GPU (value), plus an end-to-end run with host
+                     buffers copied in and out every step (e2e) and the CPU
+                     oracle timed on a bounded sample (cpu_baseline).
+  --impl reference   the reference's algorithm on the host cores: the CPU
+                     restatement of mod_tsadvc (oracle/), OpenMP over all
+                     cores, on a bounded sample of the same workload.
+
+Multi-GPU (torchrun): every rank advects its own basin replica (basins are
+independent, no data-path collective), so scaling is weak; the timed region
+is bracketed by barriers and the max time over ranks is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "hycom-src_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "cell·layer·tracer updates/s, FP32-mixed batched vs FP64 plain @≤1e-6 err; %HBM"
+UNIT = "updates/s"
+WORKLOADS = {
+    # periodic-x basin, T+S, FCT2/FCT4/MPDATA, FP64
+    "c1": dict(nx=4500, ny=3298, kdm=41, periodic=True, courant=0.8, delt1=240.0, seed=1),
+    # closed basin 257x193x10, T+S, FCT2, FP64 (CPU-sized case)
+    "c0": dict(nx=257, ny=193, kdm=10, periodic=False, courant=0.5, delt1=1800.0, seed=7),
+}
+SCHEME_NAMES = {0: "PCM", 1: "MPDATA", 2: "FCT2", 4: "FCT4"}
+FALLBACK_HBM_GBS = 6800.0
+
+
+def bytes_per_update(s_t: int, s_f: int, s_dp: int, ntr: int, kdm: int) -> float:
+    """Minimal DRAM bytes per cell*layer*tracer update: read fld(n), fld(m),
+    write fld(n) per tracer; uflx, vflx, dp(n) per cell-layer shared by the
+    tracers; scp2, scp2i (8+8) and the ip/iu/iv masks (1 byte each) per cell."""
+    return 3 * s_t + (2 * s_f + s_dp) / ntr + 19.0 / (kdm * ntr)
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(kernel_key: str):
+    """DRAM bytes per launch recorded in profiles/ by an ncu capture, or None."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith((".txt", ".md")):
+            continue
+        try:
+            lines = open(os.path.join(d, fn)).read().splitlines()
+        except Exception:
+            continue
+        for ln in lines:
+            ln = ln.strip().strip("`")
+            if ln.startswith(f"traffic_bytes_per_launch[{kernel_key}]:"):
+                try:
+                    return float(ln.split(":", 1)[1].split()[0])
+                except Exception:
+                    return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(self.idx)], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p is not None:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+                self.out = ""
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in (self.out or "").splitlines():
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_workload(wl: dict, device):
+    """Basin, masks (product bigrid) and the full tsadvc state on device."""
+    import hycadv
+    from hycadv import synth
+
+    b = synth.make_basin(wl["nx"], wl["ny"], wl["periodic"], wl["seed"])
+    depth, masks, nreg = hycadv.bigrid(b.depth, b.nbdy)
+    case = synth.build_case(b, masks, kdm=wl["kdm"], ntracr=0, seed=wl["seed"], courant=wl["courant"],
+                            delt1=wl["delt1"], device=device)
+    return b, masks, nreg, case
+
+
+def run_cpu_sample(wl: dict, nlayers: int, min_seconds: float, steps_max: int, warmup: int, advtyp: int,
+                   threads: int, gen_device, min_steps: int = 1):
+    """Time the CPU oracle (OpenMP, `threads`) on the workload's basin with
+    `nlayers` layers; returns (updates/s, description, steps timed)."""
+    import numpy as np
+
+    from hycadv import synth
+    from oracle import oracle
+
+    b = synth.make_basin(wl["nx"], wl["ny"], wl["periodic"], wl["seed"])
+    sc, si = b.metrics()
+    g = oracle.Grid(b.depth, sc, si, nbdy=b.nbdy, threads=threads)
+    c = synth.build_case(b, g.masks, kdm=nlayers, ntracr=0, seed=wl["seed"], courant=wl["courant"],
+                         delt1=wl["delt1"], device=gen_device)
+    h = {k: getattr(c, k).cpu().numpy().copy() for k in ("temp", "saln", "th3d", "uflx", "vflx", "dp")}
+    del c
+    ups = b.nx * b.ny * nlayers * 2
+
+    def step(s):
+        m, n = ((s + 1) % 2) + 1, (s % 2) + 1
+        g.tsadvc(m, n, temp=h["temp"], saln=h["saln"], th3d=h["th3d"], uflx=h["uflx"], vflx=h["vflx"], dp=h["dp"],
+                 delt1=wl["delt1"], advtyp=advtyp, nstep=s)
+
+    for s in range(1, warmup + 1):
+        step(s)
+    t0 = time.perf_counter()
+    n = 0
+    while n < steps_max and (n < min_steps or time.perf_counter() - t0 < min_seconds):
+        n += 1
+        step(warmup + n)
+    dt = time.perf_counter() - t0
+    desc = (f"{b.nx}x{b.ny} basin of the workload, {nlayers} of {wl['kdm']} layers, T+S, "
+            f"{SCHEME_NAMES[advtyp]}, {n} timed steps after {warmup} warm-up")
+    return ups * n / dt, desc, n, dt
+
+
+def reference_arm(args, wl):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    import torch
+
+    from oracle import oracle
+
+    oracle.build()
+    threads = os.cpu_count() or 1
+    gen_dev = "cuda:0" if torch.cuda.is_available() else "cpu"
+    rate, desc, n, dt = run_cpu_sample(wl, nlayers=args.ref_layers, min_seconds=0.0, steps_max=args.steps,
+                                       warmup=args.warmup, advtyp=args.advtyp, threads=threads, gen_device=gen_dev,
+                                       min_steps=args.steps)
+    line = {
+        "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": ws, "steps": n, "warmup": args.warmup,
+        "ms_per_step": dt * 1e3 / max(n, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generator, HYCOM units/layout)", "impl": "reference",
+        "config": config_of(args, wl),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_of(args, wl):
+    return {"workload": f"{args.workload}: {'periodic-x' if wl['periodic'] else 'closed'} basin "
+                        f"{wl['nx']}x{wl['ny']}x{wl['kdm']}, T+S, {SCHEME_NAMES[args.advtyp]} "
+                        f"(advtyp={args.advtyp}), FP64 plain, max Courant {wl['courant']}, delt1 {wl['delt1']} s",
+            "form": "fp64-plain", "updates_per_step": wl["nx"] * wl["ny"] * wl["kdm"] * 2,
+            "l2": "inputs larger than L2 (full model state resident in HBM, ~40 GB)" if args.workload == "c1"
+            else "small case, fits in L2", "parallelism": "independent basin replica per GPU"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS))
+    ap.add_argument("--advtyp", type=int, default=2, choices=[0, 1, 2, 4])
+    ap.add_argument("--layers", type=int, default=0, help="override kdm (smaller profiling case)")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--ref-layers", type=int, default=4, help="layers in the CPU sample")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    wl = dict(WORKLOADS[args.workload])
+    if args.layers > 0:
+        wl["kdm"] = args.layers
+    if args.impl == "reference":
+        return reference_arm(args, wl)
+
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_setup()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+
+    import build as hbuild
+
+    hbuild.build()
+    import hycadv
+
+    b, masks, nreg, case = make_workload(wl, dev)
+    sc, si = b.metrics()
+    kdm = wl["kdm"]
+    ctx = hycadv.Context.from_masks(masks, sc, si, kdm=kdm, nreg=nreg, nbdy=b.nbdy, device=local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream)
+    for k in ("temp", "saln", "th3d", "uflx", "vflx", "dp"):
+        ctx.bind(k, getattr(case, k))
+    delt1 = wl["delt1"]
+
+    def step(s):
+        m, n = ((s + 1) % 2) + 1, (s % 2) + 1
+        ctx.tsadvc(m, n, delt1=delt1, advtyp=args.advtyp, nstep=s)
+
+    for s in range(1, args.warmup + 1):
+        step(s)
+    torch.cuda.synchronize(dev)
+    ctx.enable_timers(True)
+    ctx.stats(reset=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for s in range(args.warmup + 1, args.warmup + args.steps + 1):
+            step(s)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    st = ctx.stats(reset=True)
+    ctx.enable_timers(False)
+    if dist:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ups_step = wl["nx"] * wl["ny"] * kdm * 2
+    value = ups_step * args.steps * ws / (ms / 1e3)
+    ms_step = ms / args.steps
+
+    # roofline of the dominant kernel (fused advection tiles), timed live
+    adv_ms, adv_calls = st["advect"]
+    bpu = bytes_per_update(8, 8, 8, 2, kdm)
+    peak, peak_kind = peak_hbm()
+    roof = None
+    if adv_calls > 0:
+        avg_s = adv_ms / adv_calls / 1e3
+        achieved = ups_step * bpu / avg_s / 1e9
+        tr = profile_traffic(f"fct2_fp64_{args.workload}")
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": tr, "peak_kind": peak_kind, "kernel": "advect_tile_kernel",
+                "algorithmic_bytes_per_update": bpu, "avg_launch_ms": adv_ms / adv_calls,
+                "share_of_step": adv_ms / max(st["tsadvc"][0], 1e-9),
+                "note": "FP64 form is FP64-ALU bound on GB300 (FP64 pipe ~1/72 of FP32); see DESIGN.md"}
+    clocks = clk.summary()
+
+    # end-to-end through the C ABI with host buffers (pinned), copies in the timed region
+    e2e = None
+    if not args.no_e2e:
+        ctx2 = hycadv.Context.from_masks(masks, sc, si, kdm=kdm, nreg=nreg, nbdy=b.nbdy, device=local)
+        ctx2.set_stream(stream)
+        host = {}
+        for k in ("temp", "saln", "uflx", "vflx", "dp"):
+            t = torch.empty(getattr(case, k).shape, dtype=torch.float64, pin_memory=True)
+            t.copy_(getattr(case, k))
+            host[k] = t
+            ctx2.bind(k, t)
+        h2d = sum(host[k].numel() * 8 for k in host)
+        d2h = (host["temp"].numel() + host["saln"].numel()) * 8
+        del case
+        torch.cuda.empty_cache()
+
+        def e2e_step(s):
+            for k in host:
+                ctx2.sync(k, True)
+            m, n = ((s + 1) % 2) + 1, (s % 2) + 1
+            ctx2.tsadvc(m, n, delt1=delt1, advtyp=args.advtyp, nstep=s)
+            ctx2.sync("temp", False)
+            ctx2.sync("saln", False)
+
+        e2e_step(1)
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for s in range(2, 2 + args.e2e_steps):
+            e2e_step(s)
+        f1.record(stream)
+        torch.cuda.synchronize(dev)
+        ems = f0.elapsed_time(f1)
+        if dist:
+            t = torch.tensor([ems], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ems = float(t.item())
+        e2e = {"value": ups_step * args.e2e_steps * ws / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
+               "note": "hyc_sync_field H2D of temp, saln, uflx, vflx, dp (whole arrays) + tsadvc + D2H of temp, saln"}
+        ctx2.close()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, desc, n, _ = run_cpu_sample(wl, nlayers=args.ref_layers, min_seconds=args.cpu_seconds, steps_max=20,
+                                          warmup=1, advtyp=args.advtyp, threads=threads, gen_device=dev)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, HYCOM units/layout)",
+            "config": config_of(args, wl), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(st["launches"]), "clocks": clocks,
+            "timers_ms": {k: v for k, v in st.items() if k != "launches"},
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

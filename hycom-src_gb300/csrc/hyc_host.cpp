@@ -48,6 +48,15 @@ struct hyc_ctx {
   double *h_sum = nullptr;      // pinned
   hyc::TileShape shape{32, 16};
   std::string err;
+  // timers (HYC_T_*) and launch accounting
+  bool timing = false;
+  struct Pending {
+    int slot;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  hyc_stats stats{};
 };
 
 namespace {
@@ -132,9 +141,69 @@ void host_halo(T *a, int ii, int jj, int nb, int ld1, int nreg) {
     }
 }
 
+cudaEvent_t get_event(hyc_ctx *c) {
+  if (!c->event_pool.empty()) {
+    cudaEvent_t e = c->event_pool.back();
+    c->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Bracket a region of stream work with events when timers are on.
+struct Timed {
+  hyc_ctx *c;
+  int slot;
+  cudaEvent_t a = nullptr;
+  Timed(hyc_ctx *c_, int s) : c(c_), slot(s) {
+    if (c->timing) {
+      a = get_event(c);
+      cudaEventRecord(a, c->stream);
+    }
+  }
+  ~Timed() {
+    if (c->timing && a) {
+      cudaEvent_t b = get_event(c);
+      cudaEventRecord(b, c->stream);
+      c->pending.push_back({slot, a, b});
+    }
+  }
+};
+
+void fold_timings(hyc_ctx *c) {
+  for (auto &p : c->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      c->stats.ms[p.slot] += ms;
+      c->stats.calls[p.slot] += 1;
+    }
+    c->event_pool.push_back(p.a);
+    c->event_pool.push_back(p.b);
+  }
+  c->pending.clear();
+}
+
 }  // namespace
 
 extern "C" {
+
+int hyc_enable_timers(hyc_ctx *c, int32_t on) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  c->timing = on != 0;
+  return HYC_OK;
+}
+
+int hyc_get_stats(hyc_ctx *c, hyc_stats *out, int32_t reset) {
+  if (!c || !out) return fail(c, HYC_ERR_ARG, "hyc_get_stats: null argument");
+  DeviceGuard g(c->device);
+  CK(cudaStreamSynchronize(c->stream), "stats sync");
+  fold_timings(c);
+  *out = c->stats;
+  if (reset) c->stats = hyc_stats{};
+  return HYC_OK;
+}
 
 const char *hyc_version(void) { return "hycadv 0.1 sm_103a"; }
 
@@ -239,6 +308,8 @@ int hyc_adv_init(hyc_ctx **out, int32_t idm, int32_t jdm, int32_t kdm, int32_t n
     for (int i = 1 - nb; i <= ii + nb; i++) {
       long long o = off(c, i, j);
       bool p = ip[o] != 0, u = iu[o] != 0, v = iv[o] != 0;
+      // the outermost halo column/row cannot be checked (no i-1 / j-1) and
+      // is never read by the kernels
       if (i > 1 - nb) {
         bool want = p && ip[o - 1] != 0;
         if (u != want) {
@@ -246,10 +317,6 @@ int hyc_adv_init(hyc_ctx **out, int32_t idm, int32_t jdm, int32_t kdm, int32_t n
           delete c;
           return rc;
         }
-      } else if (u) {
-        int rc = fail(nullptr, HYC_ERR_MASK, "iu(%d,%d) set on the outer halo column", i, j);
-        delete c;
-        return rc;
       }
       if (j > 1 - nb) {
         bool want = p && ip[o - c->ld1] != 0;
@@ -258,10 +325,6 @@ int hyc_adv_init(hyc_ctx **out, int32_t idm, int32_t jdm, int32_t kdm, int32_t n
           delete c;
           return rc;
         }
-      } else if (v) {
-        int rc = fail(nullptr, HYC_ERR_MASK, "iv(%d,%d) set on the outer halo row", i, j);
-        delete c;
-        return rc;
       }
       m[o] = (p ? hyc::kIP : 0) | (u ? hyc::kIU : 0) | (v ? hyc::kIV : 0);
     }
@@ -310,6 +373,11 @@ int hyc_adv_finalize(hyc_ctx *c) {
     cudaFree(c->d_tmp);
     cudaFree(c->d_keys);
     cudaFree(c->d_sum);
+    for (auto &p : c->pending) {
+      cudaEventDestroy(p.a);
+      cudaEventDestroy(p.b);
+    }
+    for (auto e : c->event_pool) cudaEventDestroy(e);
     if (c->h_keys) cudaFreeHost(c->h_keys);
     if (c->h_sum) cudaFreeHost(c->h_sum);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -376,7 +444,9 @@ int hyc_xctilr(hyc_ctx *c, double *a, int32_t nlev, int32_t mh, int32_t nh, int3
   if (!a || nlev < 1) return fail(c, HYC_ERR_ARG, "hyc_xctilr: bad arguments");
   DeviceGuard g(c->device);
   if (where == HYC_DEVICE) {
+    Timed t(c, HYC_T_XCTILR);
     CK(hyc::launch_xctilr(a, c->slice, nlev, c->idm, c->jdm, c->nbdy, c->ld1, mh, nh, c->nreg, c->stream), "xctilr");
+    c->stats.launches += (nlev + 65534) / 65535;
     return HYC_OK;
   }
   // host array: stage one slice at a time through the staging buffer
@@ -386,6 +456,7 @@ int hyc_xctilr(hyc_ctx *c, double *a, int32_t nlev, int32_t mh, int32_t nh, int3
     CK(cudaMemcpyAsync(c->d_tmp, h, c->slice * 8, cudaMemcpyHostToDevice, c->stream), "h2d");
     CK(hyc::launch_xctilr(c->d_tmp, c->slice, 1, c->idm, c->jdm, c->nbdy, c->ld1, mh, nh, c->nreg, c->stream),
        "xctilr");
+    c->stats.launches += 1;
     CK(cudaMemcpyAsync(h, c->d_tmp, c->slice * 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
   }
   CK(cudaStreamSynchronize(c->stream), "xctilr sync");
@@ -450,8 +521,12 @@ int hyc_advem(hyc_ctx *c, int32_t advtyp, double *fld, const double *fldc, const
   a.f[0].posdef = posdef;
   a.out = c->d_scratch;
   a.kdm = 1;
-  CK(hyc::launch_advect_tiles(advtyp, a, 1, c->shape, c->stream), "advem kernel");
+  {
+    Timed t(c, HYC_T_ADVECT);
+    CK(hyc::launch_advect_tiles(advtyp, a, 1, c->shape, c->stream), "advem kernel");
+  }
   CK(hyc::launch_copy_back(a, 1, c->stream), "advem copy");
+  c->stats.launches += 2;
   if (where == HYC_HOST)
     CK(cudaMemcpyAsync(fld, c->d_tmp, sl * 8, cudaMemcpyDeviceToHost, c->stream), "advem d2h");
   CK(cudaStreamSynchronize(c->stream), "advem");
@@ -493,24 +568,31 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
   DeviceGuard g(c->device);
   cudaStream_t s = c->stream;
   const int mm = m - 1, nn = n - 1;
+  Timed t_all(c, HYC_T_TSADVC);
 
   // halo refresh, mod_tsadvc.F90:1827-1840 (dp halo is up to date on entry)
   const int l = kMbdy[at];
   auto halo = [&](int id, int nlev) -> cudaError_t {
     if (!F[id].dev) return cudaSuccess;
+    c->stats.launches += (nlev + 65534) / 65535;
     return hyc::launch_xctilr(F[id].dev, sl, nlev, c->idm, c->jdm, c->nbdy, c->ld1, l, l, c->nreg, s);
   };
+  {
+  Timed t_halo(c, HYC_T_XCTILR);
   CK(halo(HYC_F_SALN, 2 * kk), "xctilr saln");
   CK(halo(HYC_F_TEMP, 2 * kk), "xctilr temp");
   CK(halo(HYC_F_TH3D, 2 * kk), "xctilr th3d");
   CK(halo(HYC_F_UFLX, kk), "xctilr uflx");
   CK(halo(HYC_F_VFLX, kk), "xctilr vflx");
-  if (p->ntracr > 0)
+  if (p->ntracr > 0) {
+    c->stats.launches += (2 * kk * p->ntracr + 65534) / 65535;
     CK(hyc::launch_xctilr(F[HYC_F_TRACER].dev, sl, 2 * kk * p->ntracr, c->idm, c->jdm, c->nbdy, c->ld1, l, l,
                           c->nreg, s), "xctilr tracer");
+  }
   if (p->mxlmy) {
     CK(halo(HYC_F_Q2, 2 * kk + 4), "xctilr q2");
     CK(halo(HYC_F_Q2L, 2 * kk + 4), "xctilr q2l");
+  }
   }
 
   // field list in the reference's call order (mod_tsadvc.F90:1969-2048)
@@ -567,8 +649,15 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
     int nf = (int)(fl.size() - f0) < chunk ? (int)(fl.size() - f0) : chunk;
     a.nfld = nf;
     for (int q = 0; q < nf; q++) a.f[q] = fl[f0 + q];
-    CK(hyc::launch_advect_tiles(at, a, kk, c->shape, s), "advect kernel");
-    CK(hyc::launch_copy_back(a, kk, s), "copy back");
+    {
+      Timed t(c, HYC_T_ADVECT);
+      CK(hyc::launch_advect_tiles(at, a, kk, c->shape, s), "advect kernel");
+    }
+    {
+      Timed t(c, HYC_T_COPY);
+      CK(hyc::launch_copy_back(a, kk, s), "copy back");
+    }
+    c->stats.launches += 2;
   }
 
   // salinity range diagnostic, mod_tsadvc.F90:2065-2084
@@ -578,8 +667,12 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
       c->h_keys[kk + k] = hyc::double_to_key(-999.);
     }
     CK(cudaMemcpyAsync(c->d_keys, c->h_keys, 2 * kk * sizeof(long long), cudaMemcpyHostToDevice, s), "keys h2d");
-    CK(hyc::launch_saln_range(F[HYC_F_SALN].dev + (long long)nn * kk * sl, a.dpn, c->d_msk, sl, kk, c->idm, c->jdm,
-                              c->nbdy, c->ld1, c->d_keys, s), "saln range");
+    {
+      Timed t(c, HYC_T_DIAG);
+      CK(hyc::launch_saln_range(F[HYC_F_SALN].dev + (long long)nn * kk * sl, a.dpn, c->d_msk, sl, kk, c->idm,
+                                c->jdm, c->nbdy, c->ld1, c->d_keys, s), "saln range");
+    }
+    c->stats.launches += 1;
     CK(cudaMemcpyAsync(c->h_keys, c->d_keys, 2 * kk * sizeof(long long), cudaMemcpyDeviceToHost, s), "keys d2h");
     CK(cudaStreamSynchronize(s), "saln range sync");
     for (int k = 0; k < kk; k++) {
@@ -597,6 +690,7 @@ int hyc_mass_sum(hyc_ctx *c, const double *fld, const double *fc, double *sum) {
   double *partial = c->d_sum, *res = c->d_sum + 2 * hyc::mass_sum_partials();
   CK(hyc::launch_mass_sum(fld, fc, c->d_scp2, c->d_msk, c->idm, c->jdm, c->nbdy, c->ld1, partial, res, c->stream),
      "mass sum");
+  c->stats.launches += 2;
   CK(cudaMemcpyAsync(c->h_sum, res, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "mass sum d2h");
   CK(cudaStreamSynchronize(c->stream), "mass sum sync");
   *sum = c->h_sum[0];

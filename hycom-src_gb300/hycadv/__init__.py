@@ -40,13 +40,18 @@ FIELDS = {"temp": 0, "saln": 1, "th3d": 2, "tracer": 3, "uflx": 4, "vflx": 5, "d
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "hyc_set_stream", "hyc_bind_field",
            "hyc_sync_field", "hyc_synchronize", "hyc_tsadvc", "hyc_advem", "hyc_xctilr", "hyc_mass_sum",
-           "hyc_version")
+           "hyc_version", "hyc_enable_timers", "hyc_get_stats")
+TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4}
 
 
 class HycError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"{ERRORS.get(code, code)}: {msg}")
         self.code = code
+
+
+class Stats(C.Structure):
+    _fields_ = [("launches", C.c_int64), ("calls", C.c_int64 * 8), ("ms", C.c_double * 8)]
 
 
 class TsadvcParams(C.Structure):
@@ -82,6 +87,8 @@ def lib() -> C.CDLL:
                                 C.c_int32]
         L.hyc_xctilr.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         L.hyc_mass_sum.argtypes = [vp, vp, vp, dp]
+        L.hyc_enable_timers.argtypes = [vp, C.c_int32]
+        L.hyc_get_stats.argtypes = [vp, C.POINTER(Stats), C.c_int32]
         _lib = L
     return _lib
 
@@ -212,7 +219,7 @@ class Context:
         p = TsadvcParams(advtyp=advtyp, advflg=advflg, btrmas=int(btrmas), ntracr=ntracr, nhybrd=nh,
                          isopyc=int(isopyc), hybrid=int(nh > 0), mxlmy=int(mxlmy), nstep=nstep, diagno=int(diagno),
                          delt1=float(delt1), trcflg=tf.ctypes.data_as(C.POINTER(C.c_int32)))
-        if range_diag:
+        if range_diag and (nstep % 3 == 0 or diagno):  # mod_tsadvc.F90:2065
             xmin = np.zeros(self.kdm)
             xmax = np.zeros(self.kdm)
             _check(lib().hyc_tsadvc(self._h, m, n, C.byref(p), xmin.ctypes.data_as(C.POINTER(C.c_double)),
@@ -237,6 +244,18 @@ class Context:
         p, where = _ptr(a)
         nlev = int(np.prod(a.shape[:-2])) if len(a.shape) > 2 else 1
         _check(lib().hyc_xctilr(self._h, p, nlev, mh, nh, where), self._h)
+
+    def enable_timers(self, on: bool = True):
+        _check(lib().hyc_enable_timers(self._h, int(bool(on))), self._h)
+
+    def stats(self, reset: bool = False) -> dict:
+        """Kernel launches and device-time per timer slot (ms, calls)."""
+        s = Stats()
+        _check(lib().hyc_get_stats(self._h, C.byref(s), int(bool(reset))), self._h)
+        out = {"launches": int(s.launches)}
+        for name, i in TIMERS.items():
+            out[name] = (float(s.ms[i]), int(s.calls[i]))
+        return out
 
     def mass_sum(self, fld, fc) -> float:
         """sum over interior sea cells of fld*(fc+onemu)*scp2 (device tensors)."""

@@ -172,6 +172,30 @@ int hyc_xctilr(hyc_ctx *ctx, double *a, int32_t nlev, int32_t mh, int32_t nh, in
  */
 int hyc_mass_sum(hyc_ctx *ctx, const double *fld, const double *fc, double *sum);
 
+/*
+ * Timers and launch counts, the counterpart of the reference's wall-clock
+ * timers xctmr0/xctmr1/xctmrp (mod_xc_sm.h:1431-1627; timer 41 = tsadvc,
+ * mod_hycom.F90:1146, timer 12 = xctilr).  When enabled, every timed
+ * region is bracketed by CUDA events on the context stream, so the times
+ * are device times.  Timer slots: HYC_T_*.
+ */
+#define HYC_T_TSADVC 0 /* whole hyc_tsadvc call (device span)   */
+#define HYC_T_XCTILR 1 /* halo fills                            */
+#define HYC_T_ADVECT 2 /* fused advection kernels               */
+#define HYC_T_COPY 3   /* copy of updated slices into level n   */
+#define HYC_T_DIAG 4   /* salinity range diagnostic             */
+#define HYC_NTIMERS 8
+
+typedef struct hyc_stats {
+  int64_t launches;            /* kernels launched by this context      */
+  int64_t calls[HYC_NTIMERS];  /* timed regions completed per slot      */
+  double ms[HYC_NTIMERS];      /* accumulated device milliseconds       */
+} hyc_stats;
+
+int hyc_enable_timers(hyc_ctx *ctx, int32_t on);
+/* Wait for the stream, fold finished timings in, copy out; reset=1 zeroes. */
+int hyc_get_stats(hyc_ctx *ctx, hyc_stats *out, int32_t reset);
+
 /* Library build identification, e.g. "hycadv 0.1 sm_103a". */
 const char *hyc_version(void);
 

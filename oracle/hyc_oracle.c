@@ -1303,7 +1303,8 @@ int hyo_tsadvc(hyo_grid *g, const hyo_tsparams *p, int m, int n, double *temp, d
 /* xcsum: mod_xc_sm.h:900-963 (row sums in 2*nbdy+1 strips, then serial) */
 double hyo_xcsum(const hyo_grid *g, const double *a, const int32_t *mask) {
   const int idm = g->ii, jdm = g->jj, w = 2 * g->nbdy + 1;
-  double *sj = (double *)malloc((size_t)jdm * sizeof(double));
+  if (jdm < 1) return 0.0;
+  double *sj = (double *)calloc((size_t)jdm, sizeof(double));
   if (!sj) return NAN;
   for (int j = 1; j <= jdm; j++) {
     double s8 = 0.0;
