@@ -1,0 +1,277 @@
+// hyc_fct.cuh -- FP64 FCT2/FCT4 tile kernel tuned for GB300's FP64 pipe.
+//
+// Same stages and arithmetic as the generic tile kernel (hyc_tile.cuh; map to
+// mod_tsadvc.F90:645-997 for FCT2 and :1370-1706 for FCT4), reorganised so
+// that two CTAs fit on an SM (the FP64 pipe needs more resident warps to
+// hide its latency than one 256-thread CTA gives):
+//   * 15 shared arrays instead of 19: fmxlo/fmnlo overwrite fld/fldc in
+//     place once fld and fldc are dead, and fqmax/fqmin live in registers of
+//     the thread that later updates the same output cell;
+//   * fco+onemu is formed once per cell (the reference forms it per field);
+//   * the stage loops have compile-time bounds and are unrolled, so a
+//     thread's cells interleave (more independent FP64 work in flight).
+// Only sea cells of the interior are written to the output slice.
+#pragma once
+#include "hyc_args.h"
+#include "hyc_device.cuh"
+
+namespace hyc {
+
+template <int TX, int TY>
+struct FctGeom {
+  static constexpr int RX = TX + 6, RY = TY + 6, N = RX * RY;
+  static constexpr int NARR = 15;  // U V FCN HO HN RH SCL SCI | FLD FLDC FX FY FLO RP RM
+  static constexpr size_t smem_bytes = (size_t)NARR * N * sizeof(double) + ((N + 15) / 16) * 16;
+};
+
+// Compile-time rectangle [A0,A1) x [B0,B1) of a region of width RX, spread
+// over 256 threads; f(a, b, e, it) with e = b*RX + a and it the iteration.
+template <int RX, int A0, int A1, int B0, int B1, class F>
+__device__ __forceinline__ void rect(F &&f) {
+  constexpr int W = A1 - A0;
+  constexpr int NN = W * (B1 - B0);
+  constexpr int IT = (NN + 255) / 256;
+#pragma unroll
+  for (int it = 0; it < IT; it++) {
+    const int t = threadIdx.x + it * 256;
+    if (NN % 256 == 0 || t < NN) {
+      const int bb = t / W;
+      const int aa = t - bb * W;
+      f(A0 + aa, B0 + bb, (B0 + bb) * RX + A0 + aa, it);
+    }
+  }
+}
+
+template <int SCHEME, int TX, int TY>
+__global__ void __launch_bounds__(256, 2) fct_tile_kernel(const TileArgs A) {
+  using G = FctGeom<TX, TY>;
+  constexpr int RX = G::RX, RY = G::RY, N = G::N;
+  constexpr int NOUT_IT = (TX * TY + 255) / 256;
+  extern __shared__ __align__(16) double sm[];
+  double *U = sm, *V = U + N, *FCN = V + N, *HO = FCN + N, *HN = HO + N, *RH = HN + N, *SCL = RH + N,
+         *SCI = SCL + N;
+  double *FLD = SCI + N, *FLDC = FLD + N, *FX = FLDC + N, *FY = FX + N, *FLO = FY + N, *RP = FLO + N,
+         *RM = RP + N;
+  uint8_t *MSK = reinterpret_cast<uint8_t *>(RM + N);
+
+  const int tile = blockIdx.x;
+  const int k = blockIdx.y;
+  const int tyi = tile / A.ntx, txi = tile - tyi * A.ntx;
+  const int ib0 = 1 + txi * TX - 3, jb0 = 1 + tyi * TY - 3;  // region origin (Fortran index)
+  const int nb = A.nbdy, ld1 = A.ld1, ii = A.ii, jj = A.jj;
+  const long long sl = A.slice;
+  const double dt2 = A.dt2;
+
+  // ---- per-layer inputs ------------------------------------------------------
+  {
+    const double *uk = A.mode == 0 ? A.uflx + k * sl : A.uflx;
+    const double *vk = A.mode == 0 ? A.vflx + k * sl : A.vflx;
+    for (int t = threadIdx.x; t < N; t += 256) {
+      const int bb = t / RX, aa = t - bb * RX;
+      const int i = ib0 + aa, j = jb0 + bb;
+      const bool in = (i >= 1 - nb) && (i <= ii + nb) && (j >= 1 - nb) && (j <= jj + nb);
+      const long long o = in ? (long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1 : 0;
+      MSK[t] = in ? A.msk[o] : 0;
+      U[t] = in ? uk[o] : 0.0;
+      V[t] = in ? vk[o] : 0.0;
+      SCL[t] = in ? A.scal[o] : 1.0;
+      SCI[t] = in ? A.scali[o] : 1.0;
+      if (A.mode == 0) {
+        FCN[t] = in ? A.dpn[k * sl + o] : 0.0;            // dp(:,:,k,n)
+        HO[t] = (in && A.oneta_n) ? A.oneta_n[o] : 1.0;   // onetamas(:,:,m)
+      } else {
+        HO[t] = in ? A.fco[o] : 0.0;
+        FCN[t] = in ? A.fcn[o] : 0.0;
+      }
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < N; t += 256) {
+    const int bb = t / RX, aa = t - bb * RX;
+    double fco, fcn;
+    if (A.mode == 0) {  // mod_tsadvc.F90:1931-1938
+      const double o = HO[t] * FCN[t];
+      double fdv = 0.0;
+      if (aa < RX - 1 && bb < RY - 1) fdv = ((U[t + 1] - U[t]) + (V[t + RX] - V[t])) * dt2 * SCI[t];
+      fco = kmax(o + fdv, 0.0);
+      fcn = kmax(o, 0.0);
+    } else {
+      fco = HO[t];
+      fcn = FCN[t];
+    }
+    const double hn = fcn + kOnemu;
+    FCN[t] = fcn;
+    HO[t] = fco + kOnemu;
+    HN[t] = hn;
+    RH[t] = __drcp_rn(hn);
+  }
+  __syncthreads();
+
+  const double qdt2 = 1.0 / dt2;  // mod_tsadvc.F90:865
+  for (int fi = 0; fi < A.nfld; fi++) {
+    const FieldDesc fd = A.f[fi];
+    if (k + 1 > fd.kmax || k + 1 < fd.kmin) continue;
+    const double *fn = fd.nbase + (long long)(k + fd.k_off) * sl;
+    const double *fm = fd.mbase + (long long)(k + fd.k_off) * sl;
+    double *out = A.out + ((long long)fi * A.kdm + k) * sl;
+    for (int t = threadIdx.x; t < N; t += 256) {
+      const int bb = t / RX, aa = t - bb * RX;
+      const int i = ib0 + aa, j = jb0 + bb;
+      const bool in = (i >= 1 - nb) && (i <= ii + nb) && (j >= 1 - nb) && (j <= jj + nb);
+      const long long o = in ? (long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1 : 0;
+      FLD[t] = in ? fn[o] : 0.0;
+      FLDC[t] = in ? fm[o] : 0.0;
+      FX[t] = 0.0;
+      FY[t] = 0.0;
+    }
+    __syncthreads();
+
+    // S1: upwind fluxes, :686-720 (zero on faces that are not sea-sea)
+    rect<RX, 1, RX, 1, RY - 1>([&](int a, int b, int e, int) {
+      if (MSK[e] & kIU) {
+        const double uu = U[e];
+        FX[e] = uu * (ge0(uu) ? FLD[e - 1] : FLD[e]);
+      }
+    });
+    rect<RX, 1, RX - 1, 1, RY>([&](int a, int b, int e, int) {
+      if (MSK[e] & kIV) {
+        const double vv = V[e];
+        FY[e] = vv * (ge0(vv) ? FLD[e - RX] : FLD[e]);
+      }
+    });
+    __syncthreads();
+
+    // S2: low-order solution on [1,RX-1)^2, :778-791
+    rect<RX, 1, RX - 1, 1, RY - 1>([&](int a, int b, int e, int) {
+      const uint8_t m = MSK[e];
+      if (!(m & kIP)) return;
+      const double c = FLD[e];
+      const double w = (MSK[e - 1] & kIP) ? FLD[e - 1] : c;
+      const double ea = (MSK[e + 1] & kIP) ? FLD[e + 1] : c;
+      const double s = (MSK[e - RX] & kIP) ? FLD[e - RX] : c;
+      const double n = (MSK[e + RX] & kIP) ? FLD[e + RX] : c;
+      const double fmx = kmax(kmax(kmax(kmax(c, w), ea), s), n);
+      const double fmn = kmin(kmin(kmin(kmin(c, w), ea), s), n);
+      const double fdv = ((FX[e + 1] - FX[e]) + (FY[e + RX] - FY[e])) * dt2 * SCI[e];
+      const double q = c * HO[e] - fdv;
+      FLO[e] = kmax(fmn, kmin(fmx, div_rcp(q, HN[e], RH[e])));
+    });
+    __syncthreads();
+
+    // S3: antidiffusive fluxes, :817-855 (FCT4: :1528-1580)
+    rect<RX, 2, RX - 1, 2, RY - 2>([&](int a, int b, int e, int) {
+      if (!(MSK[e] & kIU)) return;
+      const double uu = U[e];
+      double fhx;
+      if (SCHEME == kFCT4 && (MSK[e - 1] & kIU) && (MSK[e + 1] & kIU)) {
+        const double ft14 = 7.0 / 12.0, ft24 = -1.0 / 12.0;
+        fhx = uu * (ft14 * (FLDC[e] + FLDC[e - 1]) + ft24 * (FLDC[e + 1] + FLDC[e - 2]));
+      } else {
+        fhx = uu * 0.5 * (FLDC[e] + FLDC[e - 1]);
+      }
+      FX[e] = fhx - FX[e];
+    });
+    rect<RX, 2, RX - 2, 2, RY - 1>([&](int a, int b, int e, int) {
+      if (!(MSK[e] & kIV)) return;
+      const double vv = V[e];
+      double fhy;
+      if (SCHEME == kFCT4 && (MSK[e - RX] & kIV) && (MSK[e + RX] & kIV)) {
+        const double ft14 = 7.0 / 12.0, ft24 = -1.0 / 12.0;
+        fhy = vv * (ft14 * (FLDC[e] + FLDC[e - RX]) + ft24 * (FLDC[e + RX] + FLDC[e - 2 * RX]));
+      } else {
+        fhy = vv * 0.5 * (FLDC[e] + FLDC[e - RX]);
+      }
+      FY[e] = fhy - FY[e];
+    });
+    __syncthreads();
+
+    // fmxlo/fmnlo (:792-793) in place over fld/fldc, now dead
+    rect<RX, 1, RX - 1, 1, RY - 1>([&](int a, int b, int e, int) {
+      if (!(MSK[e] & kIP)) return;
+      const double c = FLD[e], cc = FLDC[e], lo = FLO[e];
+      FLD[e] = kmax(kmax(c, cc), lo);
+      FLDC[e] = kmin(kmin(c, cc), lo);
+    });
+    __syncthreads();
+
+    // S4: Zalesak bounds and ratios, :863-909.  Output cells keep
+    // fqmax/fqmin in registers for S6 (same thread-to-cell map).
+    double qx[NOUT_IT], qn[NOUT_IT];
+    auto zalesak = [&](int e, double &fqmax, double &fqmin) {
+      const bool mw = MSK[e - 1] & kIP, me = MSK[e + 1] & kIP, ms = MSK[e - RX] & kIP, mn = MSK[e + RX] & kIP;
+      fqmax = FLD[e];
+      fqmin = FLDC[e];
+      fqmax = kmax(fqmax, mw ? FLD[e - 1] : FLD[e]);
+      fqmax = kmax(fqmax, me ? FLD[e + 1] : FLD[e]);
+      fqmax = kmax(fqmax, ms ? FLD[e - RX] : FLD[e]);
+      fqmax = kmax(fqmax, mn ? FLD[e + RX] : FLD[e]);
+      fqmin = kmin(fqmin, mw ? FLDC[e - 1] : FLDC[e]);
+      fqmin = kmin(fqmin, me ? FLDC[e + 1] : FLDC[e]);
+      fqmin = kmin(fqmin, ms ? FLDC[e - RX] : FLDC[e]);
+      fqmin = kmin(fqmin, mn ? FLDC[e + RX] : FLDC[e]);
+      // ib=ipip1, jb=ipjp1 (:873-875): land to the E/N -> own face twice
+      const double fxa = FX[e], fxb = me ? FX[e + 1] : FX[e];
+      const double fya = FY[e], fyb = mn ? FY[e + RX] : FY[e];
+      const double famax = pos0(fxa) - neg0(fxb) + pos0(fya) - neg0(fyb);
+      const double famin = pos0(fxb) - neg0(fxa) + pos0(fyb) - neg0(fya);
+      const double lo = FLO[e];
+      double rp = 0.0, rm = 0.0;
+      if (gt0(famax)) {
+        const double qp = (fqmax - lo) * FCN[e] * SCL[e] * qdt2;
+        rp = klt(qp, famax) ? qp / famax : 1.0;
+      }
+      if (gt0(famin)) {
+        const double qm = (lo - fqmin) * FCN[e] * SCL[e] * qdt2;
+        rm = klt(qm, famin) ? qm / famin : 1.0;
+      }
+      RP[e] = rp;
+      RM[e] = rm;
+    };
+    rect<RX, 3, RX - 3, 3, RY - 3>([&](int a, int b, int e, int it) {
+      if (MSK[e] & kIP) zalesak(e, qx[it], qn[it]);
+    });
+    {  // the ring [2,RX-2)^2 minus the output cells: ratios only
+      constexpr int NR = 2 * (RX - 4) + 2 * (RY - 6);
+      static_assert(NR <= 256, "ring larger than the CTA");
+      const int t = threadIdx.x;
+      if (t < NR) {
+        int a, b;
+        if (t < RX - 4) { a = 2 + t; b = 2; }
+        else if (t < 2 * (RX - 4)) { a = 2 + t - (RX - 4); b = RY - 3; }
+        else if (t < 2 * (RX - 4) + (RY - 6)) { a = 2; b = 3 + t - 2 * (RX - 4); }
+        else { a = RX - 3; b = 3 + t - 2 * (RX - 4) - (RY - 6); }
+        const int e = b * RX + a;
+        double dx, dn;
+        if (MSK[e] & kIP) zalesak(e, dx, dn);
+      }
+    }
+    __syncthreads();
+
+    // S5: limit, :922-946
+    rect<RX, 3, RX - 2, 3, RY - 3>([&](int a, int b, int e, int) {
+      if (!(MSK[e] & kIU)) return;
+      const double f = FX[e];
+      const double fact = lt0(f) ? kmin(RP[e - 1], RM[e]) : kmin(RP[e], RM[e - 1]);
+      FX[e] = fact * f;
+    });
+    rect<RX, 3, RX - 3, 3, RY - 2>([&](int a, int b, int e, int) {
+      if (!(MSK[e] & kIV)) return;
+      const double f = FY[e];
+      const double fact = lt0(f) ? kmin(RP[e - RX], RM[e]) : kmin(RP[e], RM[e - RX]);
+      FY[e] = fact * f;
+    });
+    __syncthreads();
+
+    // S6: corrected update of the output cells, :962-982
+    rect<RX, 3, RX - 3, 3, RY - 3>([&](int a, int b, int e, int it) {
+      const int i = ib0 + a, j = jb0 + b;
+      if (i > ii || j > jj || !(MSK[e] & kIP)) return;
+      const double fdv = ((FX[e + 1] - FX[e]) + (FY[e + RX] - FY[e])) * dt2 * SCI[e];
+      const double res = kmax(qn[it], kmin(qx[it], FLO[e] - div_rcp(fdv, HN[e], RH[e])));
+      out[(long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1] = res;
+    });
+    __syncthreads();
+  }
+}
+
+}  // namespace hyc

@@ -6,6 +6,7 @@
 #include <cstring>
 
 #include "hyc_internal.h"
+#include "hyc_fct.cuh"
 #include "hyc_tile.cuh"
 
 namespace hyc {
@@ -13,22 +14,31 @@ namespace hyc {
 // ---------------------------------------------------------------------------
 // fused tile kernels
 // ---------------------------------------------------------------------------
-template <int S, int TX, int TY>
-static cudaError_t launch_one(const TileArgs &a, int nlayers, cudaStream_t s) {
-  using G = TileGeom<TX, TY>;
-  static_assert(G::smem_bytes <= 227 * 1024, "tile does not fit in shared memory");
-  auto kern = advect_tile_kernel<S, TX, TY>;
-  static unsigned long long attr_done = 0;  // one bit per device ordinal < 64
+template <class K>
+static cudaError_t launch_kernel(K kern, size_t smem, const TileArgs &a, int nlayers, cudaStream_t s,
+                                 unsigned long long &attr_done) {
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 64 || !(attr_done >> dev & 1ULL)) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::smem_bytes);
+  if (dev >= 64 || !(attr_done >> dev & 1ULL)) {  // one bit per device ordinal < 64
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (dev < 64) attr_done |= 1ULL << dev;
   }
   dim3 grid((unsigned)(a.ntx * a.nty), (unsigned)nlayers);
-  kern<<<grid, 256, G::smem_bytes, s>>>(a);
+  kern<<<grid, 256, smem, s>>>(a);
   return cudaGetLastError();
+}
+
+template <int S, int TX, int TY>
+static cudaError_t launch_one(const TileArgs &a, int nlayers, cudaStream_t s) {
+  static unsigned long long attr_done = 0;
+  if constexpr (S == kFCT2 || S == kFCT4) {
+    static_assert(FctGeom<TX, TY>::smem_bytes <= 227 * 1024, "tile does not fit in shared memory");
+    return launch_kernel(fct_tile_kernel<S, TX, TY>, FctGeom<TX, TY>::smem_bytes, a, nlayers, s, attr_done);
+  } else {
+    static_assert(TileGeom<TX, TY>::smem_bytes <= 227 * 1024, "tile does not fit in shared memory");
+    return launch_kernel(advect_tile_kernel<S, TX, TY>, TileGeom<TX, TY>::smem_bytes, a, nlayers, s, attr_done);
+  }
 }
 
 template <int TX, int TY>
@@ -76,7 +86,7 @@ __global__ void copy_back_kernel(const TileArgs A) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     int j = (int)(t / A.ii), i = (int)(t - (long long)j * A.ii);
     long long o = (long long)(i + A.nbdy) + (long long)(j + A.nbdy) * A.ld1;
-    dst[o] = src[o];
+    if (A.msk[o] & kIP) dst[o] = src[o];  // advem updates sea points only
   }
 }
 
