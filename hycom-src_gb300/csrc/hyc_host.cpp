@@ -187,6 +187,8 @@ void fold_timings(hyc_ctx *c) {
 
 }  // namespace
 
+void hyc::set_library_error(const char *msg) { g_lib_error = msg ? msg : ""; }
+
 extern "C" {
 
 int hyc_enable_timers(hyc_ctx *c, int32_t on) {

@@ -45,4 +45,7 @@ int mass_sum_partials();
 cudaError_t launch_mass_sum(const double *fld, const double *fc, const double *scal, const uint8_t *msk,
                             int ii, int jj, int nbdy, int ld1, double *partial, double *dres, cudaStream_t s);
 
+// Record a message for hyc_last_error(NULL, ...).
+void set_library_error(const char *msg);
+
 }  // namespace hyc

@@ -40,7 +40,7 @@ FIELDS = {"temp": 0, "saln": 1, "th3d": 2, "tracer": 3, "uflx": 4, "vflx": 5, "d
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "hyc_set_stream", "hyc_bind_field",
            "hyc_sync_field", "hyc_synchronize", "hyc_tsadvc", "hyc_advem", "hyc_xctilr", "hyc_mass_sum",
-           "hyc_version", "hyc_enable_timers", "hyc_get_stats")
+           "hyc_version", "hyc_enable_timers", "hyc_get_stats", "hyc_advem_noalloc")
 TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4}
 
 
@@ -89,6 +89,8 @@ def lib() -> C.CDLL:
         L.hyc_mass_sum.argtypes = [vp, vp, vp, dp]
         L.hyc_enable_timers.argtypes = [vp, C.c_int32]
         L.hyc_get_stats.argtypes = [vp, C.POINTER(Stats), C.c_int32]
+        L.hyc_advem_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp,
+                                        C.c_double, vp, vp, C.c_double, vp, vp, vp, vp]
         _lib = L
     return _lib
 

@@ -196,6 +196,32 @@ int hyc_enable_timers(hyc_ctx *ctx, int32_t on);
 /* Wait for the stream, fold finished timings in, copy out; reset=1 zeroes. */
 int hyc_get_stats(hyc_ctx *ctx, hyc_stats *out, int32_t reset);
 
+/*
+ * advem on one 2-D slice that allocates no device memory.  No counterpart
+ * in the reference: it exists for callers that cannot allocate device
+ * memory when they call the advection -- a model whose device memory is
+ * handed in full to its own pool allocator at start-up, or a time loop that
+ * must not call into the CUDA allocator because cudaMalloc/cudaFree can
+ * synchronise the whole device.  Same arguments and result as hyc_advem
+ * with where = HYC_DEVICE, but without a context: the grid sizes and the
+ * masks ip/iu/iv (int32, device, one slice each, the bigrid masks) are
+ * passed in, and the work is queued on `stream` (a cudaStream_t, NULL for
+ * the default stream); the call returns without waiting for it.
+ * Scratch is a fixed array of 2^21 cells (18 MiB) inside the library that
+ * every GPU loading the library holds until exit; slices with more than
+ * 2^21 cells ((idm+2*nbdy)*(jdm+2*nbdy)) are rejected with HYC_ERR_ARG.
+ * All calls on a device share that array: calls whose GPU work overlaps
+ * race and must be ordered by the caller.  The first call on a device
+ * looks up the array's address; make it before any stream capture.
+ * FCT2 with btrmas (fct2c) is not available here.  Errors: HYC_ERR_* and
+ * the message from hyc_last_error(NULL, ...).
+ */
+int hyc_advem_noalloc(int32_t idm, int32_t jdm, int32_t nbdy, int32_t advtyp, double *fld,
+                      const double *fldc, const double *u, const double *v, const double *fco,
+                      const double *fcn, double posdef, const double *scal, const double *scali,
+                      double dt2, const int32_t *ip, const int32_t *iu, const int32_t *iv,
+                      void *stream);
+
 /* Library build identification, e.g. "hycadv 0.1 sm_103a". */
 const char *hyc_version(void);
 
