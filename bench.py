@@ -221,6 +221,71 @@ def reference_arm(args, wl):
     return 0
 
 
+def run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream):
+    """The same basin through the ensemble API: FP64 plain (three leapfrog
+    levels, no copy-back) and FP32-mixed, each timed over K steps captured
+    in a CUDA graph; the mixed form's error against the FP64 form after one
+    step from the same inputs is reported per field."""
+    import torch
+
+    import hycadv
+
+    kdm = wl["kdm"]
+    spec = dict(idm=b.nx, jdm=b.ny, kdm=kdm, nbdy=b.nbdy, nreg=nreg, ntr=2, ip=masks["ip"], iu=masks["iu"],
+                iv=masks["iv"], scp2=sc, scp2i=si)
+    out = {}
+    ups_step = wl["nx"] * wl["ny"] * kdm * 2
+    peak, _ = peak_hbm()
+    first = {}
+    for prec in ("fp64", "mixed"):
+        ens = hycadv.Ensemble([spec], precision=prec)
+        ens.set_stream(stream)  # graphs are recorded on the library's own stream and launched here
+        old = torch.stack([case.temp[1], case.saln[1]]).contiguous()
+        cur = torch.stack([case.temp[0], case.saln[0]]).contiguous()
+        ens.put(0, "old", old)
+        ens.put(0, "cur", cur)
+        del old, cur
+        ens.put(0, "uflx", case.uflx)
+        ens.put(0, "vflx", case.vflx)
+        ens.put(0, "dp", case.dp[1].contiguous())
+        tx, ty, tms = ens.tune(2, wl["delt1"])
+        ens.step(2, wl["delt1"], 1)  # from the same inputs: compare one step
+        got = torch.empty((2, kdm, b.ld2, b.ld1), dtype=torch.float64, device=dev)
+        ens.get(0, "cur", got)
+        first[prec] = got
+        ens.step(2, wl["delt1"], args.steps, graph=True)  # capture
+        torch.cuda.synchronize(dev)
+        ens.enable_timers(True)
+        ens.stats(reset=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ens.step(2, wl["delt1"], args.steps, graph=True)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / args.steps
+        s_t, s_f = (8, 8) if prec == "fp64" else (4, 4)
+        bpu = bytes_per_update(s_t, s_f, 8, 2, kdm)
+        ach = ups_step * bpu / (ms / 1e3) / 1e9
+        out[prec] = {"value": ups_step / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "tile": [tx, ty],
+                     "algorithmic_bytes_per_update": bpu, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
+                     "graph_steps": args.steps}
+        ens.close()
+        torch.cuda.empty_cache()
+    ip = torch.as_tensor(masks["ip"], device=dev) != 0
+    inner = torch.zeros_like(ip)
+    inner[b.J, b.I] = True
+    sea = ip & inner
+    errs = {}
+    for q, name in enumerate(("temp", "saln")):
+        d = (first["mixed"][q] - first["fp64"][q])[:, sea]
+        ref = first["fp64"][q][:, sea]
+        errs[name] = {"max_rel": float(d.abs().max() / ref.abs().max()),
+                      "rms_rel": float(d.pow(2).mean().sqrt() / ref.abs().max())}
+    out["mixed_vs_fp64_one_step"] = errs
+    out["mixed_speedup_vs_fp64_plain"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def config_of(args, wl):
     return {"workload": f"{args.workload}: {'periodic-x' if wl['periodic'] else 'closed'} basin "
                         f"{wl['nx']}x{wl['ny']}x{wl['kdm']}, T+S, {SCHEME_NAMES[args.advtyp]} "
@@ -244,6 +309,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--forms", action="store_true",
+                    help="also time the ensemble FP64 and FP32-mixed forms on the same basin")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = dict(WORKLOADS[args.workload])
@@ -327,6 +394,10 @@ def main():
                 "note": "FP64 form is FP64-ALU bound on GB300 (FP64 pipe ~1/72 of FP32); see DESIGN.md"}
     clocks = clk.summary()
 
+    forms = None
+    if args.forms:
+        forms = run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream)
+
     # end-to-end through the C ABI with host buffers (pinned), copies in the timed region
     e2e = None
     if not args.no_e2e:
@@ -384,7 +455,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, HYCOM units/layout)",
             "config": config_of(args, wl), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": int(st["launches"]), "clocks": clocks,
+            "gpu_launches": int(st["launches"]), "clocks": clocks, "forms": forms,
             "timers_ms": {k: v for k, v in st.items() if k != "launches"},
         }
         print(json.dumps(line), flush=True)

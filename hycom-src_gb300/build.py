@@ -28,6 +28,8 @@ UNITS = {
     "hyc_fp64.cu": ["-lineinfo", "-fmad=false"],
     "hyc_host.cpp": [],
     "hyc_noalloc.cu": ["-lineinfo"],
+    "hyc_mixed.cu": ["-lineinfo"],
+    "hyc_ens_host.cpp": [],
 }
 
 

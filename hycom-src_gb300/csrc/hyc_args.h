@@ -35,9 +35,12 @@ struct TileArgs {
   double dt2;
   int nfld;
   FieldDesc f[kMaxFields];
-  // output: out + (fi*kdm + k)*slice ; every interior cell written
+  // output: out + (fi*kdm + k)*slice; sea cells of the interior are written
   double *out;
   int kdm;
+  // >0: also write the periodic-x halo images of output cells with
+  // i <= images or i > ii-images (an ensemble level is its own halo source)
+  int images;
 };
 
 template <int TX, int TY>

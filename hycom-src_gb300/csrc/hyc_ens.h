@@ -1,0 +1,47 @@
+// hyc_ens.h -- device-visible descriptors and launchers of the ensemble
+// (batched) form.  Not part of the public C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "hyc_args.h"
+#include "hyc_internal.h"
+
+namespace hyc {
+
+// One basin of an FP32-mixed ensemble for one leapfrog rotation.  Slices
+// use the ensemble pitch ld1 (>= idm+2*nbdy, a multiple of 4).
+struct MixBasin {
+  int ii, jj, nbdy, ld1, ld2;
+  long long slice;
+  int ntx, nty, kdm, ntr;
+  int images;  // periodic-x halo images to write (0 when closed)
+  int pad;
+  double dt2;
+  const uint8_t *msk;
+  const double *scp2, *scp2i;
+  const float *uflx, *vflx;   // kdm slices
+  const double *dp;           // kdm slices, dp(:,:,k,n)
+  const float *fold, *fcur;   // ntr*kdm slices, levels t-1 and t
+  float *fnew;                // ntr*kdm slices, level t+1
+};
+
+bool mix_shape_ok(TileShape t);
+cudaError_t launch_mix_fct2(TileShape t, const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm,
+                            cudaStream_t s);
+
+// FP64 ensemble: the FCT tile body over a queue of (basin, tile, layer)
+cudaError_t launch_fct_queue(int scheme, TileShape t, const TileArgs *basins, const int4 *items, int nitems,
+                             int *head, int nsm, cudaStream_t s);
+
+cudaError_t launch_repitch(const void *src, int src_fp32, long long spitch, long long sslice, void *dst, int dst_fp32,
+                           long long dpitch, long long dslice, int w, int h, int nslices, cudaStream_t s);
+
+cudaError_t launch_content(const void *fld, int fld_fp32, const void *uflx, const void *vflx, int flx_fp32,
+                           const double *dp, const double *scp2, const double *scp2i, const uint8_t *msk, int ii,
+                           int jj, int nb, int ld1, long long slice, int kdm, int use_fco, double dt2,
+                           double *partial, cudaStream_t s);
+
+}  // namespace hyc

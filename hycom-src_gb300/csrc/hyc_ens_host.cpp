@@ -1,0 +1,644 @@
+// hyc_ens_host.cpp -- host side of the ensemble (batched) form: storage,
+// leapfrog level rotation, work queue, CUDA-graph capture and the tile-shape
+// autotuner.  C ABI in include/hycom_adv.h (hyc_ens_*).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/hycom_adv.h"
+#include "hyc_args.h"
+#include "hyc_ens.h"
+#include "hyc_internal.h"
+
+using hyc::MixBasin;
+using hyc::TileArgs;
+
+namespace {
+
+struct EBasin {
+  int idm, jdm, kdm, nbdy, nreg, ntr, ld1r, ld1, ld2;  // ld1r: reference pitch, ld1: ensemble pitch
+  long long slice;
+  uint8_t *msk = nullptr;
+  double *scp2 = nullptr, *scp2i = nullptr;
+  void *uflx = nullptr, *vflx = nullptr;  // FP32 (mixed) or FP64
+  double *dp = nullptr;
+  void *lev[3] = {nullptr, nullptr, nullptr};  // tracer state, physical levels
+  long long work = 0;                           // cells*layers*tracers, for queue ordering
+};
+
+}  // namespace
+
+struct hyc_ens {
+  int device = 0, prec = HYC_PREC_FP64, nsm = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaStream_t cap_stream = nullptr;  // graphs are recorded here, then launched on `stream`
+  std::vector<EBasin> b;
+  int rot = 0;           // logical OLD = lev[rot], CUR = lev[(rot+1)%3], NEW = lev[(rot+2)%3]
+  bool primed = false;   // NEW level initialised (land and halo cells) from CUR
+  hyc::TileShape shape{32, 16};
+  // device tables, one per rotation
+  MixBasin *d_mix[3] = {nullptr, nullptr, nullptr};
+  TileArgs *d_targs[3] = {nullptr, nullptr, nullptr};
+  double tbl_dt2 = -1.0;
+  int4 *d_items = nullptr;
+  int nitems = 0;
+  int items_tx = 0, items_ty = 0, items_layers = -1;
+  int *d_head = nullptr;  // one queue counter per step slot
+  int nhead = 0;
+  double *d_partial = nullptr;
+  int npartial = 0;
+  // graph cache
+  cudaGraphExec_t gexec = nullptr;
+  int g_nsteps = 0, g_advtyp = -1, g_rot = -1, g_tx = 0, g_ty = 0;
+  double g_dt = 0.0;
+  // timers
+  bool timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+  hyc_stats stats{};
+  std::string err;
+};
+
+namespace {
+
+int efail(hyc_ens *e, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (e) e->err = buf;
+  hyc::set_library_error(buf);
+  return code;
+}
+
+#define ECK(call, what)                                                                    \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return efail(e, HYC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e_)); \
+  } while (0)
+
+struct Dev {
+  int prev = -1;
+  explicit Dev(int d) {
+    cudaGetDevice(&prev);
+    if (prev != d) cudaSetDevice(d);
+  }
+  ~Dev() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+size_t esz(const hyc_ens *e) { return e->prec == HYC_PREC_MIXED ? 4 : 8; }
+
+void free_all(hyc_ens *e) {
+  for (auto &b : e->b) {
+    cudaFree(b.msk);
+    cudaFree(b.scp2);
+    cudaFree(b.scp2i);
+    cudaFree(b.uflx);
+    cudaFree(b.vflx);
+    cudaFree(b.dp);
+    for (auto &l : b.lev) cudaFree(l);
+  }
+  for (int r = 0; r < 3; r++) {
+    cudaFree(e->d_mix[r]);
+    cudaFree(e->d_targs[r]);
+  }
+  cudaFree(e->d_items);
+  cudaFree(e->d_head);
+  cudaFree(e->d_partial);
+  if (e->gexec) cudaGraphExecDestroy(e->gexec);
+  for (auto &p : e->pending) {
+    cudaEventDestroy(p.first);
+    cudaEventDestroy(p.second);
+  }
+}
+
+// device tables for the three rotations (rebuilt when delt1 changes)
+int build_tables(hyc_ens *e, double dt2) {
+  if (e->tbl_dt2 == dt2) return HYC_OK;
+  ECK(cudaStreamSynchronize(e->stream), "tables sync");  // earlier steps may still read the tables
+  const int nb = (int)e->b.size();
+  for (int r = 0; r < 3; r++) {
+    const int lo = r, lc = (r + 1) % 3, ln = (r + 2) % 3;
+    if (e->prec == HYC_PREC_MIXED) {
+      std::vector<MixBasin> t(nb);
+      for (int i = 0; i < nb; i++) {
+        const EBasin &b = e->b[i];
+        MixBasin &m = t[i];
+        memset(&m, 0, sizeof m);
+        m.ii = b.idm;
+        m.jj = b.jdm;
+        m.nbdy = b.nbdy;
+        m.ld1 = b.ld1;
+        m.ld2 = b.ld2;
+        m.slice = b.slice;
+        m.ntx = (b.idm + e->shape.tx - 1) / e->shape.tx;
+        m.nty = (b.jdm + e->shape.ty - 1) / e->shape.ty;
+        m.kdm = b.kdm;
+        m.ntr = b.ntr;
+        m.images = b.nreg == 1 ? std::min(5, b.nbdy) : 0;
+        m.dt2 = dt2;
+        m.msk = b.msk;
+        m.scp2 = b.scp2;
+        m.scp2i = b.scp2i;
+        m.uflx = (const float *)b.uflx;
+        m.vflx = (const float *)b.vflx;
+        m.dp = b.dp;
+        m.fold = (const float *)b.lev[lo];
+        m.fcur = (const float *)b.lev[lc];
+        m.fnew = (float *)b.lev[ln];
+      }
+      ECK(cudaMemcpy(e->d_mix[r], t.data(), nb * sizeof(MixBasin), cudaMemcpyHostToDevice), "mix table");
+    } else {
+      std::vector<TileArgs> t(nb);
+      for (int i = 0; i < nb; i++) {
+        const EBasin &b = e->b[i];
+        TileArgs &a = t[i];
+        memset(&a, 0, sizeof a);
+        a.ii = b.idm;
+        a.jj = b.jdm;
+        a.nbdy = b.nbdy;
+        a.ld1 = b.ld1;
+        a.ld2 = b.ld2;
+        a.slice = b.slice;
+        a.ntx = (b.idm + e->shape.tx - 1) / e->shape.tx;
+        a.nty = (b.jdm + e->shape.ty - 1) / e->shape.ty;
+        a.mode = 0;
+        a.msk = b.msk;
+        a.scal = b.scp2;
+        a.scali = b.scp2i;
+        a.uflx = (const double *)b.uflx;
+        a.vflx = (const double *)b.vflx;
+        a.dpn = b.dp;
+        a.dt2 = dt2;
+        a.nfld = b.ntr;
+        for (int q = 0; q < b.ntr; q++) {
+          a.f[q].nbase = (double *)b.lev[lo] + (long long)q * b.kdm * b.slice;
+          a.f[q].mbase = (const double *)b.lev[lc] + (long long)q * b.kdm * b.slice;
+          a.f[q].k_off = 0;
+          a.f[q].kmin = 1;
+          a.f[q].kmax = b.kdm;
+          a.f[q].posdef = 0.0;
+        }
+        a.out = (double *)b.lev[ln];
+        a.kdm = b.kdm;
+        a.images = b.nreg == 1 ? std::min(5, b.nbdy) : 0;
+      }
+      ECK(cudaMemcpy(e->d_targs[r], t.data(), nb * sizeof(TileArgs), cudaMemcpyHostToDevice), "fp64 table");
+    }
+  }
+  e->tbl_dt2 = dt2;
+  return HYC_OK;
+}
+
+// queue of work items, largest first (longest-processing-time order)
+int build_items(hyc_ens *e) {
+  const bool per_layer = e->prec != HYC_PREC_MIXED;
+  if (e->d_items && e->items_tx == e->shape.tx && e->items_ty == e->shape.ty) return HYC_OK;
+  struct W {
+    long long work;
+    int4 it;
+  };
+  std::vector<W> w;
+  for (int i = 0; i < (int)e->b.size(); i++) {
+    const EBasin &b = e->b[i];
+    const int ntx = (b.idm + e->shape.tx - 1) / e->shape.tx, nty = (b.jdm + e->shape.ty - 1) / e->shape.ty;
+    for (int t = 0; t < ntx * nty; t++) {
+      if (per_layer) {
+        for (int k = 0; k < b.kdm; k++) w.push_back({(long long)b.ntr, make_int4(i, t, k, 0)});
+      } else {
+        w.push_back({(long long)b.kdm * b.ntr, make_int4(i, t, 0, 0)});
+      }
+    }
+  }
+  std::stable_sort(w.begin(), w.end(), [](const W &a, const W &c) { return a.work > c.work; });
+  ECK(cudaStreamSynchronize(e->stream), "items sync");
+  std::vector<int4> it(w.size());
+  for (size_t i = 0; i < w.size(); i++) it[i] = w[i].it;
+  cudaFree(e->d_items);
+  e->d_items = nullptr;
+  ECK(cudaMalloc(&e->d_items, std::max<size_t>(1, it.size()) * sizeof(int4)), "items");
+  ECK(cudaMemcpy(e->d_items, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice), "items copy");
+  e->nitems = (int)it.size();
+  e->items_tx = e->shape.tx;
+  e->items_ty = e->shape.ty;
+  e->tbl_dt2 = -1.0;  // ntx/nty in the tables depend on the shape
+  return HYC_OK;
+}
+
+int ensure_heads(hyc_ens *e, int n) {
+  if (e->nhead >= n) return HYC_OK;
+  cudaFree(e->d_head);
+  e->d_head = nullptr;
+  ECK(cudaMalloc(&e->d_head, n * sizeof(int)), "queue heads");
+  e->nhead = n;
+  return HYC_OK;
+}
+
+// NEW level <- CUR level for every basin (land cells and halo of the spare level)
+int prime(hyc_ens *e) {
+  if (e->primed) return HYC_OK;
+  const int lc = (e->rot + 1) % 3, ln = (e->rot + 2) % 3;
+  for (auto &b : e->b)
+    ECK(cudaMemcpyAsync(b.lev[ln], b.lev[lc], (size_t)b.ntr * b.kdm * b.slice * esz(e), cudaMemcpyDeviceToDevice,
+                        e->stream),
+        "prime");
+  e->primed = true;
+  return HYC_OK;
+}
+
+// one step's launches (queue reset + step kernel) for rotation r, head slot h
+int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
+  ECK(cudaMemsetAsync(e->d_head + h, 0, sizeof(int), st), "queue reset");
+  cudaError_t c;
+  if (e->prec == HYC_PREC_MIXED)
+    c = hyc::launch_mix_fct2(e->shape, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, st);
+  else
+    c = hyc::launch_fct_queue(advtyp, e->shape, e->d_targs[r], e->d_items, e->nitems, e->d_head + h, e->nsm, st);
+  if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "step kernel: %s", cudaGetErrorString(c));
+  e->stats.launches += 1;
+  return HYC_OK;
+}
+
+bool shape_ok(const hyc_ens *e, hyc::TileShape t) {
+  if (e->prec == HYC_PREC_MIXED) return hyc::mix_shape_ok(t);
+  return (t.tx == 32 && t.ty == 16) || (t.tx == 16 && t.ty == 16);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *hyc_ens_last_error(const hyc_ens *e) { return e ? e->err.c_str() : ""; }
+
+int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, int32_t precision, int32_t device) {
+  if (!out || nbasin < 1 || !specs || (precision != HYC_PREC_FP64 && precision != HYC_PREC_MIXED))
+    return efail(nullptr, HYC_ERR_ARG, "hyc_ens_create: bad arguments");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+    return efail(nullptr, HYC_ERR_CUDA, "hyc_ens_create: CUDA device %d not available", device);
+  hyc_ens *e = new hyc_ens;
+  e->device = device;
+  e->prec = precision;
+  Dev g(device);
+  cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, device);
+  auto bail = [&](int rc) {
+    free_all(e);
+    if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(efail(nullptr, HYC_ERR_CUDA, "stream"));
+  e->own_stream = true;
+  const int align = precision == HYC_PREC_MIXED ? 4 : 2;  // 16-byte rows
+  int maxk = 0;
+  for (int i = 0; i < nbasin; i++) {
+    const hyc_basin_spec &s = specs[i];
+    if (s.idm < 1 || s.jdm < 1 || s.kdm < 1 || s.nbdy < 5 || s.ntr < 1 || s.ntr > hyc::kMaxFields ||
+        !(s.nreg == 0 || s.nreg == 1) || !s.ip || !s.iu || !s.iv || !s.scp2 || !s.scp2i)
+      return bail(efail(nullptr, HYC_ERR_ARG, "basin %d: bad spec (nbdy>=5, 1<=ntr<=16, nreg 0/1)", i));
+    EBasin b;
+    b.idm = s.idm;
+    b.jdm = s.jdm;
+    b.kdm = s.kdm;
+    b.nbdy = s.nbdy;
+    b.nreg = s.nreg;
+    b.ntr = s.ntr;
+    b.ld1r = s.idm + 2 * s.nbdy;
+    b.ld1 = (b.ld1r + align - 1) / align * align;
+    b.ld2 = s.jdm + 2 * s.nbdy;
+    b.slice = (long long)b.ld1 * b.ld2;
+    b.work = (long long)s.idm * s.jdm * s.kdm * s.ntr;
+    maxk = std::max(maxk, s.kdm);
+    // masks (validated like hyc_adv_init) and metrics, repitched
+    std::vector<uint8_t> m((size_t)b.slice, 0);
+    std::vector<double> sc((size_t)b.slice, 1.0), si((size_t)b.slice, 1.0);
+    for (int j = 0; j < b.ld2; j++)
+      for (int ia = 0; ia < b.ld1r; ia++) {
+        const size_t o = (size_t)ia + (size_t)j * b.ld1r, d = (size_t)ia + (size_t)j * b.ld1;
+        const bool p = s.ip[o] != 0, u = s.iu[o] != 0, v = s.iv[o] != 0;
+        if (ia > 0 && u != (p && s.ip[o - 1] != 0))
+          return bail(efail(nullptr, HYC_ERR_MASK, "basin %d: iu inconsistent with ip", i));
+        if (j > 0 && v != (p && s.ip[o - b.ld1r] != 0))
+          return bail(efail(nullptr, HYC_ERR_MASK, "basin %d: iv inconsistent with ip", i));
+        m[d] = (p ? hyc::kIP : 0) | (u ? hyc::kIU : 0) | (v ? hyc::kIV : 0);
+        sc[d] = s.scp2[o];
+        si[d] = s.scp2i[o];
+      }
+    const size_t es = precision == HYC_PREC_MIXED ? 4 : 8;
+    bool ok = cudaMalloc(&b.msk, b.slice) == cudaSuccess && cudaMalloc(&b.scp2, b.slice * 8) == cudaSuccess &&
+              cudaMalloc(&b.scp2i, b.slice * 8) == cudaSuccess &&
+              cudaMalloc(&b.uflx, b.slice * b.kdm * es) == cudaSuccess &&
+              cudaMalloc(&b.vflx, b.slice * b.kdm * es) == cudaSuccess &&
+              cudaMalloc(&b.dp, b.slice * b.kdm * 8) == cudaSuccess;
+    for (int l = 0; l < 3 && ok; l++) ok = cudaMalloc(&b.lev[l], b.slice * b.kdm * b.ntr * es) == cudaSuccess;
+    e->b.push_back(b);
+    if (!ok) return bail(efail(nullptr, HYC_ERR_NOMEM, "basin %d: device allocation failed", i));
+    EBasin &bb = e->b.back();
+    bool cp = cudaMemcpy(bb.msk, m.data(), bb.slice, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(bb.scp2, sc.data(), bb.slice * 8, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(bb.scp2i, si.data(), bb.slice * 8, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemset(bb.uflx, 0, bb.slice * bb.kdm * es) == cudaSuccess &&
+              cudaMemset(bb.vflx, 0, bb.slice * bb.kdm * es) == cudaSuccess &&
+              cudaMemset(bb.dp, 0, bb.slice * bb.kdm * 8) == cudaSuccess;
+    for (int l = 0; l < 3 && cp; l++) cp = cudaMemset(bb.lev[l], 0, bb.slice * bb.kdm * bb.ntr * es) == cudaSuccess;
+    if (!cp) return bail(efail(nullptr, HYC_ERR_CUDA, "basin %d: upload failed", i));
+  }
+  for (int r = 0; r < 3; r++) {
+    bool ok = precision == HYC_PREC_MIXED ? cudaMalloc(&e->d_mix[r], nbasin * sizeof(MixBasin)) == cudaSuccess
+                                          : cudaMalloc(&e->d_targs[r], nbasin * sizeof(TileArgs)) == cudaSuccess;
+    if (!ok) return bail(efail(nullptr, HYC_ERR_NOMEM, "tables"));
+  }
+  e->npartial = maxk;
+  if (cudaMalloc(&e->d_partial, 2 * maxk * sizeof(double)) != cudaSuccess)
+    return bail(efail(nullptr, HYC_ERR_NOMEM, "partials"));
+  *out = e;
+  return HYC_OK;
+}
+
+int hyc_ens_destroy(hyc_ens *e) {
+  if (!e) return HYC_OK;
+  {
+    Dev g(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    free_all(e);
+    if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
+    if (e->cap_stream) cudaStreamDestroy(e->cap_stream);
+  }
+  delete e;
+  return HYC_OK;
+}
+
+int hyc_ens_set_stream(hyc_ens *e, void *stream) {
+  if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
+  Dev g(e->device);
+  if (e->own_stream && e->stream) {
+    cudaStreamSynchronize(e->stream);
+    cudaStreamDestroy(e->stream);
+  }
+  e->stream = (cudaStream_t)stream;
+  e->own_stream = false;
+  if (e->gexec) {
+    cudaGraphExecDestroy(e->gexec);
+    e->gexec = nullptr;
+  }
+  return HYC_OK;
+}
+
+static int move(hyc_ens *e, int32_t basin, int32_t what, void *host, int32_t where, bool put) {
+  if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
+  if (basin < 0 || basin >= (int)e->b.size() || what < HYC_E_OLD || what > HYC_E_DP || !host ||
+      (where != HYC_HOST && where != HYC_DEVICE) || (!put && what > HYC_E_CUR && what != HYC_E_DP))
+    return efail(e, HYC_ERR_ARG, "hyc_ens_put/get: bad arguments");
+  Dev g(e->device);
+  EBasin &b = e->b[basin];
+  void *dst;
+  int dfp32 = e->prec == HYC_PREC_MIXED;
+  int ns;
+  switch (what) {
+    case HYC_E_OLD: dst = b.lev[e->rot]; ns = b.ntr * b.kdm; break;
+    case HYC_E_CUR: dst = b.lev[(e->rot + 1) % 3]; ns = b.ntr * b.kdm; break;
+    case HYC_E_UFLX: dst = b.uflx; ns = b.kdm; break;
+    case HYC_E_VFLX: dst = b.vflx; ns = b.kdm; break;
+    default: dst = b.dp; ns = b.kdm; dfp32 = 0; break;
+  }
+  const long long rsl = (long long)b.ld1r * b.ld2;
+  const size_t bytes = (size_t)rsl * ns * 8;
+  double *stage = nullptr;
+  ECK(cudaMallocAsync(&stage, bytes, e->stream), "staging");
+  cudaError_t c;
+  if (put) {
+    ECK(cudaMemcpyAsync(stage, host, bytes, where == HYC_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                        e->stream),
+        "put copy");
+    // tsadvc refreshes these halos before advecting (mod_tsadvc.F90:1829-1836); dp's is taken as given
+    if (what != HYC_E_DP) {
+      c = hyc::launch_xctilr(stage, rsl, ns, b.idm, b.jdm, b.nbdy, b.ld1r, 5, 5, b.nreg, e->stream);
+      if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put halo: %s", cudaGetErrorString(c));
+    }
+    c = hyc::launch_repitch(stage, 0, b.ld1r, rsl, dst, dfp32, b.ld1, b.slice, b.ld1r, b.ld2, ns, e->stream);
+  } else {
+    c = hyc::launch_repitch(dst, dfp32, b.ld1, b.slice, stage, 0, b.ld1r, rsl, b.ld1r, b.ld2, ns, e->stream);
+    if (c == cudaSuccess)
+      c = cudaMemcpyAsync(host, stage, bytes, where == HYC_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                          e->stream);
+  }
+  if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put/get: %s", cudaGetErrorString(c));
+  ECK(cudaFreeAsync(stage, e->stream), "staging free");
+  ECK(cudaStreamSynchronize(e->stream), "put/get sync");
+  if (put && (what == HYC_E_OLD || what == HYC_E_CUR)) e->primed = false;
+  return HYC_OK;
+}
+
+int hyc_ens_put(hyc_ens *e, int32_t basin, int32_t what, const double *src, int32_t where) {
+  return move(e, basin, what, (void *)src, where, true);
+}
+
+int hyc_ens_get(hyc_ens *e, int32_t basin, int32_t what, double *dst, int32_t where) {
+  return move(e, basin, what, dst, where, false);
+}
+
+int hyc_ens_set_tile(hyc_ens *e, int32_t tx, int32_t ty) {
+  if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
+  hyc::TileShape t{tx, ty};
+  if (!shape_ok(e, t)) return efail(e, HYC_ERR_ARG, "tile %dx%d not available", tx, ty);
+  if (t.tx != e->shape.tx || t.ty != e->shape.ty) {
+    e->shape = t;
+    e->tbl_dt2 = -1.0;
+    if (e->gexec) {
+      cudaGraphExecDestroy(e->gexec);
+      e->gexec = nullptr;
+    }
+  }
+  return HYC_OK;
+}
+
+int hyc_ens_enable_timers(hyc_ens *e, int32_t on) {
+  if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
+  e->timing = on != 0;
+  return HYC_OK;
+}
+
+int hyc_ens_stats(hyc_ens *e, hyc_stats *out, int32_t reset) {
+  if (!e || !out) return efail(e, HYC_ERR_ARG, "null argument");
+  Dev g(e->device);
+  ECK(cudaStreamSynchronize(e->stream), "stats sync");
+  for (auto &p : e->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.first, p.second) == cudaSuccess) {
+      e->stats.ms[HYC_T_ADVECT] += ms;
+      e->stats.calls[HYC_T_ADVECT] += 1;
+    }
+    cudaEventDestroy(p.first);
+    cudaEventDestroy(p.second);
+  }
+  e->pending.clear();
+  *out = e->stats;
+  if (reset) e->stats = hyc_stats{};
+  return HYC_OK;
+}
+
+int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32_t use_graph) {
+  if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
+  if (nsteps < 1) return efail(e, HYC_ERR_ARG, "nsteps < 1");
+  if (e->prec == HYC_PREC_MIXED ? advtyp != 2 : (advtyp != 2 && advtyp != 4))
+    return efail(e, HYC_ERR_UNSUPPORTED, "ensemble advtyp %d not available for this precision", advtyp);
+  Dev g(e->device);
+  int rc;
+  if ((rc = build_items(e)) || (rc = build_tables(e, delt1)) || (rc = ensure_heads(e, nsteps)) || (rc = prime(e)))
+    return rc;
+  cudaEvent_t a = nullptr, z = nullptr;
+  if (e->timing) {
+    cudaEventCreate(&a);
+    cudaEventCreate(&z);
+    cudaEventRecord(a, e->stream);
+  }
+  if (!use_graph) {
+    for (int s = 0; s < nsteps; s++) {
+      if ((rc = enqueue_step(e, advtyp, e->rot, s, e->stream))) return rc;
+      e->rot = (e->rot + 1) % 3;
+    }
+  } else {
+    const bool reuse = e->gexec && e->g_nsteps == nsteps && e->g_advtyp == advtyp && e->g_dt == delt1 &&
+                       e->g_rot == e->rot && e->g_tx == e->shape.tx && e->g_ty == e->shape.ty;
+    if (!reuse) {
+      if (e->gexec) {
+        cudaGraphExecDestroy(e->gexec);
+        e->gexec = nullptr;
+      }
+      // recorded on a private stream (the caller's may be the legacy default
+      // stream, which cannot be captured), launched on the caller's stream
+      if (!e->cap_stream) ECK(cudaStreamCreateWithFlags(&e->cap_stream, cudaStreamNonBlocking), "capture stream");
+      ECK(cudaStreamSynchronize(e->stream), "pre-capture sync");
+      cudaGraph_t graph = nullptr;
+      ECK(cudaStreamBeginCapture(e->cap_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+      int r = e->rot;
+      int64_t l0 = e->stats.launches;
+      for (int s = 0; s < nsteps; s++) {
+        if ((rc = enqueue_step(e, advtyp, r, s, e->cap_stream))) {
+          cudaStreamEndCapture(e->cap_stream, &graph);
+          if (graph) cudaGraphDestroy(graph);
+          return rc;
+        }
+        r = (r + 1) % 3;
+      }
+      e->stats.launches = l0;
+      ECK(cudaStreamEndCapture(e->cap_stream, &graph), "end capture");
+      cudaError_t c = cudaGraphInstantiate(&e->gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(c));
+      e->g_nsteps = nsteps;
+      e->g_advtyp = advtyp;
+      e->g_dt = delt1;
+      e->g_rot = e->rot;
+      e->g_tx = e->shape.tx;
+      e->g_ty = e->shape.ty;
+    }
+    ECK(cudaGraphLaunch(e->gexec, e->stream), "graph launch");
+    e->stats.launches += nsteps;
+    e->rot = (e->rot + nsteps) % 3;
+  }
+  if (e->timing) {
+    cudaEventRecord(z, e->stream);
+    e->pending.push_back({a, z});
+  }
+  return HYC_OK;
+}
+
+int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t *ty, double *ms_out) {
+  if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
+  Dev g(e->device);
+  static const hyc::TileShape cands[] = {{32, 16}, {64, 16}, {32, 32}, {64, 8}, {128, 8}, {16, 16}};
+  hyc::TileShape best = e->shape;
+  float best_ms = 1e30f;
+  const hyc::TileShape keep = e->shape;
+  cudaEvent_t a, z;
+  cudaEventCreate(&a);
+  cudaEventCreate(&z);
+  int rc = prime(e);
+  if (rc) return rc;
+  for (const auto &c : cands) {
+    if (!shape_ok(e, c)) continue;
+    e->shape = c;
+    e->tbl_dt2 = -1.0;
+    if ((rc = build_items(e)) || (rc = build_tables(e, delt1)) || (rc = ensure_heads(e, 1))) break;
+    // the step kernel writes only the spare level: the state is unchanged
+    if ((rc = enqueue_step(e, advtyp, e->rot, 0, e->stream))) break;  // warm-up
+    float tot = 0.f;
+    const int reps = 3;
+    for (int r = 0; r < reps && !rc; r++) {
+      cudaEventRecord(a, e->stream);
+      rc = enqueue_step(e, advtyp, e->rot, 0, e->stream);
+      cudaEventRecord(z, e->stream);
+      cudaEventSynchronize(z);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, z);
+      tot += ms;
+    }
+    if (rc) break;
+    if (tot / reps < best_ms) {
+      best_ms = tot / reps;
+      best = c;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(z);
+  if (rc) {
+    e->shape = keep;
+    e->tbl_dt2 = -1.0;
+    return rc;
+  }
+  e->shape = best;
+  e->tbl_dt2 = -1.0;
+  e->items_tx = 0;  // force the queue for the chosen shape
+  if (e->gexec) {
+    cudaGraphExecDestroy(e->gexec);
+    e->gexec = nullptr;
+  }
+  if (tx) *tx = best.tx;
+  if (ty) *ty = best.ty;
+  if (ms_out) *ms_out = best_ms;
+  return HYC_OK;
+}
+
+int hyc_ens_content(hyc_ens *e, int32_t basin, int32_t tracer, int32_t what, double delt1, double *sum) {
+  if (!e || !sum || basin < 0 || basin >= (int)e->b.size() || (what != HYC_E_OLD && what != HYC_E_CUR))
+    return efail(e, HYC_ERR_ARG, "hyc_ens_content: bad arguments");
+  EBasin &b = e->b[basin];
+  if (tracer < 0 || tracer >= b.ntr) return efail(e, HYC_ERR_ARG, "tracer out of range");
+  Dev g(e->device);
+  const int lev = what == HYC_E_OLD ? e->rot : (e->rot + 1) % 3;
+  const size_t es = esz(e);
+  const char *base = (const char *)b.lev[lev] + (size_t)tracer * b.kdm * b.slice * es;
+  const int fp32 = e->prec == HYC_PREC_MIXED;
+  cudaError_t c = hyc::launch_content(base, fp32, b.uflx, b.vflx, fp32, b.dp, b.scp2, b.scp2i, b.msk, b.idm, b.jdm,
+                                      b.nbdy, b.ld1, b.slice, b.kdm, what == HYC_E_OLD, delt1, e->d_partial,
+                                      e->stream);
+  if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "content: %s", cudaGetErrorString(c));
+  std::vector<double> p(2 * b.kdm);
+  ECK(cudaMemcpyAsync(p.data(), e->d_partial, p.size() * 8, cudaMemcpyDeviceToHost, e->stream), "content d2h");
+  ECK(cudaStreamSynchronize(e->stream), "content sync");
+  double hi = 0.0, lo = 0.0;
+  for (int k = 0; k < b.kdm; k++) {  // compensated, fixed order
+    const double s = hi + p[2 * k];
+    const double bb = s - hi;
+    lo += (hi - (s - bb)) + (p[2 * k] - bb) + p[2 * k + 1];
+    hi = s;
+  }
+  *sum = hi + lo;
+  return HYC_OK;
+}
+
+}  // extern "C"

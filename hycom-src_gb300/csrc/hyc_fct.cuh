@@ -42,20 +42,19 @@ __device__ __forceinline__ void rect(F &&f) {
   }
 }
 
+// One tile (tile index, 0-based layer k) of one basin; sm is the CTA's
+// dynamic shared memory (FctGeom<TX,TY>::smem_bytes).
 template <int SCHEME, int TX, int TY>
-__global__ void __launch_bounds__(256, 2) fct_tile_kernel(const TileArgs A) {
+__device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile, const int k, double *sm) {
   using G = FctGeom<TX, TY>;
   constexpr int RX = G::RX, RY = G::RY, N = G::N;
   constexpr int NOUT_IT = (TX * TY + 255) / 256;
-  extern __shared__ __align__(16) double sm[];
   double *U = sm, *V = U + N, *FCN = V + N, *HO = FCN + N, *HN = HO + N, *RH = HN + N, *SCL = RH + N,
          *SCI = SCL + N;
   double *FLD = SCI + N, *FLDC = FLD + N, *FX = FLDC + N, *FY = FX + N, *FLO = FY + N, *RP = FLO + N,
          *RM = RP + N;
   uint8_t *MSK = reinterpret_cast<uint8_t *>(RM + N);
 
-  const int tile = blockIdx.x;
-  const int k = blockIdx.y;
   const int tyi = tile / A.ntx, txi = tile - tyi * A.ntx;
   const int ib0 = 1 + txi * TX - 3, jb0 = 1 + tyi * TY - 3;  // region origin (Fortran index)
   const int nb = A.nbdy, ld1 = A.ld1, ii = A.ii, jj = A.jj;
@@ -268,9 +267,38 @@ __global__ void __launch_bounds__(256, 2) fct_tile_kernel(const TileArgs A) {
       if (i > ii || j > jj || !(MSK[e] & kIP)) return;
       const double fdv = ((FX[e + 1] - FX[e]) + (FY[e + RX] - FY[e])) * dt2 * SCI[e];
       const double res = kmax(qn[it], kmin(qx[it], FLO[e] - div_rcp(fdv, HN[e], RH[e])));
-      out[(long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1] = res;
+      const long long o = (long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1;
+      out[o] = res;
+      if (A.images) {  // periodic in x: the xctilr copy (mod_xc_sm.h:1415-1421) written here
+        if (i <= A.images) out[o + ii] = res;
+        if (i > ii - A.images) out[o - ii] = res;
+      }
     });
     __syncthreads();
+  }
+}
+
+template <int SCHEME, int TX, int TY>
+__global__ void __launch_bounds__(256, 2) fct_tile_kernel(const TileArgs A) {
+  extern __shared__ __align__(16) double sm[];
+  fct_tile_body<SCHEME, TX, TY>(A, blockIdx.x, blockIdx.y, sm);
+}
+
+// Persistent form for an ensemble of basins: CTAs take work items
+// (basin, tile, layer) from a queue until it is empty.
+template <int SCHEME, int TX, int TY>
+__global__ void __launch_bounds__(256, 2)
+    fct_queue_kernel(const TileArgs *__restrict__ basins, const int4 *__restrict__ items, int nitems, int *head) {
+  extern __shared__ __align__(16) double sm[];
+  __shared__ int cur;
+  for (;;) {
+    if (threadIdx.x == 0) cur = atomicAdd(head, 1);
+    __syncthreads();
+    const int it = cur;
+    __syncthreads();
+    if (it >= nitems) break;
+    const int4 w = items[it];
+    fct_tile_body<SCHEME, TX, TY>(basins[w.x], w.y, w.z, sm);
   }
 }
 

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 
+#include "hyc_ens.h"
 #include "hyc_internal.h"
 #include "hyc_fct.cuh"
 #include "hyc_tile.cuh"
@@ -68,6 +69,35 @@ cudaError_t launch_advect_tiles(int scheme, const TileArgs &a, int nlayers, Tile
   if (t.tx == 32 && t.ty == 16) return launch_shape<32, 16>(scheme, a, nlayers, s);
   if (t.tx == 32 && t.ty == 32) return launch_shape<32, 32>(scheme, a, nlayers, s);
   if (t.tx == 16 && t.ty == 16) return launch_shape<16, 16>(scheme, a, nlayers, s);
+  return cudaErrorInvalidValue;
+}
+
+// persistent FCT kernels for the FP64 ensemble
+template <int S, int TX, int TY>
+static cudaError_t launch_queue_one(const TileArgs *basins, const int4 *items, int nitems, int *head, int nsm,
+                                    cudaStream_t s) {
+  constexpr size_t smem = FctGeom<TX, TY>::smem_bytes;
+  auto kern = fct_queue_kernel<S, TX, TY>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  kern<<<nsm * per_sm, 256, smem, s>>>(basins, items, nitems, head);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fct_queue(int scheme, TileShape t, const TileArgs *basins, const int4 *items, int nitems,
+                             int *head, int nsm, cudaStream_t s) {
+  if (t.tx == 32 && t.ty == 16) {
+    if (scheme == kFCT2) return launch_queue_one<kFCT2, 32, 16>(basins, items, nitems, head, nsm, s);
+    if (scheme == kFCT4) return launch_queue_one<kFCT4, 32, 16>(basins, items, nitems, head, nsm, s);
+  }
+  if (t.tx == 16 && t.ty == 16) {
+    if (scheme == kFCT2) return launch_queue_one<kFCT2, 16, 16>(basins, items, nitems, head, nsm, s);
+    if (scheme == kFCT4) return launch_queue_one<kFCT4, 16, 16>(basins, items, nitems, head, nsm, s);
+  }
   return cudaErrorInvalidValue;
 }
 

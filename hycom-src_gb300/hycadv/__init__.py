@@ -40,7 +40,12 @@ FIELDS = {"temp": 0, "saln": 1, "th3d": 2, "tracer": 3, "uflx": 4, "vflx": 5, "d
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "hyc_set_stream", "hyc_bind_field",
            "hyc_sync_field", "hyc_synchronize", "hyc_tsadvc", "hyc_advem", "hyc_xctilr", "hyc_mass_sum",
-           "hyc_version", "hyc_enable_timers", "hyc_get_stats", "hyc_advem_noalloc")
+           "hyc_version", "hyc_enable_timers", "hyc_get_stats", "hyc_advem_noalloc", "hyc_ens_create",
+           "hyc_ens_destroy", "hyc_ens_set_stream", "hyc_ens_put", "hyc_ens_get", "hyc_ens_set_tile",
+           "hyc_ens_tune", "hyc_ens_step", "hyc_ens_content", "hyc_ens_stats", "hyc_ens_enable_timers",
+           "hyc_ens_last_error")
+ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
+PRECISION = {"fp64": 0, "mixed": 1}
 TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4}
 
 
@@ -52,6 +57,13 @@ class HycError(RuntimeError):
 
 class Stats(C.Structure):
     _fields_ = [("launches", C.c_int64), ("calls", C.c_int64 * 8), ("ms", C.c_double * 8)]
+
+
+class BasinSpec(C.Structure):
+    _fields_ = [("idm", C.c_int32), ("jdm", C.c_int32), ("kdm", C.c_int32), ("nbdy", C.c_int32),
+                ("nreg", C.c_int32), ("ntr", C.c_int32), ("ip", C.POINTER(C.c_int32)),
+                ("iu", C.POINTER(C.c_int32)), ("iv", C.POINTER(C.c_int32)), ("scp2", C.POINTER(C.c_double)),
+                ("scp2i", C.POINTER(C.c_double))]
 
 
 class TsadvcParams(C.Structure):
@@ -89,6 +101,20 @@ def lib() -> C.CDLL:
         L.hyc_mass_sum.argtypes = [vp, vp, vp, dp]
         L.hyc_enable_timers.argtypes = [vp, C.c_int32]
         L.hyc_get_stats.argtypes = [vp, C.POINTER(Stats), C.c_int32]
+        L.hyc_ens_create.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(BasinSpec), C.c_int32, C.c_int32]
+        L.hyc_ens_destroy.argtypes = [vp]
+        L.hyc_ens_set_stream.argtypes = [vp, vp]
+        L.hyc_ens_put.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int32]
+        L.hyc_ens_get.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int32]
+        L.hyc_ens_set_tile.argtypes = [vp, C.c_int32, C.c_int32]
+        L.hyc_ens_tune.argtypes = [vp, C.c_int32, C.c_double, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_double)]
+        L.hyc_ens_step.argtypes = [vp, C.c_int32, C.c_double, C.c_int32, C.c_int32]
+        L.hyc_ens_content.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.POINTER(C.c_double)]
+        L.hyc_ens_stats.argtypes = [vp, C.POINTER(Stats), C.c_int32]
+        L.hyc_ens_enable_timers.argtypes = [vp, C.c_int32]
+        L.hyc_ens_last_error.argtypes = [vp]
+        L.hyc_ens_last_error.restype = C.c_char_p
         L.hyc_advem_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp,
                                         C.c_double, vp, vp, C.c_double, vp, vp, vp, vp]
         _lib = L
@@ -264,3 +290,80 @@ class Context:
         out = C.c_double(0.0)
         _check(lib().hyc_mass_sum(self._h, _ptr(fld)[0], _ptr(fc)[0], C.byref(out)), self._h)
         return out.value
+
+
+class Ensemble:
+    """Many independent basins advected together (hyc_ens_* in the C ABI).
+
+    basins: list of dicts with idm, jdm, kdm, nbdy, nreg, ntr and the
+    bigrid masks ip/iu/iv plus scp2/scp2i (numpy, reference layout).
+    precision: "fp64" (plain form) or "mixed" (FP32-mixed form).
+    """
+
+    def __init__(self, basins, precision: str = "fp64", device: int = 0):
+        L = lib()
+        self._keep = []
+        specs = (BasinSpec * len(basins))()
+        for i, b in enumerate(basins):
+            ip, iu, iv = _i32(b["ip"]), _i32(b["iu"]), _i32(b["iv"])
+            sc, si = _f64(b["scp2"]), _f64(b["scp2i"])
+            self._keep += [ip, iu, iv, sc, si]
+            specs[i] = BasinSpec(b["idm"], b["jdm"], b["kdm"], b["nbdy"], b["nreg"], b["ntr"], ip[1], iu[1], iv[1],
+                                 sc[1], si[1])
+        h = C.c_void_p()
+        _check(L.hyc_ens_create(C.byref(h), len(basins), specs, PRECISION[precision], device))
+        self._h = h
+        self.basins = [dict(b) for b in basins]
+        self.precision = precision
+
+    def _chk(self, rc):
+        if rc != HYC_OK:
+            raise HycError(rc, lib().hyc_ens_last_error(self._h).decode(errors="replace"))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().hyc_ens_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        ptr = stream if isinstance(stream, int) else stream.cuda_stream
+        self._chk(lib().hyc_ens_set_stream(self._h, C.c_void_p(ptr)))
+
+    def put(self, b: int, what: str, a):
+        p, where = _ptr(a)
+        self._chk(lib().hyc_ens_put(self._h, b, ENS_WHAT[what], p, where))
+
+    def get(self, b: int, what: str, out):
+        p, where = _ptr(out)
+        self._chk(lib().hyc_ens_get(self._h, b, ENS_WHAT[what], p, where))
+        return out
+
+    def set_tile(self, tx: int, ty: int):
+        self._chk(lib().hyc_ens_set_tile(self._h, tx, ty))
+
+    def tune(self, advtyp: int, delt1: float):
+        tx, ty, ms = C.c_int32(), C.c_int32(), C.c_double()
+        self._chk(lib().hyc_ens_tune(self._h, advtyp, float(delt1), C.byref(tx), C.byref(ty), C.byref(ms)))
+        return tx.value, ty.value, ms.value
+
+    def step(self, advtyp: int, delt1: float, nsteps: int = 1, graph: bool = False):
+        self._chk(lib().hyc_ens_step(self._h, advtyp, float(delt1), nsteps, int(bool(graph))))
+
+    def content(self, b: int, q: int, what: str, delt1: float) -> float:
+        out = C.c_double()
+        self._chk(lib().hyc_ens_content(self._h, b, q, ENS_WHAT[what], float(delt1), C.byref(out)))
+        return out.value
+
+    def enable_timers(self, on: bool = True):
+        self._chk(lib().hyc_ens_enable_timers(self._h, int(bool(on))))
+
+    def stats(self, reset: bool = False) -> dict:
+        s = Stats()
+        self._chk(lib().hyc_ens_stats(self._h, C.byref(s), int(bool(reset))))
+        return {"launches": int(s.launches), "step_ms": float(s.ms[2]), "step_calls": int(s.calls[2])}

@@ -221,8 +221,8 @@ def make_layer(b: Basin, k: int, kdm: int, seed: int, courant: float, delt1: flo
     dp: smooth field in [10, 500] m (column sums are capped later by
     :func:`cap_columns`).  Velocity: curl of an 8-sine streamfunction (exactly
     non-divergent on the C-grid) plus a small divergent part of relative size
-    ``div_frac`` and sign ``step_sign``, scaled so that
-    max |u| * delt1 / dx = courant.  :func:`mass_fluxes` turns it into
+    ``div_frac`` and sign ``step_sign``, scaled so that the 2-D Courant
+    number (max|u| + max|v|) * delt1 / dx equals courant.  :func:`mass_fluxes` turns it into
     uflx/vflx.
     """
     import torch
@@ -248,7 +248,9 @@ def make_layer(b: Basin, k: int, kdm: int, seed: int, courant: float, delt1: flo
     dmax = torch.clamp(torch.maximum(ud.abs().max(), vd.abs().max()), min=1e-30)
     u = u / umax + step_sign * div_frac * ud / dmax
     v = v / umax + step_sign * div_frac * vd / dmax
-    smax = torch.clamp(torch.maximum(u.abs().max(), v.abs().max()), min=1e-30)
+    # 2-D Courant number: max|u|*dt/dx + max|v|*dt/dy = courant, so that the
+    # donor-cell outflow of any cell stays below its content
+    smax = torch.clamp(u.abs().max() + v.abs().max(), min=1e-30)
     vel = courant * b.dx / delt1 / smax  # m/s per unit
     return LayerForcing(dp=dp, u=u * vel, v=v * vel)
 

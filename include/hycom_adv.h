@@ -222,6 +222,68 @@ int hyc_advem_noalloc(int32_t idm, int32_t jdm, int32_t nbdy, int32_t advtyp, do
                       double dt2, const int32_t *ip, const int32_t *iu, const int32_t *iv,
                       void *stream);
 
+/* ------------------------------------------------------------------------
+ * Ensemble (batched) form: many independent basins of uneven size, layer
+ * and tracer count advected together, one persistent launch per step over
+ * a queue of (basin, tile) work items.  No counterpart in the reference
+ * (HYCOM runs one basin per executable); each basin's step is tsadvc's
+ * advection of its tracers (mod_tsadvc.F90:1708-2048, passive tracers).
+ *
+ * Precision: HYC_PREC_FP64 (the plain form: FP64 state, bit-identical to
+ * hyc_tsadvc) or HYC_PREC_MIXED (FP32 tracer state, fluxes, limiter and
+ * update; FP64 dp, continuity and thickness division; see hyc_mixed.cu).
+ * The library keeps three leapfrog levels per basin and rotates them, so a
+ * step never updates a level in place.
+ * ---------------------------------------------------------------------- */
+#define HYC_PREC_FP64 0
+#define HYC_PREC_MIXED 1
+
+/* what hyc_ens_put / hyc_ens_get move (reference layout, FP64, host or device) */
+#define HYC_E_OLD 0  /* tracers at t-1: ntr*kdm slices (tracer-major)  */
+#define HYC_E_CUR 1  /* tracers at t:   ntr*kdm slices                 */
+#define HYC_E_UFLX 2 /* uflx(:,:,k), kdm slices                        */
+#define HYC_E_VFLX 3 /* vflx(:,:,k), kdm slices                        */
+#define HYC_E_DP 4   /* dp(:,:,k,n), kdm slices (new thickness)         */
+
+typedef struct hyc_ens hyc_ens;
+
+typedef struct hyc_basin_spec {
+  int32_t idm, jdm, kdm, nbdy, nreg, ntr;
+  const int32_t *ip, *iu, *iv;  /* host, ld1*ld2 each (bigrid masks)          */
+  const double *scp2, *scp2i;   /* host, ld1*ld2 each                         */
+} hyc_basin_spec;
+
+int hyc_ens_create(hyc_ens **ens, int32_t nbasin, const hyc_basin_spec *specs, int32_t precision,
+                   int32_t device);
+int hyc_ens_destroy(hyc_ens *ens);
+int hyc_ens_set_stream(hyc_ens *ens, void *stream);
+/* src/dst: ld1*ld2*(slices) doubles in the reference layout (pitch idm+2*nbdy) */
+int hyc_ens_put(hyc_ens *ens, int32_t basin, int32_t what, const double *src, int32_t where);
+int hyc_ens_get(hyc_ens *ens, int32_t basin, int32_t what, double *dst, int32_t where);
+/* Tile shape of the step kernel (tx x ty cells); hyc_ens_tune picks one. */
+int hyc_ens_set_tile(hyc_ens *ens, int32_t tx, int32_t ty);
+/*
+ * Autotuner: time every supported tile shape on this ensemble (the kernel
+ * writes only the spare leapfrog level, so the state does not change),
+ * keep the fastest and return it (tx, ty, ms of the best step; may be NULL).
+ */
+int hyc_ens_tune(hyc_ens *ens, int32_t advtyp, double delt1, int32_t *tx, int32_t *ty, double *ms);
+/*
+ * Advance every basin nsteps leapfrog steps (advtyp 2 = FCT2; FP64 also 4).
+ * use_graph = 1: the nsteps launches are captured once into a CUDA graph
+ * (per nsteps/advtyp/delt1/tile) and replayed.  Asynchronous.
+ */
+int hyc_ens_step(hyc_ens *ens, int32_t advtyp, double delt1, int32_t nsteps, int32_t use_graph);
+/*
+ * FP64 tracer content of basin b, tracer q, level what (HYC_E_OLD with the
+ * old thickness fco, or HYC_E_CUR with fcn), summed over layers and interior
+ * sea cells: sum fld*(fc+onemu)*scp2, compensated.  Synchronous.
+ */
+int hyc_ens_content(hyc_ens *ens, int32_t basin, int32_t tracer, int32_t what, double delt1, double *sum);
+int hyc_ens_stats(hyc_ens *ens, hyc_stats *out, int32_t reset);
+int hyc_ens_enable_timers(hyc_ens *ens, int32_t on);
+const char *hyc_ens_last_error(const hyc_ens *ens);
+
 /* Library build identification, e.g. "hycadv 0.1 sm_103a". */
 const char *hyc_version(void);
 

@@ -1,0 +1,178 @@
+"""Ensemble (batched) form on the GPU: FP64 bit for bit against the oracle,
+FP32-mixed within its error budget, graph replay equal to eager launches,
+tuning leaves the state unchanged, tracer content conserved."""
+import numpy as np
+import pytest
+
+import hycadv
+from helpers import basin, levels, np_case, oracle_grid, same
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [  # nx, ny, periodic, kdm, ntr, seed, courant, delt1
+    (60, 45, False, 3, 2, 401, 0.5, 1800.0),
+    (70, 40, True, 2, 3, 402, 0.8, 1800.0),
+    (33, 27, False, 4, 1, 403, 0.6, 1800.0),
+]
+DELT1 = 1800.0
+
+
+def make_members(specs=SPECS, delt1=DELT1):
+    out = []
+    for nx, ny, per, kdm, ntr, seed, cour, _ in specs:
+        b = basin(nx, ny, per, seed)
+        g = oracle_grid(b)
+        c = np_case(b, g, kdm=kdm, ntracr=max(ntr - 1, 0), seed=seed, courant=cour, delt1=delt1)
+        # ensemble tracers: 0 -> saln, 1.. -> the oracle's tracer array
+        trc = np.concatenate([c["saln"][None]] + ([c["tracer"]] if ntr > 1 else []), axis=0)  # (ntr, 2, kdm, ...)
+        out.append(dict(b=b, g=g, c=c, ntr=ntr, kdm=kdm, trc=trc))
+    return out
+
+
+def spec_of(m):
+    b, g = m["b"], m["g"]
+    sc, si = b.metrics()
+    return dict(idm=b.nx, jdm=b.ny, kdm=m["kdm"], nbdy=b.nbdy, nreg=g.nreg, ntr=m["ntr"], ip=g.masks["ip"],
+                iu=g.masks["iu"], iv=g.masks["iv"], scp2=sc, scp2i=si)
+
+
+def load(ens, members, first_step=1):
+    for i, m in enumerate(members):
+        mm, nn = levels(first_step)
+        old = np.ascontiguousarray(m["trc"][:, nn - 1])
+        cur = np.ascontiguousarray(m["trc"][:, mm - 1])
+        ens.put(i, "old", old)
+        ens.put(i, "cur", cur)
+        ens.put(i, "uflx", np.ascontiguousarray(m["c"]["uflx"]))
+        ens.put(i, "vflx", np.ascontiguousarray(m["c"]["vflx"]))
+        ens.put(i, "dp", np.ascontiguousarray(m["c"]["dp"][nn - 1]))
+
+
+def oracle_step(m, step, advtyp):
+    c = m["c"]
+    mm, nn = levels(step)
+    g = m["g"]
+    g.tsadvc(mm, nn, temp=c["temp"], saln=c["saln"], th3d=c["th3d"], uflx=c["uflx"], vflx=c["vflx"], dp=c["dp"],
+             delt1=DELT1, advtyp=advtyp, tracer=c["tracer"] if m["ntr"] > 1 else None,
+             trcflg=np.zeros(max(m["ntr"] - 1, 1), np.int32), nhybrd=0, nstep=step)
+    trc = np.concatenate([c["saln"][None]] + ([c["tracer"]] if m["ntr"] > 1 else []), axis=0)
+    return np.ascontiguousarray(trc[:, nn - 1])  # the new level
+
+
+def sea_interior(m):
+    """Sea cells of the interior: the halo of a new level is refreshed by the
+    ensemble at once and by tsadvc only at its next call."""
+    b = m["b"]
+    msk = np.zeros_like(m["g"].masks["ip"], dtype=bool)
+    msk[b.J, b.I] = True
+    return msk & (m["g"].masks["ip"] != 0)
+
+
+def get_cur(ens, i, m):
+    out = np.zeros((m["ntr"], m["kdm"], m["b"].ld2, m["b"].ld1))
+    return ens.get(i, "cur", out)
+
+
+@pytest.mark.parametrize("advtyp", [2, 4])
+def test_fp64_ensemble_bitwise(cuda, advtyp):
+    members = make_members()
+    ens = hycadv.Ensemble([spec_of(m) for m in members], precision="fp64")
+    load(ens, members)
+    for step in range(1, 5):
+        ens.step(advtyp, DELT1, 1)
+        for i, m in enumerate(members):
+            want = oracle_step(m, step, advtyp)
+            got = get_cur(ens, i, m)
+            ip = sea_interior(m)
+            assert same(got[..., ip], want[..., ip]), f"basin {i} step {step}"
+            # dp is constant here, but every step reads dp(:,:,k,n) of its own n
+            mm, nn = levels(step + 1)
+            ens.put(i, "dp", np.ascontiguousarray(m["c"]["dp"][nn - 1]))
+    ens.close()
+
+
+def test_graph_replay_equals_eager(cuda):
+    results = []
+    for prec in ("fp64", "mixed"):
+        per = []
+        for graph in (False, True):
+            members = make_members(SPECS[:2])
+            ens = hycadv.Ensemble([spec_of(m) for m in members], precision=prec)
+            load(ens, members)
+            ens.step(2, DELT1, 3, graph=graph)
+            per.append([get_cur(ens, i, m) for i, m in enumerate(members)])
+            ens.close()
+        for a, b in zip(per[0], per[1]):
+            assert np.array_equal(a, b)
+        results.append(per)
+
+
+def test_tune_keeps_state(cuda):
+    members = make_members(SPECS[:2])
+    ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
+    load(ens, members)
+    before = [get_cur(ens, i, m) for i, m in enumerate(members)]
+    tx, ty, ms = ens.tune(2, DELT1)
+    assert (tx, ty) in [(32, 16), (64, 16), (32, 32), (64, 8), (128, 8)] and ms > 0
+    after = [get_cur(ens, i, m) for i, m in enumerate(members)]
+    for a, b in zip(before, after):
+        assert np.array_equal(a, b)
+    ens.close()
+
+
+def test_mixed_one_step_error(cuda):
+    """From identical inputs, one FP32-mixed step is within 1e-6 (relative to
+    each tracer's max |value|) of the FP64 oracle."""
+    members = make_members()
+    ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
+    load(ens, members)
+    ens.step(2, DELT1, 1)
+    for i, m in enumerate(members):
+        want = oracle_step(m, 1, 2)
+        got = get_cur(ens, i, m)
+        ip = sea_interior(m)
+        for q in range(m["ntr"]):
+            err = np.abs(got[q][..., ip] - want[q][..., ip]).max() / np.abs(want[q][..., ip]).max()
+            assert err < 1e-6, (i, q, err)
+    ens.close()
+
+
+@pytest.mark.parametrize("prec,cons_tol,err_tol", [("fp64", 1e-13, 0.0), ("mixed", 1e-6, 1e-4)])
+def test_ensemble_multistep_conservation_extrema(cuda, prec, cons_tol, err_tol):
+    """20 steps: tracer content conserved (FP64 to round-off), no new extrema,
+    and the FP32-mixed drift from the oracle stays within the envelope of the
+    leapfrog-FCT dynamics (an FP64 run perturbed by one FP32 rounding of its
+    inputs already drifts ~1e-5 in 20 steps)."""
+    members = make_members()
+    ens = hycadv.Ensemble([spec_of(m) for m in members], precision=prec)
+    load(ens, members)
+    nsteps = 20
+    start = [(m["trc"][..., m["g"].masks["ip"] != 0].min(), m["trc"][..., m["g"].masks["ip"] != 0].max())
+             for m in members]
+    worst_cons = 0.0
+    for step in range(1, nsteps + 1):
+        for i, m in enumerate(members):
+            mm, nn = levels(step)
+            ens.put(i, "dp", np.ascontiguousarray(m["c"]["dp"][nn - 1]))
+        c_old = [[ens.content(i, q, "old", DELT1) for q in range(m["ntr"])] for i, m in enumerate(members)]
+        ens.step(2, DELT1, 1)
+        c_new = [[ens.content(i, q, "cur", DELT1) for q in range(m["ntr"])] for i, m in enumerate(members)]
+        for i, m in enumerate(members):
+            for q in range(m["ntr"]):
+                worst_cons = max(worst_cons, abs(c_new[i][q] - c_old[i][q]) / abs(c_old[i][q]))
+            oracle_step(m, step, 2)
+    print(f"{prec}: worst relative content change in one step {worst_cons:.2e}")
+    assert worst_cons < cons_tol
+    for i, m in enumerate(members):
+        mm, nn = levels(nsteps)
+        c = m["c"]
+        want = np.concatenate([c["saln"][None]] + ([c["tracer"]] if m["ntr"] > 1 else []), axis=0)[:, nn - 1]
+        got = get_cur(ens, i, m)
+        ip = sea_interior(m)
+        for q in range(m["ntr"]):
+            err = np.abs(got[q][..., ip] - want[q][..., ip]).max() / np.abs(want[q][..., ip]).max()
+            print(f"{prec}: basin {i} tracer {q}: max rel err after {nsteps} steps {err:.2e}")
+            assert err <= err_tol
+        lo, hi = start[i]
+        assert got[..., ip].min() >= lo - 1e-6 * abs(lo) and got[..., ip].max() <= hi + 1e-6 * abs(hi)
+    ens.close()
