@@ -221,7 +221,7 @@ def reference_arm(args, wl):
     return 0
 
 
-def run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream):
+def run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream, precs=("fp64", "mixed")):
     """The same basin through the ensemble API: FP64 plain (three leapfrog
     levels, no copy-back) and FP32-mixed, each timed over K steps captured
     in a CUDA graph; the mixed form's error against the FP64 form after one
@@ -237,8 +237,11 @@ def run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream):
     ups_step = wl["nx"] * wl["ny"] * kdm * 2
     peak, _ = peak_hbm()
     first = {}
-    for prec in ("fp64", "mixed"):
+    for form in precs:
+        prec = "mixed" if form.startswith("mixed") else "fp64"
         ens = hycadv.Ensemble([spec], precision=prec)
+        if prec == "mixed":
+            ens.set_prep64(form == "mixed")
         ens.set_stream(stream)  # graphs are recorded on the library's own stream and launched here
         old = torch.stack([case.temp[1], case.saln[1]]).contiguous()
         cur = torch.stack([case.temp[0], case.saln[0]]).contiguous()
@@ -252,7 +255,7 @@ def run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream):
         ens.step(2, wl["delt1"], 1)  # from the same inputs: compare one step
         got = torch.empty((2, kdm, b.ld2, b.ld1), dtype=torch.float64, device=dev)
         ens.get(0, "cur", got)
-        first[prec] = got
+        first[form] = got
         ens.step(2, wl["delt1"], args.steps, graph=True)  # capture
         torch.cuda.synchronize(dev)
         ens.enable_timers(True)
@@ -263,26 +266,31 @@ def run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream):
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1) / args.steps
-        s_t, s_f = (8, 8) if prec == "fp64" else (4, 4)
+        s_t, s_f = (8, 8) if prec == "fp64" else (4, 4)  # dp stays FP64 in both
         bpu = bytes_per_update(s_t, s_f, 8, 2, kdm)
         ach = ups_step * bpu / (ms / 1e3) / 1e9
-        out[prec] = {"value": ups_step / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "tile": [tx, ty],
+        out[form] = {"value": ups_step / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "tile": [tx, ty],
                      "algorithmic_bytes_per_update": bpu, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
                      "graph_steps": args.steps}
         ens.close()
         torch.cuda.empty_cache()
+    if "fp64" not in first or len(first) < 2:
+        return out
     ip = torch.as_tensor(masks["ip"], device=dev) != 0
     inner = torch.zeros_like(ip)
     inner[b.J, b.I] = True
     sea = ip & inner
-    errs = {}
-    for q, name in enumerate(("temp", "saln")):
-        d = (first["mixed"][q] - first["fp64"][q])[:, sea]
-        ref = first["fp64"][q][:, sea]
-        errs[name] = {"max_rel": float(d.abs().max() / ref.abs().max()),
-                      "rms_rel": float(d.pow(2).mean().sqrt() / ref.abs().max())}
-    out["mixed_vs_fp64_one_step"] = errs
-    out["mixed_speedup_vs_fp64_plain"] = out["mixed"]["value"] / out["fp64"]["value"]
+    for form in first:
+        if form == "fp64":
+            continue
+        errs = {}
+        for q, name in enumerate(("temp", "saln")):
+            d = (first[form][q] - first["fp64"][q])[:, sea]
+            ref = first["fp64"][q][:, sea]
+            errs[name] = {"max_rel": float(d.abs().max() / ref.abs().max()),
+                          "rms_rel": float(d.pow(2).mean().sqrt() / ref.abs().max())}
+        out[f"{form}_vs_fp64_one_step"] = errs
+        out[f"{form}_speedup_vs_fp64_ensemble"] = out[form]["value"] / out["fp64"]["value"]
     return out
 
 
@@ -309,6 +317,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--arm", default="tsadvc", choices=["tsadvc", "ens-fp64", "ens-mixed", "ens-mixed-fp32prep"],
+                    help="tsadvc: the reference-layout C ABI (headline); ens-*: the ensemble form only")
     ap.add_argument("--forms", action="store_true",
                     help="also time the ensemble FP64 and FP32-mixed forms on the same basin")
     args = ap.parse_args()
@@ -339,6 +349,20 @@ def main():
     b, masks, nreg, case = make_workload(wl, dev)
     sc, si = b.metrics()
     kdm = wl["kdm"]
+    if args.arm != "tsadvc":  # one ensemble form alone (profiling, form comparisons)
+        prec = args.arm[4:]
+        f = run_forms(args, wl, b, masks, nreg, sc, si, case, dev, torch.cuda.current_stream(dev), precs=(prec,))[prec]
+        peak, peak_kind = peak_hbm()
+        line = {"metric": METRIC, "value": f["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": f["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32-mixed",
+                "data": "synthetic (seeded generator, HYCOM units/layout)", "impl": args.arm,
+                "config": dict(config_of(args, wl), form=f"ensemble-{prec}", tile=f["tile"]),
+                "roofline": {"bound": "hbm", "achieved": f["achieved_GBs"], "peak": peak, "unit": "GB/s",
+                             "frac": f["frac_of_measured_hbm"], "traffic": None, "peak_kind": peak_kind}}
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return 0
     ctx = hycadv.Context.from_masks(masks, sc, si, kdm=kdm, nreg=nreg, nbdy=b.nbdy, device=local)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream)
@@ -396,7 +420,7 @@ def main():
 
     forms = None
     if args.forms:
-        forms = run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream)
+        forms = run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream, precs=("fp64", "mixed", "mixed-fp32prep"))
 
     # end-to-end through the C ABI with host buffers (pinned), copies in the timed region
     e2e = None

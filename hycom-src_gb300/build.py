@@ -29,6 +29,7 @@ UNITS = {
     "hyc_host.cpp": [],
     "hyc_noalloc.cu": ["-lineinfo"],
     "hyc_mixed.cu": ["-lineinfo"],
+    "hyc_mixed_tma.cu": ["-lineinfo"],
     "hyc_ens_host.cpp": [],
 }
 

@@ -1,6 +1,7 @@
 // hyc_ens.h -- device-visible descriptors and launchers of the ensemble
 // (batched) form.  Not part of the public C ABI.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -26,11 +27,21 @@ struct MixBasin {
   const double *dp;           // kdm slices, dp(:,:,k,n)
   const float *fold, *fcur;   // ntr*kdm slices, levels t-1 and t
   float *fnew;                // ntr*kdm slices, level t+1
+  // TMA descriptors (device memory) for the current tile shape: levels t-1
+  // and t (3-D: ld1 x ld2 x ntr*kdm, FP32), uflx, vflx (FP32) and dp (FP64)
+  const CUtensorMap *tm_old, *tm_cur, *tm_u, *tm_v, *tm_dp;
 };
 
 bool mix_shape_ok(TileShape t);
 cudaError_t launch_mix_fct2(TileShape t, const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm,
-                            cudaStream_t s);
+                            bool prep64, cudaStream_t s);
+
+bool mix_tma_shape_ok(TileShape t);
+cudaError_t launch_mix_fct2_tma(TileShape t, const MixBasin *basins, const int4 *items, int nitems, int *head,
+                                int nsm, bool prep64, int *err, cudaStream_t s);
+// TMA box width (elements) of a tile shape: TX + 12 for the nbdy = 6 halo
+inline int tma_box_x(TileShape t) { return (t.tx + 9 + 3) / 4 * 4; }
+inline int tma_box_y(TileShape t) { return t.ty + 6; }
 
 // FP64 ensemble: the FCT tile body over a queue of (basin, tile, layer)
 cudaError_t launch_fct_queue(int scheme, TileShape t, const TileArgs *basins, const int4 *items, int nitems,

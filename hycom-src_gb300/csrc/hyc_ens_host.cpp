@@ -1,6 +1,7 @@
 // hyc_ens_host.cpp -- host side of the ensemble (batched) form: storage,
 // leapfrog level rotation, work queue, CUDA-graph capture and the tile-shape
 // autotuner.  C ABI in include/hycom_adv.h (hyc_ens_*).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,6 +44,11 @@ struct hyc_ens {
   int rot = 0;           // logical OLD = lev[rot], CUR = lev[(rot+1)%3], NEW = lev[(rot+2)%3]
   bool primed = false;   // NEW level initialised (land and halo cells) from CUR
   hyc::TileShape shape{32, 16};
+  bool prep64 = true;  // FP32-mixed: thickness prep in FP64 (else compensated FP32)
+  bool use_tma = false;  // FP32-mixed: TMA-staged kernel (needs nbdy = 6 everywhere)
+  CUtensorMap *d_tmaps = nullptr;  // [nbasin][6]: level 0,1,2, uflx, vflx, dp
+  int tm_tx = 0, tm_ty = 0;        // shape the maps were encoded for
+  int *d_err = nullptr;            // device error flag (bounded waits that gave up)
   // device tables, one per rotation
   MixBasin *d_mix[3] = {nullptr, nullptr, nullptr};
   TileArgs *d_targs[3] = {nullptr, nullptr, nullptr};
@@ -116,11 +122,66 @@ void free_all(hyc_ens *e) {
   cudaFree(e->d_items);
   cudaFree(e->d_head);
   cudaFree(e->d_partial);
+  cudaFree(e->d_tmaps);
+  cudaFree(e->d_err);
   if (e->gexec) cudaGraphExecDestroy(e->gexec);
   for (auto &p : e->pending) {
     cudaEventDestroy(p.first);
     cudaEventDestroy(p.second);
   }
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+// 3-D tiled map over nz slices of (ld1 x ld2) elements, box (bx, by, 1)
+bool encode3(CUtensorMap *m, void *base, bool fp64, int ld1, int ld2, long long nz, int bx, int by) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  const size_t es = fp64 ? 8 : 4;
+  cuuint64_t dims[3] = {(cuuint64_t)ld1, (cuuint64_t)ld2, (cuuint64_t)nz};
+  cuuint64_t strides[2] = {(cuuint64_t)ld1 * es, (cuuint64_t)ld1 * ld2 * es};
+  cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  return fn(m, fp64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides,
+            box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int encode_maps(hyc_ens *e) {
+  if (e->tm_tx == e->shape.tx && e->tm_ty == e->shape.ty) return HYC_OK;
+  ECK(cudaStreamSynchronize(e->stream), "maps sync");
+  const int bx = hyc::tma_box_x(e->shape), by = hyc::tma_box_y(e->shape);
+  std::vector<CUtensorMap> h(e->b.size() * 6);
+  for (size_t i = 0; i < e->b.size(); i++) {
+    EBasin &b = e->b[i];
+    bool ok = true;
+    for (int l = 0; l < 3; l++)
+      ok &= encode3(&h[i * 6 + l], b.lev[l], false, b.ld1, b.ld2, (long long)b.ntr * b.kdm, bx, by);
+    ok &= encode3(&h[i * 6 + 3], b.uflx, false, b.ld1, b.ld2, b.kdm, bx, by);
+    ok &= encode3(&h[i * 6 + 4], b.vflx, false, b.ld1, b.ld2, b.kdm, bx, by);
+    ok &= encode3(&h[i * 6 + 5], b.dp, true, b.ld1, b.ld2, b.kdm, bx, by);
+    if (!ok) return efail(e, HYC_ERR_CUDA, "cuTensorMapEncodeTiled failed (basin %zu)", i);
+  }
+  ECK(cudaMemcpy(e->d_tmaps, h.data(), h.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "maps copy");
+  e->tm_tx = e->shape.tx;
+  e->tm_ty = e->shape.ty;
+  return HYC_OK;
 }
 
 // device tables for the three rotations (rebuilt when delt1 changes)
@@ -157,6 +218,13 @@ int build_tables(hyc_ens *e, double dt2) {
         m.fold = (const float *)b.lev[lo];
         m.fcur = (const float *)b.lev[lc];
         m.fnew = (float *)b.lev[ln];
+        if (e->d_tmaps) {
+          m.tm_old = e->d_tmaps + i * 6 + lo;
+          m.tm_cur = e->d_tmaps + i * 6 + lc;
+          m.tm_u = e->d_tmaps + i * 6 + 3;
+          m.tm_v = e->d_tmaps + i * 6 + 4;
+          m.tm_dp = e->d_tmaps + i * 6 + 5;
+        }
       }
       ECK(cudaMemcpy(e->d_mix[r], t.data(), nb * sizeof(MixBasin), cudaMemcpyHostToDevice), "mix table");
     } else {
@@ -261,8 +329,11 @@ int prime(hyc_ens *e) {
 int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
   ECK(cudaMemsetAsync(e->d_head + h, 0, sizeof(int), st), "queue reset");
   cudaError_t c;
-  if (e->prec == HYC_PREC_MIXED)
-    c = hyc::launch_mix_fct2(e->shape, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, st);
+  if (e->prec == HYC_PREC_MIXED && e->use_tma)
+    c = hyc::launch_mix_fct2_tma(e->shape, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->prep64,
+                                 e->d_err, st);
+  else if (e->prec == HYC_PREC_MIXED)
+    c = hyc::launch_mix_fct2(e->shape, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->prep64, st);
   else
     c = hyc::launch_fct_queue(advtyp, e->shape, e->d_targs[r], e->d_items, e->nitems, e->d_head + h, e->nsm, st);
   if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "step kernel: %s", cudaGetErrorString(c));
@@ -271,7 +342,7 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
 }
 
 bool shape_ok(const hyc_ens *e, hyc::TileShape t) {
-  if (e->prec == HYC_PREC_MIXED) return hyc::mix_shape_ok(t);
+  if (e->prec == HYC_PREC_MIXED) return e->use_tma ? hyc::mix_tma_shape_ok(t) : hyc::mix_shape_ok(t);
   return (t.tx == 32 && t.ty == 16) || (t.tx == 16 && t.ty == 16);
 }
 
@@ -364,6 +435,16 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
   e->npartial = maxk;
   if (cudaMalloc(&e->d_partial, 2 * maxk * sizeof(double)) != cudaSuccess)
     return bail(efail(nullptr, HYC_ERR_NOMEM, "partials"));
+  if (cudaMalloc(&e->d_err, sizeof(int)) != cudaSuccess || cudaMemset(e->d_err, 0, sizeof(int)) != cudaSuccess)
+    return bail(efail(nullptr, HYC_ERR_NOMEM, "error flag"));
+  if (precision == HYC_PREC_MIXED) {
+    bool all6 = true;
+    for (auto &b : e->b) all6 &= b.nbdy == 6;
+    if (all6 && encode_fn() && cudaMalloc(&e->d_tmaps, nbasin * 6 * sizeof(CUtensorMap)) == cudaSuccess) {
+      e->use_tma = true;
+      e->shape = hyc::TileShape{32, 16};
+    }
+  }
   *out = e;
   return HYC_OK;
 }
@@ -465,6 +546,35 @@ int hyc_ens_set_tile(hyc_ens *e, int32_t tx, int32_t ty) {
   return HYC_OK;
 }
 
+int hyc_ens_set_option(hyc_ens *e, int32_t option, int32_t value) {
+  if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
+  if (option == HYC_OPT_PREP64) {
+    if (e->prec != HYC_PREC_MIXED) return efail(e, HYC_ERR_ARG, "HYC_OPT_PREP64 applies to the mixed form");
+    if (e->prep64 != (value != 0) && e->gexec) {
+      cudaGraphExecDestroy(e->gexec);
+      e->gexec = nullptr;
+    }
+    e->prep64 = value != 0;
+    return HYC_OK;
+  }
+  if (option == HYC_OPT_TMA) {
+    if (e->prec != HYC_PREC_MIXED || (value && !e->d_tmaps))
+      return efail(e, HYC_ERR_ARG, "HYC_OPT_TMA needs the mixed form with nbdy = 6");
+    if (e->use_tma != (value != 0)) {
+      e->use_tma = value != 0;
+      e->shape = hyc::TileShape{32, 16};
+      e->tbl_dt2 = -1.0;
+      e->items_tx = 0;
+      if (e->gexec) {
+        cudaGraphExecDestroy(e->gexec);
+        e->gexec = nullptr;
+      }
+    }
+    return HYC_OK;
+  }
+  return efail(e, HYC_ERR_ARG, "unknown option %d", option);
+}
+
 int hyc_ens_enable_timers(hyc_ens *e, int32_t on) {
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   e->timing = on != 0;
@@ -475,6 +585,9 @@ int hyc_ens_stats(hyc_ens *e, hyc_stats *out, int32_t reset) {
   if (!e || !out) return efail(e, HYC_ERR_ARG, "null argument");
   Dev g(e->device);
   ECK(cudaStreamSynchronize(e->stream), "stats sync");
+  int flag = 0;
+  ECK(cudaMemcpy(&flag, e->d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+  if (flag) return efail(e, HYC_ERR_CUDA, "a step kernel gave up waiting for its TMA loads");
   for (auto &p : e->pending) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, p.first, p.second) == cudaSuccess) {
@@ -497,7 +610,8 @@ int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32
     return efail(e, HYC_ERR_UNSUPPORTED, "ensemble advtyp %d not available for this precision", advtyp);
   Dev g(e->device);
   int rc;
-  if ((rc = build_items(e)) || (rc = build_tables(e, delt1)) || (rc = ensure_heads(e, nsteps)) || (rc = prime(e)))
+  if ((rc = build_items(e)) || (e->use_tma && (rc = encode_maps(e))) || (rc = build_tables(e, delt1)) ||
+      (rc = ensure_heads(e, nsteps)) || (rc = prime(e)))
     return rc;
   cudaEvent_t a = nullptr, z = nullptr;
   if (e->timing) {
@@ -560,7 +674,7 @@ int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32
 int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t *ty, double *ms_out) {
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   Dev g(e->device);
-  static const hyc::TileShape cands[] = {{32, 16}, {64, 16}, {32, 32}, {64, 8}, {128, 8}, {16, 16}};
+  static const hyc::TileShape cands[] = {{32, 16}, {64, 16}, {32, 32}, {64, 8}, {128, 8}, {16, 16}, {32, 8}};
   hyc::TileShape best = e->shape;
   float best_ms = 1e30f;
   const hyc::TileShape keep = e->shape;
@@ -573,7 +687,9 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
     if (!shape_ok(e, c)) continue;
     e->shape = c;
     e->tbl_dt2 = -1.0;
-    if ((rc = build_items(e)) || (rc = build_tables(e, delt1)) || (rc = ensure_heads(e, 1))) break;
+    if ((rc = build_items(e)) || (e->use_tma && (rc = encode_maps(e))) || (rc = build_tables(e, delt1)) ||
+        (rc = ensure_heads(e, 1)))
+      break;
     // the step kernel writes only the spare level: the state is unchanged
     if ((rc = enqueue_step(e, advtyp, e->rot, 0, e->stream))) break;  // warm-up
     float tot = 0.f;

@@ -70,7 +70,7 @@ __device__ __forceinline__ float comp_div(float a, float b, float c, float d) {
   return s + ((e1 + e2) + e3);
 }
 
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, bool PREP64>
 __device__ __forceinline__ void mix_fct2_item(const MixBasin &B, const int tile, unsigned char *smraw) {
   using G = MixGeom<TX, TY>;
   constexpr int RX = G::RX, RY = G::RY, N = G::N;
@@ -115,19 +115,30 @@ __device__ __forceinline__ void mix_fct2_item(const MixBasin &B, const int tile,
       DPD[t] = in ? dk[o] : 0.0;
     }
     __syncthreads();
-    // FP64 thickness prep (mod_tsadvc.F90:1931-1938), FP32 factors out
+    // thickness prep (mod_tsadvc.F90:1931-1938) -> FP32 factors
+    //   W = (fco+onemu)/(fcn+onemu), R = 1/(fcn+onemu), QF = fcn*scal/delt1
     for (int t = threadIdx.x; t < N; t += NT) {
       const int bb = t / RX, aa = t - bb * RX;
-      double fdv = 0.0;
-      if (aa < RX - 1 && bb < RY - 1)
-        fdv = (((double)U[t + 1] - (double)U[t]) + ((double)V[t + RX] - (double)V[t])) * dt2 * SCI[t];
-      const double d = DPD[t];
-      const double fco = kmax(d + fdv, 0.0), fcn = kmax(d, 0.0);
-      const double hn = fcn + kOnemu;
-      const double r = 1.0 / hn;
-      W[t] = (float)((fco + kOnemu) * r);
-      R[t] = (float)r;
-      QF[t] = (float)fcn * QS[t];
+      const bool face = aa < RX - 1 && bb < RY - 1;
+      if (PREP64) {  // in FP64, as the reference
+        double fdv = 0.0;
+        if (face) fdv = (((double)U[t + 1] - (double)U[t]) + ((double)V[t + RX] - (double)V[t])) * dt2 * SCI[t];
+        const double d = DPD[t];
+        const double fco = kmax(d + fdv, 0.0), fcn = kmax(d, 0.0);
+        const double r = 1.0 / (fcn + kOnemu);
+        W[t] = (float)((fco + kOnemu) * r);
+        R[t] = (float)r;
+        QF[t] = (float)fcn * QS[t];
+      } else {  // in FP32 on the FP32 pipe: compensated divergence, W = 1 + div*R
+        const float onemu = (float)kOnemu;
+        const float fdv = face ? comp_div(U[t + 1], U[t], V[t + RX], V[t]) * DS[t] : 0.f;
+        const float d = (float)DPD[t];
+        const float fcn = fmaxf(d, 0.f);
+        const float r = __frcp_rn(fcn + onemu);
+        W[t] = (d + fdv > 0.f) ? (d >= 0.f ? fmaf(fdv, r, 1.f) : (d + fdv + onemu) * r) : onemu * r;
+        R[t] = r;
+        QF[t] = fcn * QS[t];
+      }
     }
     __syncthreads();
 
@@ -269,7 +280,7 @@ __device__ __forceinline__ void mix_fct2_item(const MixBasin &B, const int tile,
   (void)dt2f;
 }
 
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, bool PREP64>
 __global__ void __launch_bounds__(NT, 2) mix_fct2_queue_kernel(const MixBasin *__restrict__ basins,
                                                            const int4 *__restrict__ items, int nitems, int *head) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -281,17 +292,17 @@ __global__ void __launch_bounds__(NT, 2) mix_fct2_queue_kernel(const MixBasin *_
     __syncthreads();
     if (it >= nitems) break;
     const int4 w = items[it];
-    mix_fct2_item<TX, TY, NT>(basins[w.x], w.y, smraw);
+    mix_fct2_item<TX, TY, NT, PREP64>(basins[w.x], w.y, smraw);
     __syncthreads();
   }
 }
 
 template <int TX, int TY, int NT>
 static cudaError_t launch_mix(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm,
-                              cudaStream_t s) {
+                              bool prep64, cudaStream_t s) {
   constexpr size_t smem = MixGeom<TX, TY>::smem_bytes;
   static_assert(smem <= 227 * 1024, "tile does not fit");
-  auto kern = mix_fct2_queue_kernel<TX, TY, NT>;
+  auto kern = prep64 ? mix_fct2_queue_kernel<TX, TY, NT, true> : mix_fct2_queue_kernel<TX, TY, NT, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
@@ -308,12 +319,12 @@ bool mix_shape_ok(TileShape t) {
 }
 
 cudaError_t launch_mix_fct2(TileShape t, const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm,
-                            cudaStream_t s) {
-  if (t.tx == 32 && t.ty == 16) return launch_mix<32, 16, 256>(basins, items, nitems, head, nsm, s);
-  if (t.tx == 64 && t.ty == 16) return launch_mix<64, 16, 256>(basins, items, nitems, head, nsm, s);
-  if (t.tx == 32 && t.ty == 32) return launch_mix<32, 32, 256>(basins, items, nitems, head, nsm, s);
-  if (t.tx == 64 && t.ty == 8) return launch_mix<64, 8, 256>(basins, items, nitems, head, nsm, s);
-  if (t.tx == 128 && t.ty == 8) return launch_mix<128, 8, 256>(basins, items, nitems, head, nsm, s);
+                            bool prep64, cudaStream_t s) {
+  if (t.tx == 32 && t.ty == 16) return launch_mix<32, 16, 256>(basins, items, nitems, head, nsm, prep64, s);
+  if (t.tx == 64 && t.ty == 16) return launch_mix<64, 16, 256>(basins, items, nitems, head, nsm, prep64, s);
+  if (t.tx == 32 && t.ty == 32) return launch_mix<32, 32, 256>(basins, items, nitems, head, nsm, prep64, s);
+  if (t.tx == 64 && t.ty == 8) return launch_mix<64, 8, 256>(basins, items, nitems, head, nsm, prep64, s);
+  if (t.tx == 128 && t.ty == 8) return launch_mix<128, 8, 256>(basins, items, nitems, head, nsm, prep64, s);
   return cudaErrorInvalidValue;
 }
 

@@ -43,7 +43,7 @@ EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "
            "hyc_version", "hyc_enable_timers", "hyc_get_stats", "hyc_advem_noalloc", "hyc_ens_create",
            "hyc_ens_destroy", "hyc_ens_set_stream", "hyc_ens_put", "hyc_ens_get", "hyc_ens_set_tile",
            "hyc_ens_tune", "hyc_ens_step", "hyc_ens_content", "hyc_ens_stats", "hyc_ens_enable_timers",
-           "hyc_ens_last_error")
+           "hyc_ens_last_error", "hyc_ens_set_option")
 ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
 TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4}
@@ -113,6 +113,7 @@ def lib() -> C.CDLL:
         L.hyc_ens_content.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.POINTER(C.c_double)]
         L.hyc_ens_stats.argtypes = [vp, C.POINTER(Stats), C.c_int32]
         L.hyc_ens_enable_timers.argtypes = [vp, C.c_int32]
+        L.hyc_ens_set_option.argtypes = [vp, C.c_int32, C.c_int32]
         L.hyc_ens_last_error.argtypes = [vp]
         L.hyc_ens_last_error.restype = C.c_char_p
         L.hyc_advem_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp,
@@ -362,6 +363,14 @@ class Ensemble:
 
     def enable_timers(self, on: bool = True):
         self._chk(lib().hyc_ens_enable_timers(self._h, int(bool(on))))
+
+    def set_tma(self, on: bool):
+        """Mixed form: TMA-staged, double-buffered kernel (True) or plain loads."""
+        self._chk(lib().hyc_ens_set_option(self._h, 2, int(bool(on))))
+
+    def set_prep64(self, on: bool):
+        """Mixed form: thickness prep in FP64 (True, default) or compensated FP32."""
+        self._chk(lib().hyc_ens_set_option(self._h, 1, int(bool(on))))
 
     def stats(self, reset: bool = False) -> dict:
         s = Stats()

@@ -281,6 +281,20 @@ int hyc_ens_step(hyc_ens *ens, int32_t advtyp, double delt1, int32_t nsteps, int
  */
 int hyc_ens_content(hyc_ens *ens, int32_t basin, int32_t tracer, int32_t what, double delt1, double *sum);
 int hyc_ens_stats(hyc_ens *ens, hyc_stats *out, int32_t reset);
+/*
+ * Options.  HYC_OPT_PREP64 (mixed form only; default 1): 1 = the per cell
+ * and layer thickness prep (continuity fco, the division factors
+ * (fco+onemu)/(fcn+onemu) and 1/(fcn+onemu)) runs in FP64; 0 = it runs in
+ * FP32 with a compensated (two-sum) divergence and W = 1 + div/(fcn+onemu),
+ * which rounds the same factors to FP32 within one ulp without using the
+ * FP64 pipe (GB300 issues FP64 at ~1/72 of the FP32 rate).
+ */
+#define HYC_OPT_PREP64 1
+/* HYC_OPT_TMA (mixed form; default 1 when every basin has nbdy = 6): stage
+ * tiles with the Tensor Memory Accelerator, double-buffered (1), or with
+ * plain loads (0). */
+#define HYC_OPT_TMA 2
+int hyc_ens_set_option(hyc_ens *ens, int32_t option, int32_t value);
 int hyc_ens_enable_timers(hyc_ens *ens, int32_t on);
 const char *hyc_ens_last_error(const hyc_ens *ens);
 

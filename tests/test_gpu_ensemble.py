@@ -113,18 +113,21 @@ def test_tune_keeps_state(cuda):
     load(ens, members)
     before = [get_cur(ens, i, m) for i, m in enumerate(members)]
     tx, ty, ms = ens.tune(2, DELT1)
-    assert (tx, ty) in [(32, 16), (64, 16), (32, 32), (64, 8), (128, 8)] and ms > 0
+    assert (tx, ty) in [(32, 16), (64, 16), (32, 32), (64, 8), (128, 8), (32, 8)] and ms > 0
     after = [get_cur(ens, i, m) for i, m in enumerate(members)]
     for a, b in zip(before, after):
         assert np.array_equal(a, b)
     ens.close()
 
 
-def test_mixed_one_step_error(cuda):
+@pytest.mark.parametrize("prep64", [True, False])
+def test_mixed_one_step_error(cuda, prep64):
     """From identical inputs, one FP32-mixed step is within 1e-6 (relative to
-    each tracer's max |value|) of the FP64 oracle."""
+    each tracer's max |value|) of the FP64 oracle, with the thickness prep in
+    FP64 or in compensated FP32."""
     members = make_members()
     ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
+    ens.set_prep64(prep64)
     load(ens, members)
     ens.step(2, DELT1, 1)
     for i, m in enumerate(members):
@@ -137,14 +140,17 @@ def test_mixed_one_step_error(cuda):
     ens.close()
 
 
-@pytest.mark.parametrize("prec,cons_tol,err_tol", [("fp64", 1e-13, 0.0), ("mixed", 1e-6, 1e-4)])
-def test_ensemble_multistep_conservation_extrema(cuda, prec, cons_tol, err_tol):
+@pytest.mark.parametrize("prec,prep64,cons_tol,err_tol",
+                         [("fp64", True, 1e-13, 0.0), ("mixed", True, 1e-6, 1e-4), ("mixed", False, 1e-6, 1e-4)])
+def test_ensemble_multistep_conservation_extrema(cuda, prec, prep64, cons_tol, err_tol):
     """20 steps: tracer content conserved (FP64 to round-off), no new extrema,
     and the FP32-mixed drift from the oracle stays within the envelope of the
     leapfrog-FCT dynamics (an FP64 run perturbed by one FP32 rounding of its
     inputs already drifts ~1e-5 in 20 steps)."""
     members = make_members()
     ens = hycadv.Ensemble([spec_of(m) for m in members], precision=prec)
+    if prec == "mixed":
+        ens.set_prep64(prep64)
     load(ens, members)
     nsteps = 20
     start = [(m["trc"][..., m["g"].masks["ip"] != 0].min(), m["trc"][..., m["g"].masks["ip"] != 0].max())
