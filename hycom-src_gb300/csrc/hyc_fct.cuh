@@ -291,14 +291,25 @@ __global__ void __launch_bounds__(256, 2)
     fct_queue_kernel(const TileArgs *__restrict__ basins, const int4 *__restrict__ items, int nitems, int *head) {
   extern __shared__ __align__(16) double sm[];
   __shared__ int cur;
+  __shared__ int cur_basin;
+  __shared__ __align__(16) TileArgs sa;  // the item's basin, staged once (read many times below)
+  if (threadIdx.x == 0) cur_basin = -1;
   for (;;) {
     if (threadIdx.x == 0) cur = atomicAdd(head, 1);
     __syncthreads();
     const int it = cur;
-    __syncthreads();
     if (it >= nitems) break;
     const int4 w = items[it];
-    fct_tile_body<SCHEME, TX, TY>(basins[w.x], w.y, w.z, sm);
+    if (w.x != cur_basin) {  // uniform: every thread read the same item
+      __syncthreads();
+      const int *src = reinterpret_cast<const int *>(basins + w.x);
+      int *dst = reinterpret_cast<int *>(&sa);
+      for (int q = threadIdx.x; q < (int)(sizeof(TileArgs) / 4); q += blockDim.x) dst[q] = src[q];
+      __syncthreads();
+      if (threadIdx.x == 0) cur_basin = w.x;
+    }
+    __syncthreads();
+    fct_tile_body<SCHEME, TX, TY>(sa, w.y, w.z, sm);
   }
 }
 

@@ -23,6 +23,9 @@ static cudaError_t launch_kernel(K kern, size_t smem, const TileArgs &a, int nla
   if (dev >= 64 || !(attr_done >> dev & 1ULL)) {  // one bit per device ordinal < 64
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    // ask for the largest shared-memory carveout so that two CTAs fit per SM
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
     if (dev < 64) attr_done |= 1ULL << dev;
   }
   dim3 grid((unsigned)(a.ntx * a.nty), (unsigned)nlayers);
@@ -79,6 +82,8 @@ static cudaError_t launch_queue_one(const TileArgs *basins, const int4 *items, i
   constexpr size_t smem = FctGeom<TX, TY>::smem_bytes;
   auto kern = fct_queue_kernel<S, TX, TY>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);

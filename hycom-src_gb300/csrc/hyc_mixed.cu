@@ -305,6 +305,8 @@ static cudaError_t launch_mix(const MixBasin *basins, const int4 *items, int nit
   auto kern = prep64 ? mix_fct2_queue_kernel<TX, TY, NT, true> : mix_fct2_queue_kernel<TX, TY, NT, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
   if (e != cudaSuccess) return e;

@@ -404,6 +404,8 @@ static cudaError_t launch_tma(const MixBasin *basins, const int4 *items, int nit
   auto kern = prep64 ? mix_fct2_tma_kernel<TX, TY, 256, true> : mix_fct2_tma_kernel<TX, TY, 256, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
   if (e != cudaSuccess) return e;
