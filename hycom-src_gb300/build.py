@@ -30,6 +30,7 @@ UNITS = {
     "hyc_noalloc.cu": ["-lineinfo"],
     "hyc_mixed.cu": ["-lineinfo"],
     "hyc_mixed_tma.cu": ["-lineinfo"],
+    "hyc_mixed_col.cu": ["-lineinfo"],
     "hyc_ens_host.cpp": [],
 }
 

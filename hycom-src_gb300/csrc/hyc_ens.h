@@ -30,6 +30,10 @@ struct MixBasin {
   // TMA descriptors (device memory) for the current tile shape: levels t-1
   // and t (3-D: ld1 x ld2 x ntr*kdm, FP32), uflx, vflx (FP32) and dp (FP64)
   const CUtensorMap *tm_old, *tm_cur, *tm_u, *tm_v, *tm_dp;
+  // column kernel: (dt2*scp2i, scp2/dt2) per cell, rows per segment
+  const float2 *dsqs;
+  int seg;
+  int pad2;
 };
 
 bool mix_shape_ok(TileShape t);
@@ -39,6 +43,13 @@ cudaError_t launch_mix_fct2(TileShape t, const MixBasin *basins, const int4 *ite
 bool mix_tma_shape_ok(TileShape t);
 cudaError_t launch_mix_fct2_tma(TileShape t, const MixBasin *basins, const int4 *items, int nitems, int *head,
                                 int nsm, bool prep64, int *err, cudaStream_t s);
+// one warp per 32-column strip (26 updated), segments of `seg` rows
+constexpr int kColStrip = 26;
+cudaError_t launch_mix_fct2_col(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm, int nq,
+                                bool prep64, cudaStream_t s);
+cudaError_t launch_dsqs(const double *scp2, const double *scp2i, double dt2, long long n, float2 *out,
+                        cudaStream_t s);
+
 // TMA box width (elements) of a tile shape: TX + 12 for the nbdy = 6 halo
 inline int tma_box_x(TileShape t) { return (t.tx + 9 + 3) / 4 * 4; }
 inline int tma_box_y(TileShape t) { return t.ty + 6; }

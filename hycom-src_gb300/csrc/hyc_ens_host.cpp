@@ -30,6 +30,7 @@ struct EBasin {
   void *uflx = nullptr, *vflx = nullptr;  // FP32 (mixed) or FP64
   double *dp = nullptr;
   void *lev[3] = {nullptr, nullptr, nullptr};  // tracer state, physical levels
+  float2 *dsqs = nullptr;                       // column kernel metric factors (mixed form)
   long long work = 0;                           // cells*layers*tracers, for queue ordering
 };
 
@@ -46,6 +47,7 @@ struct hyc_ens {
   hyc::TileShape shape{32, 16};
   bool prep64 = true;  // FP32-mixed: thickness prep in FP64 (else compensated FP32)
   bool use_tma = false;  // FP32-mixed: TMA-staged kernel (needs nbdy = 6 everywhere)
+  int maxntr = 1;        // largest tracer count (column kernel processes tracers in pairs)
   CUtensorMap *d_tmaps = nullptr;  // [nbasin][6]: level 0,1,2, uflx, vflx, dp
   int tm_tx = 0, tm_ty = 0;        // shape the maps were encoded for
   int *d_err = nullptr;            // device error flag (bounded waits that gave up)
@@ -105,6 +107,9 @@ struct Dev {
 
 size_t esz(const hyc_ens *e) { return e->prec == HYC_PREC_MIXED ? 4 : 8; }
 
+// tile shapes with tx == 26 select the column-strip kernel (ty = rows per segment)
+bool is_col(hyc::TileShape t) { return t.tx == hyc::kColStrip; }
+
 void free_all(hyc_ens *e) {
   for (auto &b : e->b) {
     cudaFree(b.msk);
@@ -113,6 +118,7 @@ void free_all(hyc_ens *e) {
     cudaFree(b.uflx);
     cudaFree(b.vflx);
     cudaFree(b.dp);
+    cudaFree(b.dsqs);
     for (auto &l : b.lev) cudaFree(l);
   }
   for (int r = 0; r < 3; r++) {
@@ -189,6 +195,11 @@ int build_tables(hyc_ens *e, double dt2) {
   if (e->tbl_dt2 == dt2) return HYC_OK;
   ECK(cudaStreamSynchronize(e->stream), "tables sync");  // earlier steps may still read the tables
   const int nb = (int)e->b.size();
+  if (e->prec == HYC_PREC_MIXED)
+    for (auto &b : e->b) {
+      if (!b.dsqs) ECK(cudaMalloc(&b.dsqs, b.slice * sizeof(float2)), "dsqs");
+      ECK(hyc::launch_dsqs(b.scp2, b.scp2i, dt2, b.slice, b.dsqs, e->stream), "dsqs");
+    }
   for (int r = 0; r < 3; r++) {
     const int lo = r, lc = (r + 1) % 3, ln = (r + 2) % 3;
     if (e->prec == HYC_PREC_MIXED) {
@@ -218,6 +229,8 @@ int build_tables(hyc_ens *e, double dt2) {
         m.fold = (const float *)b.lev[lo];
         m.fcur = (const float *)b.lev[lc];
         m.fnew = (float *)b.lev[ln];
+        m.seg = e->shape.ty;
+        m.dsqs = b.dsqs;
         if (e->d_tmaps) {
           m.tm_old = e->d_tmaps + i * 6 + lo;
           m.tm_cur = e->d_tmaps + i * 6 + lc;
@@ -281,6 +294,11 @@ int build_items(hyc_ens *e) {
   for (int i = 0; i < (int)e->b.size(); i++) {
     const EBasin &b = e->b[i];
     const int ntx = (b.idm + e->shape.tx - 1) / e->shape.tx, nty = (b.jdm + e->shape.ty - 1) / e->shape.ty;
+    if (is_col(e->shape)) {  // (basin, strip, segment), all layers and tracers
+      for (int sg = 0; sg < nty; sg++)
+        for (int st = 0; st < ntx; st++) w.push_back({(long long)b.kdm * b.ntr, make_int4(i, st, sg, 0)});
+      continue;
+    }
     for (int t = 0; t < ntx * nty; t++) {
       if (per_layer) {
         for (int k = 0; k < b.kdm; k++) w.push_back({(long long)b.ntr, make_int4(i, t, k, 0)});
@@ -329,7 +347,9 @@ int prime(hyc_ens *e) {
 int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
   ECK(cudaMemsetAsync(e->d_head + h, 0, sizeof(int), st), "queue reset");
   cudaError_t c;
-  if (e->prec == HYC_PREC_MIXED && e->use_tma)
+  if (e->prec == HYC_PREC_MIXED && is_col(e->shape))
+    c = hyc::launch_mix_fct2_col(e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->maxntr, e->prep64, st);
+  else if (e->prec == HYC_PREC_MIXED && e->use_tma)
     c = hyc::launch_mix_fct2_tma(e->shape, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->prep64,
                                  e->d_err, st);
   else if (e->prec == HYC_PREC_MIXED)
@@ -342,6 +362,7 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
 }
 
 bool shape_ok(const hyc_ens *e, hyc::TileShape t) {
+  if (e->prec == HYC_PREC_MIXED && is_col(t)) return t.ty == 32 || t.ty == 64 || t.ty == 128;
   if (e->prec == HYC_PREC_MIXED) return e->use_tma ? hyc::mix_tma_shape_ok(t) : hyc::mix_shape_ok(t);
   return (t.tx == 32 && t.ty == 16) || (t.tx == 16 && t.ty == 16);
 }
@@ -393,6 +414,7 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
     b.slice = (long long)b.ld1 * b.ld2;
     b.work = (long long)s.idm * s.jdm * s.kdm * s.ntr;
     maxk = std::max(maxk, s.kdm);
+    e->maxntr = std::max(e->maxntr, s.ntr);
     // masks (validated like hyc_adv_init) and metrics, repitched
     std::vector<uint8_t> m((size_t)b.slice, 0);
     std::vector<double> sc((size_t)b.slice, 1.0), si((size_t)b.slice, 1.0);
@@ -440,10 +462,9 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
   if (precision == HYC_PREC_MIXED) {
     bool all6 = true;
     for (auto &b : e->b) all6 &= b.nbdy == 6;
-    if (all6 && encode_fn() && cudaMalloc(&e->d_tmaps, nbasin * 6 * sizeof(CUtensorMap)) == cudaSuccess) {
+    if (all6 && encode_fn() && cudaMalloc(&e->d_tmaps, nbasin * 6 * sizeof(CUtensorMap)) == cudaSuccess)
       e->use_tma = true;
-      e->shape = hyc::TileShape{32, 16};
-    }
+    e->shape = hyc::TileShape{hyc::kColStrip, 64};  // column-strip kernel
   }
   *out = e;
   return HYC_OK;
@@ -562,7 +583,7 @@ int hyc_ens_set_option(hyc_ens *e, int32_t option, int32_t value) {
       return efail(e, HYC_ERR_ARG, "HYC_OPT_TMA needs the mixed form with nbdy = 6");
     if (e->use_tma != (value != 0)) {
       e->use_tma = value != 0;
-      e->shape = hyc::TileShape{32, 16};
+      if (!is_col(e->shape)) e->shape = hyc::TileShape{32, 16};
       e->tbl_dt2 = -1.0;
       e->items_tx = 0;
       if (e->gexec) {
@@ -610,8 +631,8 @@ int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32
     return efail(e, HYC_ERR_UNSUPPORTED, "ensemble advtyp %d not available for this precision", advtyp);
   Dev g(e->device);
   int rc;
-  if ((rc = build_items(e)) || (e->use_tma && (rc = encode_maps(e))) || (rc = build_tables(e, delt1)) ||
-      (rc = ensure_heads(e, nsteps)) || (rc = prime(e)))
+  if ((rc = build_items(e)) || (e->use_tma && !is_col(e->shape) && (rc = encode_maps(e))) ||
+      (rc = build_tables(e, delt1)) || (rc = ensure_heads(e, nsteps)) || (rc = prime(e)))
     return rc;
   cudaEvent_t a = nullptr, z = nullptr;
   if (e->timing) {
@@ -674,7 +695,8 @@ int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32
 int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t *ty, double *ms_out) {
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   Dev g(e->device);
-  static const hyc::TileShape cands[] = {{32, 16}, {64, 16}, {32, 32}, {64, 8}, {128, 8}, {16, 16}, {32, 8}};
+  static const hyc::TileShape cands[] = {{32, 16}, {64, 16}, {32, 32}, {64, 8}, {128, 8}, {16, 16}, {32, 8},
+                                         {26, 32}, {26, 64}, {26, 128}};
   hyc::TileShape best = e->shape;
   float best_ms = 1e30f;
   const hyc::TileShape keep = e->shape;
@@ -687,8 +709,8 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
     if (!shape_ok(e, c)) continue;
     e->shape = c;
     e->tbl_dt2 = -1.0;
-    if ((rc = build_items(e)) || (e->use_tma && (rc = encode_maps(e))) || (rc = build_tables(e, delt1)) ||
-        (rc = ensure_heads(e, 1)))
+    if ((rc = build_items(e)) || (e->use_tma && !is_col(e->shape) && (rc = encode_maps(e))) ||
+        (rc = build_tables(e, delt1)) || (rc = ensure_heads(e, 1)))
       break;
     // the step kernel writes only the spare level: the state is unchanged
     if ((rc = enqueue_step(e, advtyp, e->rot, 0, e->stream))) break;  // warm-up
