@@ -46,7 +46,7 @@ cudaError_t launch_mix_fct2_tma(TileShape t, const MixBasin *basins, const int4 
 // one warp per 32-column strip (26 updated), segments of `seg` rows
 constexpr int kColStrip = 26;
 cudaError_t launch_mix_fct2_col(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm, int nq,
-                                bool prep64, cudaStream_t s);
+                                bool prep64, int seg, cudaStream_t s);
 cudaError_t launch_dsqs(const double *scp2, const double *scp2i, double dt2, long long n, float2 *out,
                         cudaStream_t s);
 

@@ -348,7 +348,8 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
   ECK(cudaMemsetAsync(e->d_head + h, 0, sizeof(int), st), "queue reset");
   cudaError_t c;
   if (e->prec == HYC_PREC_MIXED && is_col(e->shape))
-    c = hyc::launch_mix_fct2_col(e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->maxntr, e->prep64, st);
+    c = hyc::launch_mix_fct2_col(e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->maxntr, e->prep64,
+                                 e->shape.ty, st);
   else if (e->prec == HYC_PREC_MIXED && e->use_tma)
     c = hyc::launch_mix_fct2_tma(e->shape, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->prep64,
                                  e->d_err, st);

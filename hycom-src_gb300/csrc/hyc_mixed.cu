@@ -60,14 +60,13 @@ __device__ __forceinline__ float two_sum(float a, float b, float &e) {
   return s;
 }
 
-// ((a - b) + (c - d)) with the rounding errors of the three additions added
-// back: the compensated flux divergence of four face fluxes.
+// ((a - b) + (c - d)) with the rounding errors of the two differences added
+// back (two-sum): the compensated flux divergence of four face fluxes.
 __device__ __forceinline__ float comp_div(float a, float b, float c, float d) {
-  float e1, e2, e3;
+  float e1, e2;
   const float s1 = two_sum(a, -b, e1);
   const float s2 = two_sum(c, -d, e2);
-  const float s = two_sum(s1, s2, e3);
-  return s + ((e1 + e2) + e3);
+  return (s1 + s2) + (e1 + e2);
 }
 
 template <int TX, int TY, int NT, bool PREP64>

@@ -35,12 +35,15 @@ __device__ __forceinline__ float two_sum(float a, float b, float &e) {
   e = (a - (s - bb)) + (b - bb);
   return s;
 }
+// ((a - b) + (c - d)) with the rounding errors of the two differences added
+// back (two-sum): the cancellation between the large, nearly equal fluxes
+// through opposite faces is exact; the last addition rounds relative to the
+// divergence itself.
 __device__ __forceinline__ float comp_div(float a, float b, float c, float d) {
-  float e1, e2, e3;
+  float e1, e2;
   const float s1 = two_sum(a, -b, e1);
   const float s2 = two_sum(c, -d, e2);
-  const float s = two_sum(s1, s2, e3);
-  return s + ((e1 + e2) + e3);
+  return (s1 + s2) + (e1 + e2);
 }
 __device__ __forceinline__ float up(float x) { return __shfl_up_sync(0xffffffffu, x, 1); }
 __device__ __forceinline__ float dn(float x) { return __shfl_down_sync(0xffffffffu, x, 1); }
@@ -65,8 +68,15 @@ struct TrState {
 
 template <int NQ, bool PREP64>
 __global__ void __launch_bounds__(128)
-    mix_fct2_col_kernel(const MixBasin *__restrict__ basins, const int4 *__restrict__ items, int nitems, int *head) {
+    mix_fct2_col_kernel(const MixBasin *__restrict__ basins, const int4 *__restrict__ items, int nitems, int *head,
+                        int rows_max) {
   const int lane = threadIdx.x & 31;
+  // per warp: the masks and metric factors of its item's rows, read once per
+  // item instead of once per layer
+  extern __shared__ __align__(16) unsigned char csm[];
+  const int wid = threadIdx.x >> 5;
+  float2 *sdq = reinterpret_cast<float2 *>(csm) + (size_t)wid * rows_max * 32;
+  uint8_t *smk = csm + (size_t)(blockDim.x >> 5) * rows_max * 32 * sizeof(float2) + (size_t)wid * rows_max * 32;
   for (;;) {
     int it = 0;
     if (lane == 0) it = atomicAdd(head, 1);
@@ -83,6 +93,16 @@ __global__ void __launch_bounds__(128)
     const double dt2 = B.dt2;
     const float onemu = (float)kOnemu;
     const long long cbase = colin ? (long long)(i + nb - 1) : 0;
+    const int jr0 = j0 - 3, nrows = j1 + 2 - jr0 + 1;  // rows j0-3 .. j1+2
+    __syncwarp();
+    for (int r = 0; r < nrows; r++) {
+      const int J = jr0 + r;
+      const bool in = colin && J >= 1 - nb && J <= jj + nb;
+      const long long o = cbase + (long long)(J + nb - 1) * ld1;
+      smk[r * 32 + lane] = in ? B.msk[o] : 0;
+      sdq[r * 32 + lane] = in ? B.dsqs[o] : make_float2(0.f, 0.f);
+    }
+    __syncwarp();
 
     for (int q0 = 0; q0 < B.ntr; q0 += NQ) {
       const int nq = min(NQ, B.ntr - q0);
@@ -111,11 +131,11 @@ __global__ void __launch_bounds__(128)
                             float2 &dq, double &sci) {
           const bool in = colin && J >= 1 - nb && J <= jj + nb;
           const long long o = cbase + (long long)(J + nb - 1) * ld1;
-          m = in ? B.msk[o] : 0u;
+          m = smk[(J - jr0) * 32 + lane];
           u = in ? uk[o] : 0.f;
           v = in ? vk[o] : 0.f;
           d = in ? dk[o] : 0.0;
-          dq = in ? B.dsqs[o] : make_float2(0.f, 0.f);
+          dq = sdq[(J - jr0) * 32 + lane];
           sci = (PREP64 && in) ? B.scp2i[o] : 0.0;
 #pragma unroll
           for (int q = 0; q < NQ; q++) {
@@ -128,6 +148,7 @@ __global__ void __launch_bounds__(128)
         double dN, sciN;
         float2 dqN;
         load_row(j0 - 3, mN, fN, cN, uN, vN, dN, dqN, sciN);
+#pragma unroll 2
         for (int J = j0 - 3; J <= j1 + 2; J++) {
           const unsigned m0 = mN;
           float f0[NQ], c0[NQ];
@@ -294,13 +315,17 @@ cudaError_t launch_dsqs(const double *scp2, const double *scp2i, double dt2, lon
 }
 
 cudaError_t launch_mix_fct2_col(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm, int nq,
-                                bool prep64, cudaStream_t s) {
+                                bool prep64, int seg, cudaStream_t s) {
+  const int rows_max = seg + 6;
+  const size_t smem = (size_t)4 * rows_max * 32 * (sizeof(float2) + 1);
   auto pick = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
-    kern<<<nsm * per_sm, 128, 0, s>>>(basins, items, nitems, head);
+    kern<<<nsm * per_sm, 128, smem, s>>>(basins, items, nitems, head, rows_max);
     return cudaGetLastError();
   };
   if (nq >= 2) return prep64 ? pick(mix_fct2_col_kernel<2, true>) : pick(mix_fct2_col_kernel<2, false>);
