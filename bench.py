@@ -44,6 +44,10 @@ WORKLOADS = {
     "c1": dict(nx=4500, ny=3298, kdm=41, periodic=True, courant=0.8, delt1=240.0, seed=1),
     # closed basin 257x193x10, T+S, FCT2, FP64 (CPU-sized case)
     "c0": dict(nx=257, ny=193, kdm=10, periodic=False, courant=0.5, delt1=1800.0, seed=7),
+    # precision form: the c1 basin with T, S and 8 passive tracers (log-uniform, sharp fronts)
+    "c2": dict(nx=4500, ny=3298, kdm=41, periodic=True, courant=0.8, delt1=240.0, seed=1, ntr=10),
+    # batching form: 96 closed basins, nx 120-1500, ny 90-1100, kdm 22/32/41, 2-6 tracers
+    "c3": dict(nbasin=96, periodic=False, courant=0.5, delt1=1800.0, seed=3, steps=30),
 }
 SCHEME_NAMES = {0: "PCM", 1: "MPDATA", 2: "FCT2", 4: "FCT4"}
 FALLBACK_HBM_GBS = 6800.0
@@ -294,6 +298,198 @@ def run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream, precs=("fp64"
     return out
 
 
+def c3_members(wl):
+    """Seeded sizes of the 96-basin ensemble (uneven nx, ny, kdm, tracers)."""
+    import numpy as np
+
+    rng = np.random.default_rng(wl["seed"])
+    out = []
+    for bi in range(wl["nbasin"]):
+        out.append(dict(nx=int(rng.integers(120, 1501)), ny=int(rng.integers(90, 1101)),
+                        kdm=int(rng.choice([22, 32, 41])), ntr=int(rng.integers(2, 7)), seed=1000 + bi))
+    return out
+
+
+TRACER_KINDS = ("temp", "saln")
+
+
+def member_geometry(m, wl):
+    """Basin, bigrid masks and the ensemble spec of one member (host only)."""
+    import hycadv
+    from hycadv import synth
+
+    b = synth.make_basin(m["nx"], m["ny"], wl["periodic"], m["seed"])
+    _, masks, nreg = hycadv.bigrid(b.depth, b.nbdy)
+    sc, si = b.metrics()
+    spec = dict(idm=b.nx, jdm=b.ny, kdm=m["kdm"], nbdy=b.nbdy, nreg=nreg, ntr=m["ntr"], ip=masks["ip"],
+                iu=masks["iu"], iv=masks["iv"], scp2=sc, scp2i=si)
+    return b, masks, spec
+
+
+def load_member(ens, i, m, geo, wl, dev):
+    """Generate member i's flow and tracers on the device and put them one
+    tracer at a time (T, S, then passive tracers); returns each tracer's
+    (min, max) over sea cells of both input levels."""
+    import torch
+
+    from hycadv import synth
+
+    b, masks, spec = geo
+    kdm = spec["kdm"]
+    dp, uflx, vflx = synth.flow_fields(b, masks, kdm, m["seed"], wl["courant"], wl["delt1"], dev)
+    ens.put(i, "uflx", uflx)
+    ens.put(i, "vflx", vflx)
+    ens.put(i, "dp", dp[1].contiguous())
+    del dp, uflx, vflx
+    sea = sea_mask(b, masks, dev)
+    bounds = []
+    for q in range(spec["ntr"]):
+        kind = TRACER_KINDS[q] if q < 2 else "passive"
+        lv = synth.tracer_levels(b, kind, kdm, m["seed"], q=max(q - 2, 0), device=dev)
+        ens.put(i, "old", lv[1].contiguous(), s0=q * kdm, ns=kdm)
+        ens.put(i, "cur", lv[0].contiguous(), s0=q * kdm, ns=kdm)
+        vals = lv[:, :, sea]
+        bounds.append((float(vals.min()), float(vals.max())))
+        del lv, vals
+    return bounds
+
+
+def sea_mask(b, masks, dev):
+    import torch
+
+    ip = torch.as_tensor(masks["ip"], device=dev) != 0
+    inner = torch.zeros_like(ip)
+    inner[b.J, b.I] = True
+    return ip & inner
+
+
+def run_ensemble_workload(args, wl, dev):
+    """c2 (precision form) and c3 (batching form) through the ensemble API.
+
+    Every form (FP64 plain, FP32-mixed with FP64 thickness prep, FP32-mixed
+    with compensated FP32 prep) is loaded from the same seeded inputs,
+    advanced one step and compared, tracer by tracer over sea cells, with
+    the FP64 form's step (which is bit-identical to the oracle's): max and
+    RMS error relative to the tracer's max |value|, the one-step change of
+    tracer content, and the new level against the inputs' extrema.  Then
+    it is timed over K steps replayed from one CUDA graph.  Tile shapes come
+    from the library's autotuner."""
+    import torch
+
+    import hycadv
+
+    if args.workload == "c3":
+        members = c3_members(wl)
+        if args.layers:
+            for m in members:
+                m["kdm"] = args.layers
+        steps = max(args.steps, wl["steps"])
+    else:
+        members = [dict(nx=wl["nx"], ny=wl["ny"], kdm=args.layers or wl["kdm"], ntr=wl["ntr"], seed=wl["seed"])]
+        steps = args.steps
+    forms = [f for f in args.ens_forms.split(",") if f]
+    if forms[0] != "fp64":
+        raise SystemExit("--ens-forms must start with fp64 (the reference the others are compared with)")
+    t_start = time.perf_counter()
+    geos = [member_geometry(m, wl) for m in members]
+    specs = [g[2] for g in geos]
+    ups = sum(s["idm"] * s["jdm"] * s["kdm"] * s["ntr"] for s in specs)
+    peak, peak_kind = peak_hbm()
+    res, refs = {}, {}
+    for form in forms:
+        prec = "fp64" if form == "fp64" else "mixed"
+        ens = hycadv.Ensemble(specs, precision=prec)
+        if prec == "mixed":
+            ens.set_prep64(form == "mixed")
+        t0 = time.perf_counter()
+        bounds = [load_member(ens, i, m, geos[i], wl, dev) for i, m in enumerate(members)]
+        torch.cuda.synchronize(dev)
+        torch.cuda.empty_cache()
+        t_load = time.perf_counter() - t0
+        tx, ty, _ = ens.tune(2, wl["delt1"])
+        c_old = [[ens.content(i, q, "old", wl["delt1"]) for q in range(s["ntr"])] for i, s in enumerate(specs)]
+        ens.step(2, wl["delt1"], 1)
+        ntr_max = max(s["ntr"] for s in specs)
+        per_q = [{"max_rel": 0.0, "sq": 0.0, "n": 0, "cons": 0.0, "extrema_excess": 0.0} for _ in range(ntr_max)]
+        for i, s in enumerate(specs):
+            b, masks, _ = geos[i]
+            sea = sea_mask(b, masks, dev)
+            kdm = s["kdm"]
+            buf = torch.empty((kdm, b.ld2, b.ld1), dtype=torch.float64, device=dev)
+            for q in range(s["ntr"]):
+                ens.get(i, "cur", buf, s0=q * kdm, ns=kdm)
+                new = buf[:, sea]
+                lo, hi = bounds[i][q]
+                acc = per_q[q]
+                acc["extrema_excess"] = max(acc["extrema_excess"], float(max(lo - new.min(), new.max() - hi, 0.0))
+                                            / max(abs(lo), abs(hi)))
+                c_new = ens.content(i, q, "cur", wl["delt1"])
+                acc["cons"] = max(acc["cons"], abs(c_new - c_old[i][q]) / abs(c_old[i][q]))
+                if form == "fp64":
+                    refs[(i, q)] = new.clone()
+                else:
+                    ref = refs[(i, q)]
+                    scale = float(ref.abs().max())
+                    d = new - ref
+                    acc["max_rel"] = max(acc["max_rel"], float(d.abs().max()) / scale)
+                    acc["sq"] += float(d.pow(2).sum()) / scale ** 2
+                    acc["n"] += d.numel()
+                del new
+            del buf
+        torch.cuda.empty_cache()
+        names = ["temp", "saln"] + [f"passive{q - 1}" for q in range(2, ntr_max)]
+        rep = {}
+        for q, acc in enumerate(per_q):
+            r = {"content_change_one_step": acc["cons"], "new_extrema_rel": acc["extrema_excess"]}
+            if form != "fp64":
+                r["max_rel_err_vs_fp64"] = acc["max_rel"]
+                r["rms_rel_err_vs_fp64"] = (acc["sq"] / max(acc["n"], 1)) ** 0.5
+            rep[names[q]] = r
+        ens.step(2, wl["delt1"], steps, graph=True)  # capture (and warm up)
+        torch.cuda.synchronize(dev)
+        st = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(0) as clk:
+            e0.record(st)
+            ens.step(2, wl["delt1"], steps, graph=True)
+            e1.record(st)
+            torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        s_t = 8 if prec == "fp64" else 4
+        nbytes = sum(s["idm"] * s["jdm"] * s["kdm"] * s["ntr"] * bytes_per_update(s_t, s_t, 8, s["ntr"], s["kdm"])
+                     for s in specs)
+        ach = nbytes / (ms / 1e3) / 1e9
+        res[form] = {"value": ups / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "tile": [tx, ty],
+                     "graph_steps": steps, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
+                     "algorithmic_bytes_per_step": nbytes, "load_seconds": t_load, "per_tracer": rep,
+                     "clocks": clk.summary()}
+        ens.close()
+        del ens
+        torch.cuda.empty_cache()
+    refs.clear()
+    for f in forms[1:]:
+        res[f"{f}_speedup_vs_fp64"] = res[f]["value"] / res["fp64"]["value"]
+    head_form = "mixed-fp32prep" if "mixed-fp32prep" in res else forms[-1]
+    head = res[head_form]
+    if args.workload == "c3":
+        desc = (f"c3: {len(members)} closed basins, nx 120-1500, ny 90-1100, kdm 22/32/41, 2-6 tracers (T, S, "
+                f"passive), FCT2, max Courant {wl['courant']}, delt1 {wl['delt1']} s, {steps}-step CUDA graph")
+    else:
+        desc = (f"c2: periodic-x basin {wl['nx']}x{wl['ny']}x{members[0]['kdm']}, T+S+8 passive tracers "
+                f"(log-uniform 1e-6..1e2 with fronts), FCT2, max Courant {wl['courant']}, delt1 {wl['delt1']} s")
+    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": 1, "steps": steps,
+            "warmup": 1, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-mixed" if head_form != "fp64" else "f64",
+            "data": "synthetic (seeded generator, HYCOM units/layout)", "impl": f"ensemble-{args.workload}",
+            "config": {"workload": desc, "form": head_form, "updates_per_step": ups,
+                       "l2": "inputs larger than L2 (state resident in HBM)"},
+            "roofline": {"bound": "hbm", "achieved": head["achieved_GBs"], "peak": peak, "unit": "GB/s",
+                         "frac": head["frac_of_measured_hbm"], "traffic": None, "peak_kind": peak_kind},
+            "clocks": head["clocks"], "wall_seconds": time.perf_counter() - t_start, "forms": res}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def config_of(args, wl):
     return {"workload": f"{args.workload}: {'periodic-x' if wl['periodic'] else 'closed'} basin "
                         f"{wl['nx']}x{wl['ny']}x{wl['kdm']}, T+S, {SCHEME_NAMES[args.advtyp]} "
@@ -319,8 +515,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--arm", default="tsadvc", choices=["tsadvc", "ens-fp64", "ens-mixed", "ens-mixed-fp32prep"],
                     help="tsadvc: the reference-layout C ABI (headline); ens-*: the ensemble form only")
-    ap.add_argument("--forms", action="store_true",
-                    help="also time the ensemble FP64 and FP32-mixed forms on the same basin")
+    ap.add_argument("--ens-forms", default="fp64,mixed-fp32prep,mixed",
+                    help="c2/c3: ensemble forms to run, fp64 first")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the ensemble FP64 / FP32-mixed forms on the same basin")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = dict(WORKLOADS[args.workload])
@@ -332,6 +530,11 @@ def main():
     import numpy as np
     import torch
 
+    if args.workload in ("c2", "c3"):
+        import build as hbuild
+
+        hbuild.build()
+        return run_ensemble_workload(args, wl, torch.device("cuda:0"))
     ws, rank, local = dist_setup()
     dist = None
     if ws > 1:
@@ -419,7 +622,7 @@ def main():
     clocks = clk.summary()
 
     forms = None
-    if args.forms:
+    if not args.no_forms:
         forms = run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream, precs=("fp64", "mixed", "mixed-fp32prep"))
 
     # end-to-end through the C ABI with host buffers (pinned), copies in the timed region

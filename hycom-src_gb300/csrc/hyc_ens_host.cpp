@@ -500,7 +500,8 @@ int hyc_ens_set_stream(hyc_ens *e, void *stream) {
   return HYC_OK;
 }
 
-static int move(hyc_ens *e, int32_t basin, int32_t what, void *host, int32_t where, bool put) {
+static int move(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns_req, void *host, int32_t where,
+                bool put) {
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   if (basin < 0 || basin >= (int)e->b.size() || what < HYC_E_OLD || what > HYC_E_DP || !host ||
       (where != HYC_HOST && where != HYC_DEVICE) || (!put && what > HYC_E_CUR && what != HYC_E_DP))
@@ -517,6 +518,15 @@ static int move(hyc_ens *e, int32_t basin, int32_t what, void *host, int32_t whe
     case HYC_E_VFLX: dst = b.vflx; ns = b.kdm; break;
     default: dst = b.dp; ns = b.kdm; dfp32 = 0; break;
   }
+  // a contiguous run of slices [s0, s0+ns_req); ns_req < 0 means all of them
+  if (ns_req < 0) {
+    if (s0 != 0) return efail(e, HYC_ERR_ARG, "hyc_ens_put/get: s0 without a slice count");
+    ns_req = ns;
+  }
+  if (s0 < 0 || ns_req < 1 || (long long)s0 + ns_req > ns)
+    return efail(e, HYC_ERR_ARG, "hyc_ens_put/get: slices [%d, %d) outside [0, %d)", s0, s0 + ns_req, ns);
+  ns = ns_req;
+  dst = (char *)dst + (size_t)s0 * b.slice * (dfp32 ? 4 : 8);
   const long long rsl = (long long)b.ld1r * b.ld2;
   const size_t bytes = (size_t)rsl * ns * 8;
   double *stage = nullptr;
@@ -546,11 +556,21 @@ static int move(hyc_ens *e, int32_t basin, int32_t what, void *host, int32_t whe
 }
 
 int hyc_ens_put(hyc_ens *e, int32_t basin, int32_t what, const double *src, int32_t where) {
-  return move(e, basin, what, (void *)src, where, true);
+  return move(e, basin, what, 0, -1, (void *)src, where, true);
 }
 
 int hyc_ens_get(hyc_ens *e, int32_t basin, int32_t what, double *dst, int32_t where) {
-  return move(e, basin, what, dst, where, false);
+  return move(e, basin, what, 0, -1, dst, where, false);
+}
+
+int hyc_ens_put_slices(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns, const double *src,
+                       int32_t where) {
+  return move(e, basin, what, s0, ns, (void *)src, where, true);
+}
+
+int hyc_ens_get_slices(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns, double *dst,
+                       int32_t where) {
+  return move(e, basin, what, s0, ns, dst, where, false);
 }
 
 int hyc_ens_set_tile(hyc_ens *e, int32_t tx, int32_t ty) {

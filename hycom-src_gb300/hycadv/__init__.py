@@ -41,7 +41,8 @@ FIELDS = {"temp": 0, "saln": 1, "th3d": 2, "tracer": 3, "uflx": 4, "vflx": 5, "d
 EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "hyc_set_stream", "hyc_bind_field",
            "hyc_sync_field", "hyc_synchronize", "hyc_tsadvc", "hyc_advem", "hyc_xctilr", "hyc_mass_sum",
            "hyc_version", "hyc_enable_timers", "hyc_get_stats", "hyc_advem_noalloc", "hyc_ens_create",
-           "hyc_ens_destroy", "hyc_ens_set_stream", "hyc_ens_put", "hyc_ens_get", "hyc_ens_set_tile",
+           "hyc_ens_destroy", "hyc_ens_set_stream", "hyc_ens_put", "hyc_ens_get",
+           "hyc_ens_put_slices", "hyc_ens_get_slices", "hyc_ens_set_tile",
            "hyc_ens_tune", "hyc_ens_step", "hyc_ens_content", "hyc_ens_stats", "hyc_ens_enable_timers",
            "hyc_ens_last_error", "hyc_ens_set_option")
 ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
@@ -106,6 +107,8 @@ def lib() -> C.CDLL:
         L.hyc_ens_set_stream.argtypes = [vp, vp]
         L.hyc_ens_put.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int32]
         L.hyc_ens_get.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int32]
+        L.hyc_ens_put_slices.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
+        L.hyc_ens_get_slices.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
         L.hyc_ens_set_tile.argtypes = [vp, C.c_int32, C.c_int32]
         L.hyc_ens_tune.argtypes = [vp, C.c_int32, C.c_double, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_double)]
@@ -164,6 +167,43 @@ def _ptr(a):
     raise TypeError(type(a))
 
 
+class _StreamFollower:
+    """Stream ordering between torch and the library.
+
+    The library queues its work on one CUDA stream per context (its own
+    non-blocking stream unless set_stream chose another).  Device tensors
+    handed over from torch were written on torch's current stream, so by
+    default the wrappers put the library on torch's current stream of the
+    device before each call that queues work: reads of torch-produced
+    tensors and torch's later reads of the library's results are then
+    ordered by the stream itself.  After an explicit set_stream the caller
+    owns the ordering, and the wrappers wait for torch's current stream
+    before a call that passes it device tensors."""
+
+    def _init_stream(self, device: int):
+        self.device = device
+        self._explicit = None  # stream pointer chosen by set_stream
+        self._cur = None       # stream pointer the library uses now (None: its own)
+
+    def _set_stream_ptr(self, ptr: int):
+        raise NotImplementedError
+
+    def _order(self, tensors=()):
+        import sys
+
+        torch = sys.modules.get("torch")
+        if torch is None or not torch.cuda.is_available():
+            return
+        cur = torch.cuda.current_stream(self.device)
+        if self._explicit is None:
+            if self._cur != cur.cuda_stream:
+                self._set_stream_ptr(cur.cuda_stream)
+                self._cur = cur.cuda_stream
+        elif cur.cuda_stream != self._explicit and any(
+                isinstance(t, torch.Tensor) and t.is_cuda for t in tensors):
+            cur.synchronize()
+
+
 def bigrid(depth: np.ndarray, nbdy: int = 6):
     """bigrid.F90 for one tile: returns (depth_after, masks, nreg).
 
@@ -179,7 +219,7 @@ def bigrid(depth: np.ndarray, nbdy: int = 6):
     return d, masks, nreg.value
 
 
-class Context:
+class Context(_StreamFollower):
     """One basin on one GPU: the state tsadvc reads from mod_dimensions/mod_cb_arrays."""
 
     def __init__(self, idm, jdm, kdm, nbdy, nreg, ip, iu, iv, scp2, scp2i, device: int = 0):
@@ -193,6 +233,10 @@ class Context:
                               keep[4][1], device))
         self._h = h
         self._bound = {}
+        self._init_stream(device)
+
+    def _set_stream_ptr(self, ptr: int):
+        _check(lib().hyc_set_stream(self._h, C.c_void_p(ptr)), self._h)
 
     @classmethod
     def from_masks(cls, masks: dict, scp2, scp2i, kdm: int, nreg: int, nbdy: int = 6, device: int = 0):
@@ -223,19 +267,23 @@ class Context:
         array gets a resident device mirror (move data with :meth:`sync`)."""
         p, where = _ptr(array)
         n = array.size if isinstance(array, np.ndarray) else array.numel()
+        self._order((array,))
         _check(lib().hyc_bind_field(self._h, FIELDS[name], p, n, where), self._h)
         self._bound[name] = array
 
     def sync(self, name: str, to_device: bool):
+        self._order(self._bound.values())
         _check(lib().hyc_sync_field(self._h, FIELDS[name], int(bool(to_device))), self._h)
 
     def synchronize(self):
         _check(lib().hyc_synchronize(self._h), self._h)
 
     def set_stream(self, stream):
-        """Queue later work on a torch.cuda.Stream (or a raw cudaStream_t int)."""
+        """Queue later work on a torch.cuda.Stream (or a raw cudaStream_t int).
+        The caller then orders it against torch's other streams."""
         ptr = stream if isinstance(stream, int) else stream.cuda_stream
-        _check(lib().hyc_set_stream(self._h, C.c_void_p(ptr)), self._h)
+        self._set_stream_ptr(ptr)
+        self._explicit = self._cur = ptr
 
     # -- the reference's routines --------------------------------------------
     def tsadvc(self, m: int, n: int, *, delt1: float, advtyp: int = 2, advflg: int = 0, btrmas: bool = False,
@@ -248,6 +296,7 @@ class Context:
         p = TsadvcParams(advtyp=advtyp, advflg=advflg, btrmas=int(btrmas), ntracr=ntracr, nhybrd=nh,
                          isopyc=int(isopyc), hybrid=int(nh > 0), mxlmy=int(mxlmy), nstep=nstep, diagno=int(diagno),
                          delt1=float(delt1), trcflg=tf.ctypes.data_as(C.POINTER(C.c_int32)))
+        self._order(self._bound.values())
         if range_diag and (nstep % 3 == 0 or diagno):  # mod_tsadvc.F90:2065
             xmin = np.zeros(self.kdm)
             xmax = np.zeros(self.kdm)
@@ -266,12 +315,14 @@ class Context:
             raise HycError(-1, "advem arrays must all be host or all device")
         where = wheres.pop()
         p = [pp for pp, _ in ptrs]
+        self._order(arrs)
         _check(lib().hyc_advem(self._h, int(advtyp), p[0], p[1], p[2], p[3], p[4], p[5], float(posdef), p[6], p[7],
                                float(dt2), int(bool(btrmas)), where), self._h)
 
     def xctilr(self, a, mh: int, nh: int):
         p, where = _ptr(a)
         nlev = int(np.prod(a.shape[:-2])) if len(a.shape) > 2 else 1
+        self._order((a,))
         _check(lib().hyc_xctilr(self._h, p, nlev, mh, nh, where), self._h)
 
     def enable_timers(self, on: bool = True):
@@ -289,11 +340,12 @@ class Context:
     def mass_sum(self, fld, fc) -> float:
         """sum over interior sea cells of fld*(fc+onemu)*scp2 (device tensors)."""
         out = C.c_double(0.0)
+        self._order((fld, fc))
         _check(lib().hyc_mass_sum(self._h, _ptr(fld)[0], _ptr(fc)[0], C.byref(out)), self._h)
         return out.value
 
 
-class Ensemble:
+class Ensemble(_StreamFollower):
     """Many independent basins advected together (hyc_ens_* in the C ABI).
 
     basins: list of dicts with idm, jdm, kdm, nbdy, nreg, ntr and the
@@ -316,6 +368,10 @@ class Ensemble:
         self._h = h
         self.basins = [dict(b) for b in basins]
         self.precision = precision
+        self._init_stream(device)
+
+    def _set_stream_ptr(self, ptr: int):
+        self._chk(lib().hyc_ens_set_stream(self._h, C.c_void_p(ptr)))
 
     def _chk(self, rc):
         if rc != HYC_OK:
@@ -333,16 +389,30 @@ class Ensemble:
             pass
 
     def set_stream(self, stream):
+        """Queue later work on a torch.cuda.Stream (or a raw cudaStream_t int);
+        graphs are replayed there.  The caller then orders it against
+        torch's other streams."""
         ptr = stream if isinstance(stream, int) else stream.cuda_stream
-        self._chk(lib().hyc_ens_set_stream(self._h, C.c_void_p(ptr)))
+        self._set_stream_ptr(ptr)
+        self._explicit = self._cur = ptr
 
-    def put(self, b: int, what: str, a):
+    def put(self, b: int, what: str, a, s0: int = None, ns: int = None):
+        """Whole field, or (s0, ns) the slices [s0, s0+ns) only (tracer q of
+        old/cur is s0 = q*kdm, ns = kdm)."""
         p, where = _ptr(a)
-        self._chk(lib().hyc_ens_put(self._h, b, ENS_WHAT[what], p, where))
+        self._order((a,))
+        if s0 is None:
+            self._chk(lib().hyc_ens_put(self._h, b, ENS_WHAT[what], p, where))
+        else:
+            self._chk(lib().hyc_ens_put_slices(self._h, b, ENS_WHAT[what], s0, ns, p, where))
 
-    def get(self, b: int, what: str, out):
+    def get(self, b: int, what: str, out, s0: int = None, ns: int = None):
         p, where = _ptr(out)
-        self._chk(lib().hyc_ens_get(self._h, b, ENS_WHAT[what], p, where))
+        self._order((out,))
+        if s0 is None:
+            self._chk(lib().hyc_ens_get(self._h, b, ENS_WHAT[what], p, where))
+        else:
+            self._chk(lib().hyc_ens_get_slices(self._h, b, ENS_WHAT[what], s0, ns, p, where))
         return out
 
     def set_tile(self, tx: int, ty: int):
@@ -350,14 +420,17 @@ class Ensemble:
 
     def tune(self, advtyp: int, delt1: float):
         tx, ty, ms = C.c_int32(), C.c_int32(), C.c_double()
+        self._order()
         self._chk(lib().hyc_ens_tune(self._h, advtyp, float(delt1), C.byref(tx), C.byref(ty), C.byref(ms)))
         return tx.value, ty.value, ms.value
 
     def step(self, advtyp: int, delt1: float, nsteps: int = 1, graph: bool = False):
+        self._order()
         self._chk(lib().hyc_ens_step(self._h, advtyp, float(delt1), nsteps, int(bool(graph))))
 
     def content(self, b: int, q: int, what: str, delt1: float) -> float:
         out = C.c_double()
+        self._order()
         self._chk(lib().hyc_ens_content(self._h, b, q, ENS_WHAT[what], float(delt1), C.byref(out)))
         return out.value
 

@@ -350,41 +350,59 @@ class Case:
     scp2i: object
 
 
-def build_case(b: Basin, masks: dict, kdm: int, ntracr: int, seed: int, courant: float, delt1: float,
-               device="cpu", passive: bool = True) -> Case:
-    """Generate every field of a tsadvc call for basin ``b`` (masks from bigrid)."""
+def flow_fields(b: Basin, masks: dict, kdm: int, seed: int, courant: float, delt1: float, device="cpu"):
+    """Layer thickness at both levels and the mass fluxes: (dp, uflx, vflx),
+    dp (2, kdm, ld2, ld1) with index 1 the generated thickness and index 0
+    its perturbed copy; uflx/vflx (kdm, ld2, ld1)."""
     import torch
 
-    ld1, ld2 = b.ld1, b.ld2
     f64 = dict(dtype=torch.float64, device=device)
-    temp = torch.empty((2, kdm, ld2, ld1), **f64)
-    saln = torch.empty((2, kdm, ld2, ld1), **f64)
-    th3d = torch.empty((2, kdm, ld2, ld1), **f64)
-    dp = torch.empty((2, kdm, ld2, ld1), **f64)
-    uflx = torch.empty((kdm, ld2, ld1), **f64)
-    vflx = torch.empty((kdm, ld2, ld1), **f64)
-    tracer = torch.empty((max(ntracr, 0), 2, kdm, ld2, ld1), **f64)
+    dp = torch.empty((2, kdm, b.ld2, b.ld1), **f64)
+    uflx = torch.empty((kdm, b.ld2, b.ld1), **f64)
+    vflx = torch.empty((kdm, b.ld2, b.ld1), **f64)
     layers = [make_layer(b, k, kdm, seed, courant, delt1, device) for k in range(1, kdm + 1)]
     cap_columns([lf.dp for lf in layers])
     for k, lf in enumerate(layers):
         dp[1, k] = lf.dp
         dp[0, k] = perturb_old(lf.dp, seed, k + 1, 99, 0.02, b, device)
         uflx[k], vflx[k] = mass_fluxes(b, masks, lf.dp, lf.u, lf.v)
-        t = make_tracer_layer(b, "temp", k + 1, kdm, seed, device=device)
-        s = make_tracer_layer(b, "saln", k + 1, kdm, seed, device=device)
-        temp[0, k] = t
-        temp[1, k] = perturb_old(t, seed, k + 1, 1, 0.01, b, device)
-        saln[0, k] = s
-        saln[1, k] = perturb_old(s, seed, k + 1, 2, 0.002, b, device)
-        th3d[0, k] = 20.0 + 0.1 * (k + 1) + 0.01 * t
+    return dp, uflx, vflx
+
+
+TRACER_TAGS = {"temp": (1, 0.01), "saln": (2, 0.002)}
+
+
+def tracer_levels(b: Basin, kind: str, kdm: int, seed: int, q: int = 0, device="cpu", like=None):
+    """Both time levels of one tracer, (2, kdm, ld2, ld1): index 0 at time t,
+    index 1 at t-1.  kind 'temp', 'saln' or 'passive' (passive tracer q);
+    like='temp' gives a passive tracer that copies temperature."""
+    import torch
+
+    out = torch.empty((2, kdm, b.ld2, b.ld1), dtype=torch.float64, device=device)
+    tag, rel = TRACER_TAGS.get(kind, (10 + q, 0.01))
+    for k in range(kdm):
+        src = like or kind
+        c = make_tracer_layer(b, src, k + 1, kdm, seed, tracer_index=q, device=device)
+        out[0, k] = c
+        out[1, k] = perturb_old(c, seed, k + 1, tag, rel, b, device)
+    return out
+
+
+def build_case(b: Basin, masks: dict, kdm: int, ntracr: int, seed: int, courant: float, delt1: float,
+               device="cpu", passive: bool = True) -> Case:
+    """Generate every field of a tsadvc call for basin ``b`` (masks from bigrid)."""
+    import torch
+
+    dp, uflx, vflx = flow_fields(b, masks, kdm, seed, courant, delt1, device)
+    temp = tracer_levels(b, "temp", kdm, seed, device=device)
+    saln = tracer_levels(b, "saln", kdm, seed, device=device)
+    th3d = torch.empty_like(temp)
+    for k in range(kdm):
+        th3d[0, k] = 20.0 + 0.1 * (k + 1) + 0.01 * temp[0, k]
         th3d[1, k] = perturb_old(th3d[0, k], seed, k + 1, 3, 0.001, b, device)
-        for q in range(ntracr):
-            if passive:
-                c = make_tracer_layer(b, "passive", k + 1, kdm, seed, tracer_index=q, device=device)
-            else:
-                c = t.clone()
-            tracer[q, 0, k] = c
-            tracer[q, 1, k] = perturb_old(c, seed, k + 1, 10 + q, 0.01, b, device)
+    tracer = torch.empty((max(ntracr, 0), 2, kdm, b.ld2, b.ld1), dtype=torch.float64, device=device)
+    for q in range(ntracr):
+        tracer[q] = tracer_levels(b, "passive", kdm, seed, q=q, device=device, like=None if passive else "temp")
     scp2, scp2i = b.metrics()
     return Case(basin=b, kdm=kdm, ntracr=ntracr, delt1=delt1, temp=temp, saln=saln, th3d=th3d,
                 tracer=tracer, uflx=uflx, vflx=vflx, dp=dp,

@@ -110,7 +110,14 @@ int hyc_adv_finalize(hyc_ctx *ctx);
 /* Copy the last error message of ctx (or of the library when ctx is NULL). */
 int hyc_last_error(const hyc_ctx *ctx, char *buf, size_t n);
 
-/* Use this CUDA stream (a cudaStream_t passed as void*) for later calls. */
+/*
+ * Use this CUDA stream (a cudaStream_t passed as void*; NULL = the legacy
+ * default stream) for later calls.  Until then a context queues its work
+ * on a non-blocking stream of its own.  Device memory the caller passes in
+ * is read and written in order on that stream: a caller that fills or
+ * reads such memory on another stream orders the two itself (an event, a
+ * synchronize, or by setting its own stream here).
+ */
 int hyc_set_stream(hyc_ctx *ctx, void *stream);
 
 /*
@@ -256,10 +263,17 @@ typedef struct hyc_basin_spec {
 int hyc_ens_create(hyc_ens **ens, int32_t nbasin, const hyc_basin_spec *specs, int32_t precision,
                    int32_t device);
 int hyc_ens_destroy(hyc_ens *ens);
+/* As hyc_set_stream, for an ensemble (graphs are replayed on this stream). */
 int hyc_ens_set_stream(hyc_ens *ens, void *stream);
 /* src/dst: ld1*ld2*(slices) doubles in the reference layout (pitch idm+2*nbdy) */
 int hyc_ens_put(hyc_ens *ens, int32_t basin, int32_t what, const double *src, int32_t where);
 int hyc_ens_get(hyc_ens *ens, int32_t basin, int32_t what, double *dst, int32_t where);
+/* The same for the slices [s0, s0+ns) only (tracer-major for HYC_E_OLD/CUR:
+ * slice q*kdm+k), so a caller can move one tracer at a time. */
+int hyc_ens_put_slices(hyc_ens *ens, int32_t basin, int32_t what, int32_t s0, int32_t ns, const double *src,
+                       int32_t where);
+int hyc_ens_get_slices(hyc_ens *ens, int32_t basin, int32_t what, int32_t s0, int32_t ns, double *dst,
+                       int32_t where);
 /* Tile shape of the step kernel (tx x ty cells); hyc_ens_tune picks one. */
 int hyc_ens_set_tile(hyc_ens *ens, int32_t tx, int32_t ty);
 /*
