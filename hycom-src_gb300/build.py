@@ -31,6 +31,7 @@ UNITS = {
     "hyc_mixed.cu": ["-lineinfo"],
     "hyc_mixed_tma.cu": ["-lineinfo"],
     "hyc_mixed_col.cu": ["-lineinfo"],
+    "hyc_mixed_col2.cu": ["-lineinfo"],
     "hyc_ens_host.cpp": [],
 }
 

@@ -34,6 +34,10 @@ struct MixBasin {
   const float2 *dsqs;
   int seg;
   int pad2;
+  // two-column strip kernel: TMA maps (box 64 x 4 rows) of the old and
+  // centre levels, uflx, vflx, dp, the metric factors (as 2*ld1 floats per
+  // row), the u32 masks and dt2*scp2i (FP64)
+  const CUtensorMap *c2_old, *c2_cur, *c2_u, *c2_v, *c2_dp, *c2_dq, *c2_mk, *c2_si;
 };
 
 bool mix_shape_ok(TileShape t);
@@ -47,6 +51,12 @@ cudaError_t launch_mix_fct2_tma(TileShape t, const MixBasin *basins, const int4 
 constexpr int kColStrip = 26;
 cudaError_t launch_mix_fct2_col(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm, int nq,
                                 bool prep64, int seg, cudaStream_t s);
+// two columns per lane, 64-column strips (56 updated) streamed by TMA
+constexpr int kCol2Strip = 56;
+constexpr int kCol2Box = 64, kCol2Rows = 4;
+cudaError_t launch_mix_fct2_col2(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm, int nq,
+                                 bool prep64, int *err, cudaStream_t s);
+cudaError_t launch_dtsi(const double *scp2i, double dt2, long long n, double *out, cudaStream_t s);
 cudaError_t launch_dsqs(const double *scp2, const double *scp2i, double dt2, long long n, float2 *out,
                         cudaStream_t s);
 

@@ -31,6 +31,8 @@ struct EBasin {
   double *dp = nullptr;
   void *lev[3] = {nullptr, nullptr, nullptr};  // tracer state, physical levels
   float2 *dsqs = nullptr;                       // column kernel metric factors (mixed form)
+  uint32_t *msk32 = nullptr;                    // masks widened to u32 (TMA rows of the strip kernel)
+  double *dtsi = nullptr;                       // dt2*scp2i (strip kernel, FP64 thickness prep)
   long long work = 0;                           // cells*layers*tracers, for queue ordering
 };
 
@@ -48,7 +50,9 @@ struct hyc_ens {
   bool prep64 = true;  // FP32-mixed: thickness prep in FP64 (else compensated FP32)
   bool use_tma = false;  // FP32-mixed: TMA-staged kernel (needs nbdy = 6 everywhere)
   int maxntr = 1;        // largest tracer count (column kernel processes tracers in pairs)
+  int strip_nq = 2;      // two-column strip kernel: tracers per pass (1 or 2)
   CUtensorMap *d_tmaps = nullptr;  // [nbasin][6]: level 0,1,2, uflx, vflx, dp
+  CUtensorMap *d_cmaps = nullptr;  // [nbasin][9]: strip kernel maps (levels 0-2, u, v, dp, dq, mk, si)
   int tm_tx = 0, tm_ty = 0;        // shape the maps were encoded for
   int *d_err = nullptr;            // device error flag (bounded waits that gave up)
   // device tables, one per rotation
@@ -109,6 +113,9 @@ size_t esz(const hyc_ens *e) { return e->prec == HYC_PREC_MIXED ? 4 : 8; }
 
 // tile shapes with tx == 26 select the column-strip kernel (ty = rows per segment)
 bool is_col(hyc::TileShape t) { return t.tx == hyc::kColStrip; }
+// tx == 56 selects the two-column strip kernel (ty = rows per segment)
+bool is_col2(hyc::TileShape t) { return t.tx == hyc::kCol2Strip; }
+bool is_strip(hyc::TileShape t) { return is_col(t) || is_col2(t); }
 
 void free_all(hyc_ens *e) {
   for (auto &b : e->b) {
@@ -119,6 +126,8 @@ void free_all(hyc_ens *e) {
     cudaFree(b.vflx);
     cudaFree(b.dp);
     cudaFree(b.dsqs);
+    cudaFree(b.msk32);
+    cudaFree(b.dtsi);
     for (auto &l : b.lev) cudaFree(l);
   }
   for (int r = 0; r < 3; r++) {
@@ -129,6 +138,7 @@ void free_all(hyc_ens *e) {
   cudaFree(e->d_head);
   cudaFree(e->d_partial);
   cudaFree(e->d_tmaps);
+  cudaFree(e->d_cmaps);
   cudaFree(e->d_err);
   if (e->gexec) cudaGraphExecDestroy(e->gexec);
   for (auto &p : e->pending) {
@@ -156,17 +166,54 @@ EncodeTiledFn encode_fn() {
 }
 
 // 3-D tiled map over nz slices of (ld1 x ld2) elements, box (bx, by, 1)
-bool encode3(CUtensorMap *m, void *base, bool fp64, int ld1, int ld2, long long nz, int bx, int by) {
+bool encode3t(CUtensorMap *m, void *base, CUtensorMapDataType dt, size_t es, int ld1, int ld2, long long nz, int bx,
+              int by) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
-  const size_t es = fp64 ? 8 : 4;
   cuuint64_t dims[3] = {(cuuint64_t)ld1, (cuuint64_t)ld2, (cuuint64_t)nz};
   cuuint64_t strides[2] = {(cuuint64_t)ld1 * es, (cuuint64_t)ld1 * ld2 * es};
   cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
   cuuint32_t estr[3] = {1, 1, 1};
-  return fn(m, fp64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides,
-            box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  return fn(m, dt, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+bool encode3(CUtensorMap *m, void *base, bool fp64, int ld1, int ld2, long long nz, int bx, int by) {
+  return encode3t(m, base, fp64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, fp64 ? 8 : 4,
+                  ld1, ld2, nz, bx, by);
+}
+// 2-D tiled map over one (w x ld2) slice, box (bx, by)
+bool encode2t(CUtensorMap *m, void *base, CUtensorMapDataType dt, size_t es, int w, int ld2, int bx, int by) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)w, (cuuint64_t)ld2};
+  cuuint64_t strides[1] = {(cuuint64_t)w * es};
+  cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(m, dt, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// maps of the two-column strip kernel; they depend only on the allocations
+int encode_strip_maps(hyc_ens *e) {
+  const int bx = hyc::kCol2Box, by = hyc::kCol2Rows;
+  const CUtensorMapDataType F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32, F64 = CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                            U32 = CU_TENSOR_MAP_DATA_TYPE_UINT32;
+  std::vector<CUtensorMap> h(e->b.size() * 9);
+  for (size_t i = 0; i < e->b.size(); i++) {
+    EBasin &b = e->b[i];
+    CUtensorMap *m = &h[i * 9];
+    bool ok = true;
+    for (int l = 0; l < 3; l++) ok &= encode3t(m + l, b.lev[l], F32, 4, b.ld1, b.ld2, (long long)b.ntr * b.kdm, bx, by);
+    ok &= encode3t(m + 3, b.uflx, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
+    ok &= encode3t(m + 4, b.vflx, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
+    ok &= encode3t(m + 5, b.dp, F64, 8, b.ld1, b.ld2, b.kdm, bx, by);
+    ok &= encode2t(m + 6, b.dsqs, F32, 4, 2 * b.ld1, b.ld2, 2 * bx, by);
+    ok &= encode2t(m + 7, b.msk32, U32, 4, b.ld1, b.ld2, bx, by);
+    ok &= encode2t(m + 8, b.dtsi, F64, 8, b.ld1, b.ld2, bx, by);
+    if (!ok) return efail(e, HYC_ERR_CUDA, "cuTensorMapEncodeTiled failed for the strip maps (basin %zu)", i);
+  }
+  ECK(cudaMemcpy(e->d_cmaps, h.data(), h.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "strip maps copy");
+  return HYC_OK;
 }
 
 int encode_maps(hyc_ens *e) {
@@ -199,6 +246,7 @@ int build_tables(hyc_ens *e, double dt2) {
     for (auto &b : e->b) {
       if (!b.dsqs) ECK(cudaMalloc(&b.dsqs, b.slice * sizeof(float2)), "dsqs");
       ECK(hyc::launch_dsqs(b.scp2, b.scp2i, dt2, b.slice, b.dsqs, e->stream), "dsqs");
+      if (b.dtsi) ECK(hyc::launch_dtsi(b.scp2i, dt2, b.slice, b.dtsi, e->stream), "dtsi");
     }
   for (int r = 0; r < 3; r++) {
     const int lo = r, lc = (r + 1) % 3, ln = (r + 2) % 3;
@@ -231,6 +279,17 @@ int build_tables(hyc_ens *e, double dt2) {
         m.fnew = (float *)b.lev[ln];
         m.seg = e->shape.ty;
         m.dsqs = b.dsqs;
+        if (e->d_cmaps) {
+          const CUtensorMap *c = e->d_cmaps + i * 9;
+          m.c2_old = c + lo;
+          m.c2_cur = c + lc;
+          m.c2_u = c + 3;
+          m.c2_v = c + 4;
+          m.c2_dp = c + 5;
+          m.c2_dq = c + 6;
+          m.c2_mk = c + 7;
+          m.c2_si = c + 8;
+        }
         if (e->d_tmaps) {
           m.tm_old = e->d_tmaps + i * 6 + lo;
           m.tm_cur = e->d_tmaps + i * 6 + lc;
@@ -294,6 +353,12 @@ int build_items(hyc_ens *e) {
   for (int i = 0; i < (int)e->b.size(); i++) {
     const EBasin &b = e->b[i];
     const int ntx = (b.idm + e->shape.tx - 1) / e->shape.tx, nty = (b.jdm + e->shape.ty - 1) / e->shape.ty;
+    if (is_col2(e->shape)) {  // (basin, 56-column strip, segment), all layers and tracers
+      const int nstrip = (b.nbdy + b.idm - 4 + hyc::kCol2Strip - 1) / hyc::kCol2Strip;
+      for (int sg = 0; sg < nty; sg++)
+        for (int st = 0; st < nstrip; st++) w.push_back({(long long)b.kdm * b.ntr, make_int4(i, st, sg, 0)});
+      continue;
+    }
     if (is_col(e->shape)) {  // (basin, strip, segment), all layers and tracers
       for (int sg = 0; sg < nty; sg++)
         for (int st = 0; st < ntx; st++) w.push_back({(long long)b.kdm * b.ntr, make_int4(i, st, sg, 0)});
@@ -347,7 +412,10 @@ int prime(hyc_ens *e) {
 int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
   ECK(cudaMemsetAsync(e->d_head + h, 0, sizeof(int), st), "queue reset");
   cudaError_t c;
-  if (e->prec == HYC_PREC_MIXED && is_col(e->shape))
+  if (e->prec == HYC_PREC_MIXED && is_col2(e->shape))
+    c = hyc::launch_mix_fct2_col2(e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm,
+                                  std::min(e->strip_nq, e->maxntr), e->prep64, e->d_err, st);
+  else if (e->prec == HYC_PREC_MIXED && is_col(e->shape))
     c = hyc::launch_mix_fct2_col(e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->maxntr, e->prep64,
                                  e->shape.ty, st);
   else if (e->prec == HYC_PREC_MIXED && e->use_tma)
@@ -363,6 +431,7 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
 }
 
 bool shape_ok(const hyc_ens *e, hyc::TileShape t) {
+  if (e->prec == HYC_PREC_MIXED && is_col2(t)) return e->d_cmaps && (t.ty == 32 || t.ty == 64 || t.ty == 128);
   if (e->prec == HYC_PREC_MIXED && is_col(t)) return t.ty == 32 || t.ty == 64 || t.ty == 128;
   if (e->prec == HYC_PREC_MIXED) return e->use_tma ? hyc::mix_tma_shape_ok(t) : hyc::mix_shape_ok(t);
   return (t.tx == 32 && t.ty == 16) || (t.tx == 16 && t.ty == 16);
@@ -438,6 +507,10 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
               cudaMalloc(&b.vflx, b.slice * b.kdm * es) == cudaSuccess &&
               cudaMalloc(&b.dp, b.slice * b.kdm * 8) == cudaSuccess;
     for (int l = 0; l < 3 && ok; l++) ok = cudaMalloc(&b.lev[l], b.slice * b.kdm * b.ntr * es) == cudaSuccess;
+    if (ok && precision == HYC_PREC_MIXED)
+      ok = cudaMalloc(&b.dsqs, b.slice * sizeof(float2)) == cudaSuccess &&
+           cudaMalloc(&b.msk32, b.slice * sizeof(uint32_t)) == cudaSuccess &&
+           cudaMalloc(&b.dtsi, b.slice * sizeof(double)) == cudaSuccess;
     e->b.push_back(b);
     if (!ok) return bail(efail(nullptr, HYC_ERR_NOMEM, "basin %d: device allocation failed", i));
     EBasin &bb = e->b.back();
@@ -448,6 +521,10 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
               cudaMemset(bb.vflx, 0, bb.slice * bb.kdm * es) == cudaSuccess &&
               cudaMemset(bb.dp, 0, bb.slice * bb.kdm * 8) == cudaSuccess;
     for (int l = 0; l < 3 && cp; l++) cp = cudaMemset(bb.lev[l], 0, bb.slice * bb.kdm * bb.ntr * es) == cudaSuccess;
+    if (cp && bb.msk32) {
+      std::vector<uint32_t> m32(m.begin(), m.end());
+      cp = cudaMemcpy(bb.msk32, m32.data(), bb.slice * sizeof(uint32_t), cudaMemcpyHostToDevice) == cudaSuccess;
+    }
     if (!cp) return bail(efail(nullptr, HYC_ERR_CUDA, "basin %d: upload failed", i));
   }
   for (int r = 0; r < 3; r++) {
@@ -466,6 +543,14 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
     if (all6 && encode_fn() && cudaMalloc(&e->d_tmaps, nbasin * 6 * sizeof(CUtensorMap)) == cudaSuccess)
       e->use_tma = true;
     e->shape = hyc::TileShape{hyc::kColStrip, 64};  // column-strip kernel
+    if (encode_fn() && cudaMalloc(&e->d_cmaps, nbasin * 9 * sizeof(CUtensorMap)) == cudaSuccess) {
+      if (encode_strip_maps(e) == HYC_OK) {
+        e->shape = hyc::TileShape{hyc::kCol2Strip, 64};  // two-column strip kernel
+      } else {
+        cudaFree(e->d_cmaps);
+        e->d_cmaps = nullptr;
+      }
+    }
   }
   *out = e;
   return HYC_OK;
@@ -599,12 +684,22 @@ int hyc_ens_set_option(hyc_ens *e, int32_t option, int32_t value) {
     e->prep64 = value != 0;
     return HYC_OK;
   }
+  if (option == HYC_OPT_STRIP_TRACERS) {
+    if (e->prec != HYC_PREC_MIXED || (value != 1 && value != 2))
+      return efail(e, HYC_ERR_ARG, "HYC_OPT_STRIP_TRACERS: 1 or 2, mixed form");
+    if (e->strip_nq != value && e->gexec) {
+      cudaGraphExecDestroy(e->gexec);
+      e->gexec = nullptr;
+    }
+    e->strip_nq = value;
+    return HYC_OK;
+  }
   if (option == HYC_OPT_TMA) {
     if (e->prec != HYC_PREC_MIXED || (value && !e->d_tmaps))
       return efail(e, HYC_ERR_ARG, "HYC_OPT_TMA needs the mixed form with nbdy = 6");
     if (e->use_tma != (value != 0)) {
       e->use_tma = value != 0;
-      if (!is_col(e->shape)) e->shape = hyc::TileShape{32, 16};
+      if (!is_strip(e->shape)) e->shape = hyc::TileShape{32, 16};
       e->tbl_dt2 = -1.0;
       e->items_tx = 0;
       if (e->gexec) {
@@ -615,6 +710,16 @@ int hyc_ens_set_option(hyc_ens *e, int32_t option, int32_t value) {
     return HYC_OK;
   }
   return efail(e, HYC_ERR_ARG, "unknown option %d", option);
+}
+
+int hyc_ens_get_option(hyc_ens *e, int32_t option, int32_t *value) {
+  if (!e || !value) return efail(e, HYC_ERR_ARG, "null argument");
+  switch (option) {
+    case HYC_OPT_PREP64: *value = e->prep64; return HYC_OK;
+    case HYC_OPT_TMA: *value = e->use_tma; return HYC_OK;
+    case HYC_OPT_STRIP_TRACERS: *value = e->strip_nq; return HYC_OK;
+    default: return efail(e, HYC_ERR_ARG, "unknown option %d", option);
+  }
 }
 
 int hyc_ens_enable_timers(hyc_ens *e, int32_t on) {
@@ -652,7 +757,7 @@ int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32
     return efail(e, HYC_ERR_UNSUPPORTED, "ensemble advtyp %d not available for this precision", advtyp);
   Dev g(e->device);
   int rc;
-  if ((rc = build_items(e)) || (e->use_tma && !is_col(e->shape) && (rc = encode_maps(e))) ||
+  if ((rc = build_items(e)) || (e->use_tma && !is_strip(e->shape) && (rc = encode_maps(e))) ||
       (rc = build_tables(e, delt1)) || (rc = ensure_heads(e, nsteps)) || (rc = prime(e)))
     return rc;
   cudaEvent_t a = nullptr, z = nullptr;
@@ -717,7 +822,7 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   Dev g(e->device);
   static const hyc::TileShape cands[] = {{32, 16}, {64, 16}, {32, 32}, {64, 8}, {128, 8}, {16, 16}, {32, 8},
-                                         {26, 32}, {26, 64}, {26, 128}};
+                                         {26, 32}, {26, 64}, {26, 128}, {56, 32}, {56, 64}, {56, 128}};
   hyc::TileShape best = e->shape;
   float best_ms = 1e30f;
   const hyc::TileShape keep = e->shape;
@@ -726,11 +831,20 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
   cudaEventCreate(&z);
   int rc = prime(e);
   if (rc) return rc;
+  int best_nq = e->strip_nq;
+  const int keep_nq = e->strip_nq;
+  std::vector<std::pair<hyc::TileShape, int>> trials;
   for (const auto &c : cands) {
     if (!shape_ok(e, c)) continue;
+    if (is_col2(c) && e->maxntr > 1) trials.push_back({c, 1});
+    trials.push_back({c, 2});
+  }
+  for (const auto &tr : trials) {
+    const hyc::TileShape c = tr.first;
+    e->strip_nq = tr.second;
     e->shape = c;
     e->tbl_dt2 = -1.0;
-    if ((rc = build_items(e)) || (e->use_tma && !is_col(e->shape) && (rc = encode_maps(e))) ||
+    if ((rc = build_items(e)) || (e->use_tma && !is_strip(e->shape) && (rc = encode_maps(e))) ||
         (rc = build_tables(e, delt1)) || (rc = ensure_heads(e, 1)))
       break;
     // the step kernel writes only the spare level: the state is unchanged
@@ -750,16 +864,19 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
     if (tot / reps < best_ms) {
       best_ms = tot / reps;
       best = c;
+      best_nq = tr.second;
     }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(z);
   if (rc) {
     e->shape = keep;
+    e->strip_nq = keep_nq;
     e->tbl_dt2 = -1.0;
     return rc;
   }
   e->shape = best;
+  e->strip_nq = is_col2(best) ? best_nq : keep_nq;
   e->tbl_dt2 = -1.0;
   e->items_tx = 0;  // force the queue for the chosen shape
   if (e->gexec) {

@@ -1,0 +1,450 @@
+// hyc_mixed_col2.cu -- FP32-mixed FCT2 ensemble kernel: a warp marches a
+// 64-column strip north through the rows, two columns per lane, with the
+// rows streamed into a per-warp shared-memory ring by TMA.
+//
+// Work item: (basin, strip, segment of rows), all layers and tracers.  The
+// strip starts at padded column s = 56*w (a multiple of 4, so every TMA box
+// starts on a 16-byte boundary), lane l owns columns s+2l and s+2l+1, and
+// the 56 columns s+4 .. s+59 are updated (the scheme reaches 3 cells).
+//
+// Memory: lane 0 of each warp keeps kNS blocks of kRB rows in flight.  A
+// block holds, per row, the old and centre levels of the pass's tracers,
+// uflx, vflx (FP32), dp (FP64), the metric factors (dt2*scp2i, scp2/dt2 as
+// FP32), the cell masks (u32) and, with the FP64 thickness prep, dt2*scp2i
+// in FP64 -- one cp.async.bulk.tensor per array, one mbarrier per slot.
+// Out-of-range rows and columns arrive as zeros (TMA fill), so the kernel
+// has no bounds tests on loads.
+//
+// Compute: the stage pipeline of mod_tsadvc.F90:645-997 runs in registers
+// as in hyc_mixed_col.cu -- at row J the lane forms the low-order fluxes of
+// row J (:686-720), the low-order solution and antidiffusive fluxes of row
+// J-1 (:778-855), the Zalesak ratios and limited fluxes of row J-2
+// (:863-946) and the update of row J-3 (:962-982).  With two columns per
+// lane, one shuffle moves a value across the lane boundary for both
+// columns, and adds, multiplies and FMAs run as packed FP32x2 operations.
+// The flux divergences use two-sum compensation.  The thickness factors
+// W = (fco+onemu)/(fcn+onemu), R = 1/(fcn+onemu), QF = fcn*scp2/dt2 of
+// mod_tsadvc.F90:1905-1942 are formed once per cell and layer, in FP64
+// (PREP64: continuity divergence, thickness and the reciprocal by one
+// Newton step from an FP32 seed) or in compensated FP32.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "hyc_device.cuh"
+#include "hyc_ens.h"
+#include "hyc_tma.cuh"
+
+namespace hyc {
+
+namespace {
+
+constexpr int kW = 64;      // staged columns per warp, two per lane
+constexpr int kRB = 4;      // rows per TMA block
+constexpr int kNS = 2;      // ring slots per warp
+constexpr int kWarps = 4;   // warps per CTA
+constexpr unsigned kFull = 0xffffffffu;
+
+template <int NQ, bool PREP64>
+struct Ring {
+  static constexpr int FROW = kW * 4;  // one FP32 row
+  static constexpr int OFF_FO = 0;
+  static constexpr int OFF_FC = OFF_FO + NQ * kRB * FROW;
+  static constexpr int OFF_U = OFF_FC + NQ * kRB * FROW;
+  static constexpr int OFF_V = OFF_U + kRB * FROW;
+  static constexpr int OFF_DP = OFF_V + kRB * FROW;        // double per cell
+  static constexpr int OFF_DQ = OFF_DP + kRB * kW * 8;     // float2 per cell
+  static constexpr int OFF_MK = OFF_DQ + kRB * kW * 8;     // u32 per cell
+  static constexpr int OFF_SI = OFF_MK + kRB * kW * 4;     // double per cell (PREP64)
+  static constexpr int TX_BYTES = OFF_SI + (PREP64 ? kRB * kW * 8 : 0);
+  static constexpr int SLOT = (TX_BYTES + 127) / 128 * 128;
+  static constexpr int WARP = kNS * SLOT;
+  static constexpr size_t SMEM = (size_t)kWarps * WARP + kWarps * kNS * 8 + 128;
+};
+
+// packed FP32x2 arithmetic (sm_100 family)
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  unsigned long long r, x, y;
+  asm("mov.b64 %0, {%1,%2};" : "=l"(x) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1,%2};" : "=l"(y) : "f"(b.x), "f"(b.y));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(x), "l"(y));
+  float2 o;
+  asm("mov.b64 {%0,%1}, %2;" : "=f"(o.x), "=f"(o.y) : "l"(r));
+  return o;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+// ((a - b) + (c - d)) with the rounding errors of the two differences added
+// back (two-sum), both columns at once
+__device__ __forceinline__ float2 comp_div2(float2 a, float2 b, float2 c, float2 d) {
+  const float2 s1 = sub2(a, b), t1 = sub2(s1, a);
+  const float2 e1 = sub2(sub2(a, sub2(s1, t1)), add2(b, t1));
+  const float2 s2 = sub2(c, d), t2 = sub2(s2, c);
+  const float2 e2 = sub2(sub2(c, sub2(s2, t2)), add2(d, t2));
+  return add2(add2(s1, s2), add2(e1, e2));
+}
+// the column west / east of each of this lane's two columns
+__device__ __forceinline__ float2 west(float2 x) { return make_float2(__shfl_up_sync(kFull, x.y, 1), x.x); }
+__device__ __forceinline__ float2 east(float2 x) { return make_float2(x.y, __shfl_down_sync(kFull, x.x, 1)); }
+__device__ __forceinline__ double east_d(double x) { return __shfl_down_sync(kFull, x, 1); }
+__device__ __forceinline__ float2 sel(bool pa, bool pb, float2 a, float2 b) {
+  return make_float2(pa ? a.x : b.x, pb ? a.y : b.y);
+}
+__device__ __forceinline__ float2 pos2(float2 a) { return make_float2(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f)); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(fminf(a.x, 0.f), fminf(a.y, 0.f)); }
+
+// packed masks of one row: 3 bits (ip, iu, iv) for column A, column B and
+// the east neighbour of column B
+constexpr int kSA = 3, kSB = 6, kSE = 9;
+__device__ __forceinline__ bool bit(uint32_t m, int shift, uint32_t b) { return (m >> shift) & b; }
+
+// pipeline registers of one tracer, both columns.  Land neighbours drop
+// out of the 5-point extrema by carrying masked copies of the fields:
+// -BIG (for maxima) or +BIG (for minima) where ip = 0.
+struct St2 {
+  float2 f1;                 // fld at J-1
+  float2 fA1, fB1, fA2, fB2;  // fld at J-1, J-2 masked for maxima (A) / minima (B)
+  float2 c1;                 // fldc at J-1
+  float2 fx1, fy1;           // low-order x (west face) / y (south face) fluxes of row J-1
+  float2 lo2, lo3;           // fldlo at J-2, J-3
+  float2 mxA2, mnB2, mxA3, mnB3;  // fmxlo/fmnlo at J-2, J-3, masked
+  float2 ax2, ay1, ay2;      // antidiffusive x-flux of row J-2; y-fluxes of rows J-1, J-2
+  float2 rp3, rm3;           // Zalesak ratios at J-3
+  float2 lx3, ly3;           // limited fluxes of row J-3
+  float2 qx3, qn3;           // fqmax/fqmin at J-3
+};
+constexpr float kBig = 1.0e30f;   // land sentinel of the masked extrema (finite: no inf*0)
+constexpr float kTiny = 1.0e-30f;  // floor of the Zalesak denominators
+
+}  // namespace
+
+template <int NQ, bool PREP64>
+__global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
+    mix_fct2_col2_kernel(const MixBasin *__restrict__ basins, const int4 *__restrict__ items, int nitems, int *head,
+                         int *err) {
+  using RG = Ring<NQ, PREP64>;
+  extern __shared__ unsigned char c2raw_[];
+  unsigned char *sm = (unsigned char *)(((uintptr_t)c2raw_ + 127) & ~(uintptr_t)127);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned char *ring = sm + wid * RG::WARP;
+  uint64_t *bar = (uint64_t *)(sm + kWarps * RG::WARP) + wid * kNS;
+  if (lane == 0) {
+    for (int s = 0; s < kNS; s++) tma::bar_init(bar + s, 1);
+    tma::fence_bar_init();
+  }
+  __syncwarp();
+  uint32_t tg = 0;  // blocks this warp has consumed (slot and phase of the next one)
+  const float onemu = (float)kOnemu;
+
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(head, 1);
+    it = __shfl_sync(kFull, it, 0);
+    if (it >= nitems) break;
+    const int4 w = items[it];
+    const MixBasin &B = basins[w.x];
+    const int ii = B.ii, jj = B.jj, nb = B.nbdy, ld1 = B.ld1, kdm = B.kdm, ntr = B.ntr;
+    const long long sl = B.slice;
+    const int s0 = 56 * w.y;  // strip start (padded column)
+    const int j0 = 1 + w.z * B.seg, j1 = min(j0 + B.seg, jj + 1);
+    const int nblk = (j1 - j0 + 6 + kRB - 1) / kRB;
+    const int nqp = (ntr + NQ - 1) / NQ;
+    const int T = kdm * nqp * nblk;
+    // this lane's columns: padded a0 = s0 + 2*lane (A) and a0 + 1 (B)
+    const int a0 = s0 + 2 * lane;
+    const int iA = a0 - nb + 1, iB = iA + 1;  // Fortran indices
+    const bool outA = lane >= 2 && lane < 30 && iA >= 1 && iA <= ii;
+    const bool outB = lane >= 2 && lane < 30 && iB >= 1 && iB <= ii;
+
+    auto issue = [&](int t) {  // lane 0: block t of this item into its slot
+      const int k = t / (nqp * nblk);
+      const int rem = t - k * nqp * nblk;
+      const int qp = rem / nblk, blk = rem - qp * nblk;
+      const int y = j0 - 3 + blk * kRB + nb - 1;
+      const uint32_t g = tg + t;
+      unsigned char *slot = ring + (g % kNS) * RG::SLOT;
+      uint64_t *b = bar + (g % kNS);
+      tma::expect_tx(b, RG::TX_BYTES);
+#pragma unroll
+      for (int q = 0; q < NQ; q++) {
+        const int qq = min(qp * NQ + q, ntr - 1);
+        tma::load3(slot + RG::OFF_FO + q * kRB * RG::FROW, B.c2_old, b, s0, y, qq * kdm + k);
+        tma::load3(slot + RG::OFF_FC + q * kRB * RG::FROW, B.c2_cur, b, s0, y, qq * kdm + k);
+      }
+      tma::load3(slot + RG::OFF_U, B.c2_u, b, s0, y, k);
+      tma::load3(slot + RG::OFF_V, B.c2_v, b, s0, y, k);
+      tma::load3(slot + RG::OFF_DP, B.c2_dp, b, s0, y, k);
+      tma::load2(slot + RG::OFF_DQ, B.c2_dq, b, 2 * s0, y);
+      tma::load2(slot + RG::OFF_MK, B.c2_mk, b, s0, y);
+      if (PREP64) tma::load2(slot + RG::OFF_SI, B.c2_si, b, s0, y);
+    };
+    if (lane == 0)
+      for (int t = 0; t < kNS && t < T; t++) issue(t);
+
+    int t = 0;
+    bool ok = true;
+    for (int k = 0; k < kdm && ok; k++) {
+      for (int qp = 0; qp < nqp && ok; qp++) {
+        const int nq = min(NQ, ntr - qp * NQ);
+        float *fn[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; q++) fn[q] = B.fnew + ((long long)(qp * NQ + (q < nq ? q : 0)) * kdm + k) * sl;
+        St2 S[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; q++) S[q] = St2{};
+        const float2 z2 = make_float2(0.f, 0.f);
+        uint32_t m1 = 0, m2 = 0, m3 = 0;
+        float2 u1 = z2, u1m = z2, v1 = z2, R2 = z2, nR3 = z2, QF2 = z2, DS1 = z2, DS2 = z2, DS3 = z2, QS1 = z2;
+        double dA1 = 0.0, dB1 = 0.0, sA1 = 0.0, sB1 = 0.0, vA1 = 0.0, vB1 = 0.0, uA1 = 0.0, uB1 = 0.0;
+        for (int blk = 0; blk < nblk; blk++, t++) {
+          const uint32_t g = tg + t;
+          if (!__all_sync(kFull, tma::wait(bar + (g % kNS), (g / kNS) & 1u, err))) {
+            // give the other copies in flight a bounded chance to land, then stop
+            for (int d = 1; d < kNS && t + d < T; d++) tma::wait(bar + ((g + d) % kNS), ((g + d) / kNS) & 1u, nullptr);
+            ok = false;
+            break;
+          }
+          const unsigned char *slot = ring + (g % kNS) * RG::SLOT;
+#pragma unroll
+          for (int rr = 0; rr < kRB; rr++) {
+            const int J = j0 - 3 + blk * kRB + rr;
+            // ---- inputs of row J
+            const uint32_t *mk = (const uint32_t *)(slot + RG::OFF_MK + rr * kW * 4);
+            const uint2 mab = ((const uint2 *)mk)[lane];
+            const uint32_t me = mk[lane < 31 ? 2 * lane + 2 : 63];
+            const uint32_t m0 = ((mab.x & 7u) << kSA) | ((mab.y & 7u) << kSB) | ((me & 7u) << kSE);
+            const float2 u0 = ((const float2 *)(slot + RG::OFF_U + rr * RG::FROW))[lane];
+            const float2 v0 = ((const float2 *)(slot + RG::OFF_V + rr * RG::FROW))[lane];
+            const double2 d0 = ((const double2 *)(slot + RG::OFF_DP + rr * kW * 8))[lane];
+            const float4 dq0 = ((const float4 *)(slot + RG::OFF_DQ + rr * kW * 8))[lane];
+            float2 f0[NQ], c0[NQ];
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+              f0[q] = ((const float2 *)(slot + RG::OFF_FO + (q * kRB + rr) * RG::FROW))[lane];
+              c0[q] = ((const float2 *)(slot + RG::OFF_FC + (q * kRB + rr) * RG::FROW))[lane];
+            }
+
+            // ---- thickness factors of row J-1 (mod_tsadvc.F90:1905-1942)
+            float2 W1, R1, QF1;
+            if (PREP64) {
+              const double2 si0 = ((const double2 *)(slot + RG::OFF_SI + rr * kW * 8))[lane];
+              const double uA0 = (double)u0.x, uB0 = (double)u0.y, vA0 = (double)v0.x, vB0 = (double)v0.y;
+              const double uE1 = east_d(uA1);  // west face of the column east of B, row J-1
+              const double dvA = ((uB1 - uA1) + (vA0 - vA1)) * sA1;
+              const double dvB = ((uE1 - uB1) + (vB0 - vB1)) * sB1;
+              const double fcoA = kmax(dA1 + dvA, 0.0), fcnA = kmax(dA1, 0.0);
+              const double fcoB = kmax(dB1 + dvB, 0.0), fcnB = kmax(dB1, 0.0);
+              const double hA = fcnA + kOnemu, hB = fcnB + kOnemu;
+              // 1/h: FP32 seed, one Newton step (relative error ~2^-46)
+              double rA = (double)rcp_approx((float)hA), rB = (double)rcp_approx((float)hB);
+              rA = __fma_rn(rA, __fma_rn(-hA, rA, 1.0), rA);
+              rB = __fma_rn(rB, __fma_rn(-hB, rB, 1.0), rB);
+              W1 = make_float2((float)((fcoA + kOnemu) * rA), (float)((fcoB + kOnemu) * rB));
+              R1 = make_float2((float)rA, (float)rB);
+              QF1 = mul2(make_float2((float)fcnA, (float)fcnB), QS1);
+              uA1 = uA0;
+              uB1 = uB0;
+              vA1 = vA0;
+              vB1 = vB0;
+              sA1 = si0.x;
+              sB1 = si0.y;
+            } else {
+              const float2 fdv = mul2(comp_div2(east(u1), u1, v0, v1), DS1);
+              const float2 d = make_float2((float)dA1, (float)dB1);
+              const float2 fcn = pos2(d);
+              const float2 r = make_float2(__frcp_rn(fcn.x + onemu), __frcp_rn(fcn.y + onemu));
+              const float2 w1 = fma2(fdv, r, make_float2(1.f, 1.f));
+              W1.x = (d.x + fdv.x > 0.f) ? (d.x >= 0.f ? w1.x : (d.x + fdv.x + onemu) * r.x) : onemu * r.x;
+              W1.y = (d.y + fdv.y > 0.f) ? (d.y >= 0.f ? w1.y : (d.y + fdv.y + onemu) * r.y) : onemu * r.y;
+              R1 = r;
+              QF1 = mul2(fcn, QS1);
+            }
+            const float2 nR1 = make_float2(-R1.x, -R1.y);
+            // face fluxes with the face masks applied (iu/iv = 0 faces carry no
+            // advective or antidiffusive flux, mod_tsadvc.F90:738-758), split
+            // for the upwind choice: u*f_upwind = max(u,0)*f_west + min(u,0)*f
+            // (one of the two products is zero, so the rounding is that of u*f)
+            const float2 u0m = make_float2(bit(m0, kSA, kIU) ? u0.x : 0.f, bit(m0, kSB, kIU) ? u0.y : 0.f);
+            const float2 v0m = make_float2(bit(m0, kSA, kIV) ? v0.x : 0.f, bit(m0, kSB, kIV) ? v0.y : 0.f);
+            const float2 up0 = pos2(u0m), un0 = neg2(u0m), vp0 = pos2(v0m), vn0 = neg2(v0m);
+            const float2 half = make_float2(0.5f, 0.5f);
+            const float2 u1h = mul2(u1m, half), v0h = mul2(v0m, half);
+            const bool ip0A = bit(m0, kSA, kIP), ip0B = bit(m0, kSB, kIP);
+            const bool ip1A = bit(m1, kSA, kIP), ip1B = bit(m1, kSB, kIP);
+            const bool ip2B = bit(m2, kSB, kIP), ip2E = bit(m2, kSE, kIP);
+            const bool ip3A = bit(m3, kSA, kIP), ip3B = bit(m3, kSB, kIP);
+            const int jo = J - 3;
+            const bool rowout = jo >= j0 && jo < j1;
+            const bool stA = rowout && outA && ip3A, stB = rowout && outB && ip3B;
+            const float2 nbig = make_float2(-kBig, -kBig), pbig = make_float2(kBig, kBig);
+
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+              St2 &s = S[q];
+              // S1: low-order fluxes of row J (:686-720)
+              const float2 fx0 = fma2(up0, west(f0[q]), mul2(un0, f0[q]));
+              const float2 fy0 = fma2(vp0, s.f1, mul2(vn0, f0[q]));
+              const float2 fA0 = sel(ip0A, ip0B, f0[q], nbig), fB0 = sel(ip0A, ip0B, f0[q], pbig);
+              // S2: low-order solution of row J-1 (:778-791), extrema over sea neighbours
+              const float2 c = s.f1;
+              const float2 aw = west(s.fA1), ae = east(s.fA1), bw = west(s.fB1), be = east(s.fB1);
+              const float fmxA = max3f(max3f(c.x, aw.x, ae.x), s.fA2.x, fA0.x);
+              const float fmxB = max3f(max3f(c.y, aw.y, ae.y), s.fA2.y, fA0.y);
+              const float fmnA = min3f(min3f(c.x, bw.x, be.x), s.fB2.x, fB0.x);
+              const float fmnB = min3f(min3f(c.y, bw.y, be.y), s.fB2.y, fB0.y);
+              const float2 fdv = mul2(comp_div2(east(s.fx1), s.fx1, fy0, s.fy1), DS1);
+              const float2 t1 = fma2(c, W1, mul2(fdv, nR1));
+              const float2 lo1 = make_float2(fmaxf(fmnA, fminf(fmxA, t1.x)), fmaxf(fmnB, fminf(fmxB, t1.y)));
+              // S3: antidiffusive fluxes, x of row J-1 and y of row J (:817-833)
+              const float2 ax1 = sub2(mul2(u1h, add2(s.c1, west(s.c1))), s.fx1);
+              const float2 ay0 = sub2(mul2(v0h, add2(c0[q], s.c1)), fy0);
+              const float2 mx1 = make_float2(max3f(c.x, s.c1.x, lo1.x), max3f(c.y, s.c1.y, lo1.y));  // :792-793
+              const float2 mn1 = make_float2(min3f(c.x, s.c1.x, lo1.x), min3f(c.y, s.c1.y, lo1.y));
+              const float2 mxA1 = sel(ip1A, ip1B, mx1, nbig), mnB1 = sel(ip1A, ip1B, mn1, pbig);
+              // S4: Zalesak ratios of row J-2 (:863-909)
+              const float2 xw = west(s.mxA2), xe = east(s.mxA2), nw = west(s.mnB2), ne = east(s.mnB2);
+              const float2 fqmax = make_float2(max3f(max3f(s.mxA2.x, xw.x, xe.x), s.mxA3.x, mxA1.x),
+                                               max3f(max3f(s.mxA2.y, xw.y, xe.y), s.mxA3.y, mxA1.y));
+              const float2 fqmin = make_float2(min3f(min3f(s.mnB2.x, nw.x, ne.x), s.mnB3.x, mnB1.x),
+                                               min3f(min3f(s.mnB2.y, nw.y, ne.y), s.mnB3.y, mnB1.y));
+              const float2 fxa = s.ax2, fxb = sel(ip2B, ip2E, east(s.ax2), s.ax2);  // ipip1 quirk (:873-883)
+              const float2 fya = s.ay2, fyb = sel(ip1A, ip1B, s.ay1, s.ay2);
+              const float2 famax = sub2(add2(sub2(pos2(fxa), neg2(fxb)), pos2(fya)), neg2(fyb));
+              const float2 famin = sub2(add2(sub2(pos2(fxb), neg2(fxa)), pos2(fyb)), neg2(fya));
+              // rp = (qp < famax) ? qp/famax : 1, and 0 when famax <= 0 (:884-903).  Written as
+              // min(1, qp/max(famax,tiny)): equal where it matters (famax <= 0 means no
+              // antidiffusive inflow, so rp multiplies only zero fluxes)
+              const float2 qpv = pos2(mul2(sub2(fqmax, s.lo2), QF2)), qmv = pos2(mul2(sub2(s.lo2, fqmin), QF2));
+              const float2 rp2 = make_float2(fminf(1.f, qpv.x * rcp_approx(fmaxf(famax.x, kTiny))),
+                                             fminf(1.f, qpv.y * rcp_approx(fmaxf(famax.y, kTiny))));
+              const float2 rm2 = make_float2(fminf(1.f, qmv.x * rcp_approx(fmaxf(famin.x, kTiny))),
+                                             fminf(1.f, qmv.y * rcp_approx(fmaxf(famin.y, kTiny))));
+              // S5: limited fluxes of row J-2 (:922-946)
+              const float2 rp2w = west(rp2), rm2w = west(rm2);
+              const float2 cx = make_float2(s.ax2.x < 0.f ? fminf(rp2w.x, rm2.x) : fminf(rp2.x, rm2w.x),
+                                            s.ax2.y < 0.f ? fminf(rp2w.y, rm2.y) : fminf(rp2.y, rm2w.y));
+              const float2 cy = make_float2(s.ay2.x < 0.f ? fminf(s.rp3.x, rm2.x) : fminf(rp2.x, s.rm3.x),
+                                            s.ay2.y < 0.f ? fminf(s.rp3.y, rm2.y) : fminf(rp2.y, s.rm3.y));
+              const float2 lx2 = mul2(cx, s.ax2), ly2 = mul2(cy, s.ay2);
+              // S6: update of row J-3 (:962-982)
+              const float2 fd3 = mul2(comp_div2(east(s.lx3), s.lx3, ly2, s.ly3), DS3);
+              const float2 t3 = fma2(fd3, nR3, s.lo3);
+              const float resA = fmaxf(s.qn3.x, fminf(s.qx3.x, t3.x));
+              const float resB = fmaxf(s.qn3.y, fminf(s.qx3.y, t3.y));
+              if ((stA || stB) && q < nq) {
+                float *p = fn[q] + (long long)a0 + (long long)(jo + nb - 1) * ld1;
+                if (stA) p[0] = resA;
+                if (stB) p[1] = resB;
+                if (B.images) {
+                  if (stA && iA <= B.images) p[ii] = resA;
+                  if (stA && iA > ii - B.images) p[-ii] = resA;
+                  if (stB && iB <= B.images) p[1 + ii] = resB;
+                  if (stB && iB > ii - B.images) p[1 - ii] = resB;
+                }
+              }
+              // shift the pipeline one row
+              s.lx3 = lx2;
+              s.ly3 = ly2;
+              s.qx3 = fqmax;
+              s.qn3 = fqmin;
+              s.rp3 = rp2;
+              s.rm3 = rm2;
+              s.ax2 = ax1;
+              s.ay2 = s.ay1;
+              s.ay1 = ay0;
+              s.mxA3 = s.mxA2;
+              s.mnB3 = s.mnB2;
+              s.mxA2 = mxA1;
+              s.mnB2 = mnB1;
+              s.lo3 = s.lo2;
+              s.lo2 = lo1;
+              s.fx1 = fx0;
+              s.fy1 = fy0;
+              s.c1 = c0[q];
+              s.fA2 = s.fA1;
+              s.fB2 = s.fB1;
+              s.fA1 = fA0;
+              s.fB1 = fB0;
+              s.f1 = f0[q];
+            }
+            // shared per-row state
+            m3 = m2;
+            m2 = m1;
+            m1 = m0;
+            nR3 = make_float2(-R2.x, -R2.y);
+            R2 = R1;
+            QF2 = QF1;
+            DS3 = DS2;
+            DS2 = DS1;
+            DS1 = make_float2(dq0.x, dq0.z);
+            QS1 = make_float2(dq0.y, dq0.w);
+            u1 = u0;
+            u1m = u0m;
+            v1 = v0;
+            dA1 = d0.x;
+            dB1 = d0.y;
+          }
+          __syncwarp();  // every lane is done with the slot before it is refilled
+          if (lane == 0 && t + kNS < T) issue(t + kNS);
+        }
+      }
+    }
+    if (!ok) return;
+    tg += T;
+  }
+}
+
+__global__ void dtsi_kernel(const double *scp2i, double dt2, long long n, double *out) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    out[t] = dt2 * scp2i[t];
+}
+
+cudaError_t launch_dtsi(const double *scp2i, double dt2, long long n, double *out, cudaStream_t s) {
+  int bx = (int)((n + 255) / 256);
+  if (bx > 2048) bx = 2048;
+  dtsi_kernel<<<bx, 256, 0, s>>>(scp2i, dt2, n, out);
+  return cudaGetLastError();
+}
+
+size_t mix_col2_smem(int nq, bool prep64) {
+  if (nq >= 2) return prep64 ? Ring<2, true>::SMEM : Ring<2, false>::SMEM;
+  return prep64 ? Ring<1, true>::SMEM : Ring<1, false>::SMEM;
+}
+
+cudaError_t launch_mix_fct2_col2(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm, int nq,
+                                 bool prep64, int *err, cudaStream_t s) {
+  auto pick = [&](auto kern, size_t smem) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    kern<<<nsm * per_sm, kWarps * 32, smem, s>>>(basins, items, nitems, head, err);
+    return cudaGetLastError();
+  };
+  if (nq >= 2)
+    return prep64 ? pick(mix_fct2_col2_kernel<2, true>, Ring<2, true>::SMEM)
+                  : pick(mix_fct2_col2_kernel<2, false>, Ring<2, false>::SMEM);
+  return prep64 ? pick(mix_fct2_col2_kernel<1, true>, Ring<1, true>::SMEM)
+                : pick(mix_fct2_col2_kernel<1, false>, Ring<1, false>::SMEM);
+}
+
+}  // namespace hyc

@@ -274,7 +274,10 @@ int hyc_ens_put_slices(hyc_ens *ens, int32_t basin, int32_t what, int32_t s0, in
                        int32_t where);
 int hyc_ens_get_slices(hyc_ens *ens, int32_t basin, int32_t what, int32_t s0, int32_t ns, double *dst,
                        int32_t where);
-/* Tile shape of the step kernel (tx x ty cells); hyc_ens_tune picks one. */
+/* Tile shape of the step kernel; hyc_ens_tune picks one.  Mixed form:
+ * tx = 56 is the two-column strip kernel (64-column strips streamed by TMA,
+ * the default; ty = rows per segment, 32/64/128), tx = 26 the one-column
+ * strip kernel (ty likewise), other shapes tx x ty cell tiles. */
 int hyc_ens_set_tile(hyc_ens *ens, int32_t tx, int32_t ty);
 /*
  * Autotuner: time every supported tile shape on this ensemble (the kernel
@@ -308,7 +311,13 @@ int hyc_ens_stats(hyc_ens *ens, hyc_stats *out, int32_t reset);
  * tiles with the Tensor Memory Accelerator, double-buffered (1), or with
  * plain loads (0). */
 #define HYC_OPT_TMA 2
+/* HYC_OPT_STRIP_TRACERS (mixed form, two-column strip kernel; default 2):
+ * tracers advanced per pass over a layer.  2 shares the per-cell thickness
+ * factors between two tracers; 1 needs fewer registers, so more warps fit
+ * on an SM.  hyc_ens_tune tries both. */
+#define HYC_OPT_STRIP_TRACERS 3
 int hyc_ens_set_option(hyc_ens *ens, int32_t option, int32_t value);
+int hyc_ens_get_option(hyc_ens *ens, int32_t option, int32_t *value);
 int hyc_ens_enable_timers(hyc_ens *ens, int32_t on);
 const char *hyc_ens_last_error(const hyc_ens *ens);
 

@@ -113,7 +113,8 @@ def test_tune_keeps_state(cuda):
     load(ens, members)
     before = [get_cur(ens, i, m) for i, m in enumerate(members)]
     tx, ty, ms = ens.tune(2, DELT1)
-    assert (tx, ty) in [(32, 16), (64, 16), (32, 32), (64, 8), (128, 8), (32, 8), (26, 32), (26, 64), (26, 128)]
+    assert (tx, ty) in [(32, 16), (64, 16), (32, 32), (64, 8), (128, 8), (32, 8), (26, 32), (26, 64), (26, 128),
+                        (56, 32), (56, 64), (56, 128)]
     assert ms > 0
     after = [get_cur(ens, i, m) for i, m in enumerate(members)]
     for a, b in zip(before, after):
@@ -187,14 +188,20 @@ def test_ensemble_multistep_conservation_extrema(cuda, prec, prep64, cons_tol, e
 
 @pytest.mark.parametrize("prep64", [True, False])
 def test_mixed_kernels_agree(cuda, prep64):
-    """The column-strip, TMA-tile and plain-tile FP32 kernels compute the
-    same update (same operations per cell; contraction may differ by an ulp)."""
+    """The two-column strip (three segment heights), column-strip, TMA-tile
+    and plain-tile FP32 kernels compute the same update (same operations per
+    cell; contraction, the approximate reciprocal in the limiter ratios and
+    the FP64 reciprocal's Newton step may differ by a few ulp)."""
     outs = []
-    for mode in ("col", "tma", "tile"):
+    for mode in ("col2-32", "col2-64", "col2-128", "col2-64-1", "col", "tma", "tile"):
         members = make_members()
         ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
         ens.set_prep64(prep64)
-        if mode == "col":
+        if mode.startswith("col2"):
+            ens.set_tile(56, int(mode.split("-")[1]))
+            ens.set_strip_tracers(1 if mode.endswith("-1") else 2)
+            assert ens.option("strip_tracers") == (1 if mode.endswith("-1") else 2)
+        elif mode == "col":
             ens.set_tile(26, 32)
         else:
             ens.set_tma(mode == "tma")
