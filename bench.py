@@ -217,7 +217,7 @@ def reference_arm(args, wl):
         "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": ws, "steps": n, "warmup": args.warmup,
         "ms_per_step": dt * 1e3 / max(n, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded generator, HYCOM units/layout)", "impl": "reference",
-        "config": config_of(args, wl),
+        "config": config_of(args, wl, "reference CPU restatement (oracle), FP64"),
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -225,77 +225,226 @@ def reference_arm(args, wl):
     return 0
 
 
-def run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream, precs=("fp64", "mixed")):
-    """The same basin through the ensemble API: FP64 plain (three leapfrog
-    levels, no copy-back) and FP32-mixed, each timed over K steps captured
-    in a CUDA graph; the mixed form's error against the FP64 form after one
-    step from the same inputs is reported per field."""
+ENS_FORMS = {  # form -> (precision, FP64 thickness prep)
+    "fp64": ("fp64", True),
+    "mixed": ("mixed", True),
+    "mixed-fp32prep": ("mixed", False),
+}
+KERNEL_OF_TILE = {26: "mix_fct2_col_kernel", 56: "mix_fct2_col2_kernel"}
+
+
+def make_ensemble(spec, form, stream):
+    import hycadv
+
+    prec, prep64 = ENS_FORMS[form]
+    ens = hycadv.Ensemble([spec], precision=prec)
+    if prec == "mixed":
+        ens.set_prep64(prep64)
+    ens.set_stream(stream)  # graphs are recorded on the library's own stream and replayed here
+    return ens
+
+
+def put_basin(ens, case, kdm):
+    """Leapfrog levels t-1 (old) and t (cur) of T and S, the mass fluxes and
+    dp(:,:,k,n) of one tsadvc call (time level n = 2 of the generated case)."""
+    import torch
+
+    ens.put(0, "old", torch.stack([case.temp[1], case.saln[1]]).contiguous())
+    ens.put(0, "cur", torch.stack([case.temp[0], case.saln[0]]).contiguous())
+    ens.put(0, "uflx", case.uflx)
+    ens.put(0, "vflx", case.vflx)
+    ens.put(0, "dp", case.dp[1].contiguous())
+
+
+def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local, forms):
+    """The basin through the ensemble (batched) API in each form: load, tune,
+    one step from the inputs (kept for the error and content checks), then
+    W warm-up steps and K timed steps replayed from one CUDA graph, bracketed
+    by barriers; content of each tracer before and after one step."""
+    import torch
+
+    kdm = wl["kdm"]
+    ups_step = wl["nx"] * wl["ny"] * kdm * 2
+    peak, _ = peak_hbm()
+    out, first = {}, {}
+    sea = sea_mask(b, masks, dev)
+    for form in forms:
+        prec, _ = ENS_FORMS[form]
+        ens = make_ensemble(spec, form, stream)
+        put_basin(ens, case, kdm)
+        tx, ty, _ = ens.tune(2, wl["delt1"])
+        nq = ens.option("strip_tracers") if prec == "mixed" else None
+        c_old = [ens.content(0, q, "old", wl["delt1"]) for q in range(2)]
+        ens.step(2, wl["delt1"], 1)  # from the inputs: compare one step
+        c_new = [ens.content(0, q, "cur", wl["delt1"]) for q in range(2)]
+        got = torch.empty((2, kdm, b.ld2, b.ld1), dtype=torch.float64, device=dev)
+        ens.get(0, "cur", got)
+        first[form] = got[:, :, sea].clone()
+        del got
+        for _ in range(args.warmup):
+            ens.step(2, wl["delt1"], 1)
+        ens.step(2, wl["delt1"], args.steps, graph=True)  # capture (and one more warm pass)
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            e0.record(stream)
+            ens.step(2, wl["delt1"], args.steps, graph=True)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        ms /= args.steps
+        ws = dist.get_world_size() if dist else 1
+        s_t = 8 if prec == "fp64" else 4  # fluxes as the tracers; dp stays FP64 in both
+        bpu = bytes_per_update(s_t, s_t, 8, 2, kdm)
+        ach = ups_step * bpu / (ms / 1e3) / 1e9
+        out[form] = {"value": ws * ups_step / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "tile": [tx, ty],
+                     "tracers_per_pass": nq, "kernel": KERNEL_OF_TILE.get(tx, "fct tile kernel"),
+                     "algorithmic_bytes_per_update": bpu, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
+                     "graph_steps": args.steps, "clocks": clk.summary(),
+                     "content_change_one_step": {n: abs(c_new[q] - c_old[q]) / abs(c_old[q])
+                                                 for q, n in enumerate(("temp", "saln"))}}
+        ens.close()
+        del ens
+        torch.cuda.empty_cache()
+    if "fp64" in first:
+        ref = first["fp64"]
+        for form in first:
+            if form == "fp64":
+                continue
+            errs = {}
+            for q, name in enumerate(("temp", "saln")):
+                d = first[form][q] - ref[q]
+                scale = ref[q].abs().max()
+                errs[name] = {"max_rel": float(d.abs().max() / scale),
+                              "rms_rel": float(d.pow(2).mean().sqrt() / scale)}
+            out[form]["vs_fp64_one_step"] = errs
+            out[form]["speedup_vs_fp64_ensemble"] = out[form]["value"] / out["fp64"]["value"]
+    return out
+
+
+def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, advtyp=None):
+    """FP64 plain form through the reference-layout C ABI (hyc_tsadvc on
+    resident fields), timed over K steps after W warm-up steps."""
+    advtyp = args.advtyp if advtyp is None else advtyp
     import torch
 
     import hycadv
 
     kdm = wl["kdm"]
-    spec = dict(idm=b.nx, jdm=b.ny, kdm=kdm, nbdy=b.nbdy, nreg=nreg, ntr=2, ip=masks["ip"], iu=masks["iu"],
-                iv=masks["iv"], scp2=sc, scp2i=si)
-    out = {}
-    ups_step = wl["nx"] * wl["ny"] * kdm * 2
-    peak, _ = peak_hbm()
-    first = {}
-    for form in precs:
-        prec = "mixed" if form.startswith("mixed") else "fp64"
-        ens = hycadv.Ensemble([spec], precision=prec)
-        if prec == "mixed":
-            ens.set_prep64(form == "mixed")
-        ens.set_stream(stream)  # graphs are recorded on the library's own stream and launched here
-        old = torch.stack([case.temp[1], case.saln[1]]).contiguous()
-        cur = torch.stack([case.temp[0], case.saln[0]]).contiguous()
-        ens.put(0, "old", old)
-        ens.put(0, "cur", cur)
-        del old, cur
-        ens.put(0, "uflx", case.uflx)
-        ens.put(0, "vflx", case.vflx)
-        ens.put(0, "dp", case.dp[1].contiguous())
-        tx, ty, tms = ens.tune(2, wl["delt1"])
-        ens.step(2, wl["delt1"], 1)  # from the same inputs: compare one step
-        got = torch.empty((2, kdm, b.ld2, b.ld1), dtype=torch.float64, device=dev)
-        ens.get(0, "cur", got)
-        first[form] = got
-        ens.step(2, wl["delt1"], args.steps, graph=True)  # capture
-        torch.cuda.synchronize(dev)
-        ens.enable_timers(True)
-        ens.stats(reset=True)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx = hycadv.Context.from_masks(masks, sc, si, kdm=kdm, nreg=nreg, nbdy=b.nbdy, device=local)
+    ctx.set_stream(stream)
+    for k in ("temp", "saln", "th3d", "uflx", "vflx", "dp"):
+        ctx.bind(k, getattr(case, k))
+
+    def step(s):
+        m, n = ((s + 1) % 2) + 1, (s % 2) + 1
+        ctx.tsadvc(m, n, delt1=wl["delt1"], advtyp=advtyp, nstep=s)
+
+    for s in range(1, args.warmup + 1):
+        step(s)
+    torch.cuda.synchronize(dev)
+    ctx.enable_timers(True)
+    ctx.stats(reset=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
         e0.record(stream)
-        ens.step(2, wl["delt1"], args.steps, graph=True)
+        for s in range(args.warmup + 1, args.warmup + args.steps + 1):
+            step(s)
         e1.record(stream)
         torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1) / args.steps
-        s_t, s_f = (8, 8) if prec == "fp64" else (4, 4)  # dp stays FP64 in both
-        bpu = bytes_per_update(s_t, s_f, 8, 2, kdm)
-        ach = ups_step * bpu / (ms / 1e3) / 1e9
-        out[form] = {"value": ups_step / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "tile": [tx, ty],
-                     "algorithmic_bytes_per_update": bpu, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
-                     "graph_steps": args.steps}
-        ens.close()
-        torch.cuda.empty_cache()
-    if "fp64" not in first or len(first) < 2:
-        return out
-    ip = torch.as_tensor(masks["ip"], device=dev) != 0
-    inner = torch.zeros_like(ip)
-    inner[b.J, b.I] = True
-    sea = ip & inner
-    for form in first:
-        if form == "fp64":
-            continue
-        errs = {}
-        for q, name in enumerate(("temp", "saln")):
-            d = (first[form][q] - first["fp64"][q])[:, sea]
-            ref = first["fp64"][q][:, sea]
-            errs[name] = {"max_rel": float(d.abs().max() / ref.abs().max()),
-                          "rms_rel": float(d.pow(2).mean().sqrt() / ref.abs().max())}
-        out[f"{form}_vs_fp64_one_step"] = errs
-        out[f"{form}_speedup_vs_fp64_ensemble"] = out[form]["value"] / out["fp64"]["value"]
-    return out
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    st = ctx.stats(reset=True)
+    ctx.enable_timers(False)
+    ctx.close()
+    if dist:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ws = dist.get_world_size() if dist else 1
+    ups_step = wl["nx"] * wl["ny"] * kdm * 2
+    adv_ms, adv_calls = st["advect"]
+    bpu = bytes_per_update(8, 8, 8, 2, kdm)
+    peak, peak_kind = peak_hbm()
+    res = {"value": ws * ups_step * args.steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / args.steps,
+           "scheme": SCHEME_NAMES[advtyp],
+           "gpu_launches": int(st["launches"]), "clocks": clk.summary(),
+           "timers_ms": {k: v for k, v in st.items() if k != "launches"}}
+    if adv_calls > 0:
+        avg_s = adv_ms / adv_calls / 1e3
+        achieved = ups_step * bpu / avg_s / 1e9
+        res["roofline"] = {"bound": "fp64-alu (hbm fraction shown)", "achieved": achieved, "peak": peak,
+                           "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                           "kernel": "advect_tile_kernel", "algorithmic_bytes_per_update": bpu,
+                           "avg_launch_ms": adv_ms / adv_calls, "share_of_step": adv_ms / max(st["tsadvc"][0], 1e-9),
+                           "traffic": profile_traffic(f"{SCHEME_NAMES[advtyp].lower()}_fp64_{args.workload}")}
+    return res
+
+
+def run_e2e(args, wl, b, spec, case, form, tile, nq, dev, stream, dist):
+    """The headline form end to end through the C ABI with host buffers: per
+    step hyc_ens_put of T and S (levels t-1 and t), uflx, vflx and dp from
+    pinned host memory (FP64, reference layout), hyc_ens_step, hyc_ens_get
+    of the new level of T and S back to pinned host memory."""
+    import torch
+
+    kdm = wl["kdm"]
+    host = {}
+    host["old"] = torch.stack([case.temp[1], case.saln[1]]).to("cpu").pin_memory()
+    host["cur"] = torch.stack([case.temp[0], case.saln[0]]).to("cpu").pin_memory()
+    for k in ("uflx", "vflx"):
+        host[k] = getattr(case, k).to("cpu").pin_memory()
+    host["dp"] = case.dp[1].contiguous().to("cpu").pin_memory()
+    out = torch.empty_like(host["cur"]).pin_memory()
+    h2d = sum(t.numel() * 8 for t in host.values())
+    d2h = out.numel() * 8
+    ens = make_ensemble(spec, form, stream)
+    if ENS_FORMS[form][0] == "mixed":
+        ens.set_tile(*tile)
+        if nq:
+            ens.set_strip_tracers(nq)
+
+    def e2e_step():
+        for k in ("old", "cur", "uflx", "vflx", "dp"):
+            ens.put(0, k, host[k])
+        ens.step(2, wl["delt1"], 1)
+        ens.get(0, "cur", out)
+
+    e2e_step()
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    f1.record(stream)
+    torch.cuda.synchronize(dev)
+    ems = f0.elapsed_time(f1)
+    if dist:
+        t = torch.tensor([ems], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ems = float(t.item())
+    ens.close()
+    ws = dist.get_world_size() if dist else 1
+    ups_step = wl["nx"] * wl["ny"] * kdm * 2
+    return {"value": ws * ups_step * args.e2e_steps / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": args.e2e_steps, "form": form,
+            "note": "per step: hyc_ens_put of T,S (t-1, t), uflx, vflx, dp from pinned host FP64 arrays "
+                    "(reference layout), hyc_ens_step, hyc_ens_get of the new T,S level"}
 
 
 def c3_members(wl):
@@ -490,13 +639,14 @@ def run_ensemble_workload(args, wl, dev):
     return 0
 
 
-def config_of(args, wl):
-    return {"workload": f"{args.workload}: {'periodic-x' if wl['periodic'] else 'closed'} basin "
-                        f"{wl['nx']}x{wl['ny']}x{wl['kdm']}, T+S, {SCHEME_NAMES[args.advtyp]} "
-                        f"(advtyp={args.advtyp}), FP64 plain, max Courant {wl['courant']}, delt1 {wl['delt1']} s",
-            "form": "fp64-plain", "updates_per_step": wl["nx"] * wl["ny"] * wl["kdm"] * 2,
-            "l2": "inputs larger than L2 (full model state resident in HBM, ~40 GB)" if args.workload == "c1"
-            else "small case, fits in L2", "parallelism": "independent basin replica per GPU"}
+def config_of(args, wl, form):
+    kind = "periodic-x" if wl["periodic"] else "closed"
+    return {"workload": f"{args.workload}: {kind} basin {wl['nx']}x{wl['ny']}x{wl['kdm']}, T+S, "
+                        f"{SCHEME_NAMES[args.advtyp]} (advtyp={args.advtyp}), max Courant {wl['courant']}, "
+                        f"delt1 {wl['delt1']} s",
+            "form": form, "updates_per_step": wl["nx"] * wl["ny"] * wl["kdm"] * 2,
+            "l2": "inputs larger than L2 (state resident in HBM, >20 GB)" if args.workload == "c1"
+            else "small case, fits in L2", "parallelism": "independent basin replica per GPU (replicas only)"}
 
 
 def main():
@@ -508,17 +658,19 @@ def main():
     ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS))
     ap.add_argument("--advtyp", type=int, default=2, choices=[0, 1, 2, 4])
     ap.add_argument("--layers", type=int, default=0, help="override kdm (smaller profiling case)")
+    ap.add_argument("--form", default="mixed-fp32prep", choices=sorted(ENS_FORMS),
+                    help="headline form (ensemble API): FP32-mixed with FP64 thickness prep, with compensated "
+                         "FP32 prep, or FP64")
+    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,fp64,mixed,mixed-fp32prep",
+                    help="forms measured beside the headline (tsadvc[-fct4|-mpdata|-pcm] = FP64 plain through "
+                         "hyc_tsadvc, FCT2 unless named)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-layers", type=int, default=4, help="layers in the CPU sample")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--arm", default="tsadvc", choices=["tsadvc", "ens-fp64", "ens-mixed", "ens-mixed-fp32prep"],
-                    help="tsadvc: the reference-layout C ABI (headline); ens-*: the ensemble form only")
     ap.add_argument("--ens-forms", default="fp64,mixed-fp32prep,mixed",
                     help="c2/c3: ensemble forms to run, fp64 first")
-    ap.add_argument("--no-forms", action="store_true",
-                    help="skip the ensemble FP64 / FP32-mixed forms on the same basin")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = dict(WORKLOADS[args.workload])
@@ -527,7 +679,6 @@ def main():
     if args.impl == "reference":
         return reference_arm(args, wl)
 
-    import numpy as np
     import torch
 
     if args.workload in ("c2", "c3"):
@@ -547,127 +698,33 @@ def main():
     import build as hbuild
 
     hbuild.build()
-    import hycadv
-
+    t_start = time.perf_counter()
     b, masks, nreg, case = make_workload(wl, dev)
     sc, si = b.metrics()
     kdm = wl["kdm"]
-    if args.arm != "tsadvc":  # one ensemble form alone (profiling, form comparisons)
-        prec = args.arm[4:]
-        f = run_forms(args, wl, b, masks, nreg, sc, si, case, dev, torch.cuda.current_stream(dev), precs=(prec,))[prec]
-        peak, peak_kind = peak_hbm()
-        line = {"metric": METRIC, "value": f["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": f["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32-mixed",
-                "data": "synthetic (seeded generator, HYCOM units/layout)", "impl": args.arm,
-                "config": dict(config_of(args, wl), form=f"ensemble-{prec}", tile=f["tile"]),
-                "roofline": {"bound": "hbm", "achieved": f["achieved_GBs"], "peak": peak, "unit": "GB/s",
-                             "frac": f["frac_of_measured_hbm"], "traffic": None, "peak_kind": peak_kind}}
-        if rank == 0:
-            print(json.dumps(line), flush=True)
-        return 0
-    ctx = hycadv.Context.from_masks(masks, sc, si, kdm=kdm, nreg=nreg, nbdy=b.nbdy, device=local)
     stream = torch.cuda.current_stream(dev)
-    ctx.set_stream(stream)
-    for k in ("temp", "saln", "th3d", "uflx", "vflx", "dp"):
-        ctx.bind(k, getattr(case, k))
-    delt1 = wl["delt1"]
+    spec = dict(idm=b.nx, jdm=b.ny, kdm=kdm, nbdy=b.nbdy, nreg=nreg, ntr=2, ip=masks["ip"], iu=masks["iu"],
+                iv=masks["iv"], scp2=sc, scp2i=si)
+    others = [f for f in args.forms.split(",") if f]
+    tsadvc = None
+    if "tsadvc" in others:
+        tsadvc = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local)
+    schemes = {}
+    for f, adv in (("tsadvc-fct4", 4), ("tsadvc-mpdata", 1), ("tsadvc-pcm", 0)):
+        if f in others:
+            schemes[f] = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, adv)
+    ens_forms = [f for f in others if f in ENS_FORMS and f != args.form]
+    if "fp64" in ens_forms:  # the reference of the error checks runs first
+        ens_forms = ["fp64"] + [f for f in ens_forms if f != "fp64"]
+    ens_forms = ens_forms + [args.form]
+    forms = run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local, ens_forms)
+    head = forms[args.form]
 
-    def step(s):
-        m, n = ((s + 1) % 2) + 1, (s % 2) + 1
-        ctx.tsadvc(m, n, delt1=delt1, advtyp=args.advtyp, nstep=s)
-
-    for s in range(1, args.warmup + 1):
-        step(s)
-    torch.cuda.synchronize(dev)
-    ctx.enable_timers(True)
-    ctx.stats(reset=True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        e0.record(stream)
-        for s in range(args.warmup + 1, args.warmup + args.steps + 1):
-            step(s)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-    if dist:
-        dist.barrier()
-    ms = e0.elapsed_time(e1)
-    st = ctx.stats(reset=True)
-    ctx.enable_timers(False)
-    if dist:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ups_step = wl["nx"] * wl["ny"] * kdm * 2
-    value = ups_step * args.steps * ws / (ms / 1e3)
-    ms_step = ms / args.steps
-
-    # roofline of the dominant kernel (fused advection tiles), timed live
-    adv_ms, adv_calls = st["advect"]
-    bpu = bytes_per_update(8, 8, 8, 2, kdm)
-    peak, peak_kind = peak_hbm()
-    roof = None
-    if adv_calls > 0:
-        avg_s = adv_ms / adv_calls / 1e3
-        achieved = ups_step * bpu / avg_s / 1e9
-        tr = profile_traffic(f"fct2_fp64_{args.workload}")
-        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": tr, "peak_kind": peak_kind, "kernel": "advect_tile_kernel",
-                "algorithmic_bytes_per_update": bpu, "avg_launch_ms": adv_ms / adv_calls,
-                "share_of_step": adv_ms / max(st["tsadvc"][0], 1e-9),
-                "note": "FP64 form is FP64-ALU bound on GB300 (FP64 pipe ~1/72 of FP32); see DESIGN.md"}
-    clocks = clk.summary()
-
-    forms = None
-    if not args.no_forms:
-        forms = run_forms(args, wl, b, masks, nreg, sc, si, case, dev, stream, precs=("fp64", "mixed", "mixed-fp32prep"))
-
-    # end-to-end through the C ABI with host buffers (pinned), copies in the timed region
     e2e = None
     if not args.no_e2e:
-        ctx2 = hycadv.Context.from_masks(masks, sc, si, kdm=kdm, nreg=nreg, nbdy=b.nbdy, device=local)
-        ctx2.set_stream(stream)
-        host = {}
-        for k in ("temp", "saln", "uflx", "vflx", "dp"):
-            t = torch.empty(getattr(case, k).shape, dtype=torch.float64, pin_memory=True)
-            t.copy_(getattr(case, k))
-            host[k] = t
-            ctx2.bind(k, t)
-        h2d = sum(host[k].numel() * 8 for k in host)
-        d2h = (host["temp"].numel() + host["saln"].numel()) * 8
-        del case
-        torch.cuda.empty_cache()
-
-        def e2e_step(s):
-            for k in host:
-                ctx2.sync(k, True)
-            m, n = ((s + 1) % 2) + 1, (s % 2) + 1
-            ctx2.tsadvc(m, n, delt1=delt1, advtyp=args.advtyp, nstep=s)
-            ctx2.sync("temp", False)
-            ctx2.sync("saln", False)
-
-        e2e_step(1)
-        torch.cuda.synchronize(dev)
-        if dist:
-            dist.barrier()
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        for s in range(2, 2 + args.e2e_steps):
-            e2e_step(s)
-        f1.record(stream)
-        torch.cuda.synchronize(dev)
-        ems = f0.elapsed_time(f1)
-        if dist:
-            t = torch.tensor([ems], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ems = float(t.item())
-        e2e = {"value": ups_step * args.e2e_steps * ws / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
-               "note": "hyc_sync_field H2D of temp, saln, uflx, vflx, dp (whole arrays) + tsadvc + D2H of temp, saln"}
-        ctx2.close()
+        e2e = run_e2e(args, wl, b, spec, case, args.form, head["tile"], head["tracers_per_pass"], dev, stream, dist)
+    del case
+    torch.cuda.empty_cache()
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -677,16 +734,33 @@ def main():
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
 
     if rank == 0:
+        peak, peak_kind = peak_hbm()
+        prec = ENS_FORMS[args.form][0]
+        key = {"mixed": "col2_mixed", "mixed-fp32prep": "col2_mixed_fp32prep", "fp64": "fct2_fp64_ens"}[args.form]
+        roof = {"bound": "hbm", "achieved": head["achieved_GBs"], "peak": peak, "unit": "GB/s",
+                "frac": head["frac_of_measured_hbm"], "traffic": profile_traffic(f"{key}_{args.workload}"),
+                "peak_kind": peak_kind, "kernel": head["kernel"],
+                "algorithmic_bytes_per_update": head["algorithmic_bytes_per_update"],
+                "avg_launch_ms": head["ms_per_step"], "tile": head["tile"],
+                "tracers_per_pass": head["tracers_per_pass"]}
+        others_out = {k: v for k, v in forms.items() if k != args.form}
+        for f, r in schemes.items():
+            others_out[f"fp64-{f}"] = r
+        if tsadvc:
+            others_out["fp64-tsadvc"] = tsadvc
+            head["speedup_vs_fp64_tsadvc"] = head["value"] / tsadvc["value"]
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, HYCOM units/layout)",
-            "config": config_of(args, wl), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": int(st["launches"]), "clocks": clocks, "forms": forms,
-            "timers_ms": {k: v for k, v in st.items() if k != "launches"},
+            "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-mixed" if prec == "mixed" else "f64",
+            "data": "synthetic (seeded generator, HYCOM units/layout)",
+            "config": dict(config_of(args, wl, f"ensemble-{args.form}"), tile=head["tile"],
+                           tracers_per_pass=head["tracers_per_pass"]),
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
+            "clocks": head["clocks"], "headline": {k: v for k, v in head.items() if k != "clocks"},
+            "forms": others_out, "wall_seconds": time.perf_counter() - t_start,
         }
         print(json.dumps(line), flush=True)
-    ctx.close()
     if dist:
         dist.destroy_process_group()
     return 0

@@ -35,9 +35,9 @@ struct MixBasin {
   int seg;
   int pad2;
   // two-column strip kernel: TMA maps (box 64 x 4 rows) of the old and
-  // centre levels, uflx, vflx, dp, the metric factors (as 2*ld1 floats per
-  // row), the u32 masks and dt2*scp2i (FP64)
-  const CUtensorMap *c2_old, *c2_cur, *c2_u, *c2_v, *c2_dp, *c2_dq, *c2_mk, *c2_si;
+  // centre levels, uflx, vflx, dp, the per-cell factors (float4 as 4*ld1
+  // floats per row) and dt2*scp2i (FP64)
+  const CUtensorMap *c2_old, *c2_cur, *c2_u, *c2_v, *c2_dp, *c2_ge, *c2_si;
 };
 
 bool mix_shape_ok(TileShape t);
@@ -56,6 +56,8 @@ constexpr int kCol2Strip = 56;
 constexpr int kCol2Box = 64, kCol2Rows = 4;
 cudaError_t launch_mix_fct2_col2(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm, int nq,
                                  bool prep64, int *err, cudaStream_t s);
+cudaError_t launch_geo4(const double *scp2, const double *scp2i, const uint8_t *msk, double dt2, long long n,
+                        float4 *out, cudaStream_t s);
 cudaError_t launch_dtsi(const double *scp2i, double dt2, long long n, double *out, cudaStream_t s);
 cudaError_t launch_dsqs(const double *scp2, const double *scp2i, double dt2, long long n, float2 *out,
                         cudaStream_t s);

@@ -31,8 +31,8 @@ struct EBasin {
   double *dp = nullptr;
   void *lev[3] = {nullptr, nullptr, nullptr};  // tracer state, physical levels
   float2 *dsqs = nullptr;                       // column kernel metric factors (mixed form)
-  uint32_t *msk32 = nullptr;                    // masks widened to u32 (TMA rows of the strip kernel)
   double *dtsi = nullptr;                       // dt2*scp2i (strip kernel, FP64 thickness prep)
+  float4 *geo4 = nullptr;                       // strip kernel per-cell factors
   long long work = 0;                           // cells*layers*tracers, for queue ordering
 };
 
@@ -52,7 +52,7 @@ struct hyc_ens {
   int maxntr = 1;        // largest tracer count (column kernel processes tracers in pairs)
   int strip_nq = 2;      // two-column strip kernel: tracers per pass (1 or 2)
   CUtensorMap *d_tmaps = nullptr;  // [nbasin][6]: level 0,1,2, uflx, vflx, dp
-  CUtensorMap *d_cmaps = nullptr;  // [nbasin][9]: strip kernel maps (levels 0-2, u, v, dp, dq, mk, si)
+  CUtensorMap *d_cmaps = nullptr;  // [nbasin][8]: strip kernel maps (levels 0-2, u, v, dp, geo4, si)
   int tm_tx = 0, tm_ty = 0;        // shape the maps were encoded for
   int *d_err = nullptr;            // device error flag (bounded waits that gave up)
   // device tables, one per rotation
@@ -126,8 +126,8 @@ void free_all(hyc_ens *e) {
     cudaFree(b.vflx);
     cudaFree(b.dp);
     cudaFree(b.dsqs);
-    cudaFree(b.msk32);
     cudaFree(b.dtsi);
+    cudaFree(b.geo4);
     for (auto &l : b.lev) cudaFree(l);
   }
   for (int r = 0; r < 3; r++) {
@@ -196,20 +196,18 @@ bool encode2t(CUtensorMap *m, void *base, CUtensorMapDataType dt, size_t es, int
 // maps of the two-column strip kernel; they depend only on the allocations
 int encode_strip_maps(hyc_ens *e) {
   const int bx = hyc::kCol2Box, by = hyc::kCol2Rows;
-  const CUtensorMapDataType F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32, F64 = CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
-                            U32 = CU_TENSOR_MAP_DATA_TYPE_UINT32;
-  std::vector<CUtensorMap> h(e->b.size() * 9);
+  const CUtensorMapDataType F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32, F64 = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  std::vector<CUtensorMap> h(e->b.size() * 8);
   for (size_t i = 0; i < e->b.size(); i++) {
     EBasin &b = e->b[i];
-    CUtensorMap *m = &h[i * 9];
+    CUtensorMap *m = &h[i * 8];
     bool ok = true;
     for (int l = 0; l < 3; l++) ok &= encode3t(m + l, b.lev[l], F32, 4, b.ld1, b.ld2, (long long)b.ntr * b.kdm, bx, by);
     ok &= encode3t(m + 3, b.uflx, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
     ok &= encode3t(m + 4, b.vflx, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
     ok &= encode3t(m + 5, b.dp, F64, 8, b.ld1, b.ld2, b.kdm, bx, by);
-    ok &= encode2t(m + 6, b.dsqs, F32, 4, 2 * b.ld1, b.ld2, 2 * bx, by);
-    ok &= encode2t(m + 7, b.msk32, U32, 4, b.ld1, b.ld2, bx, by);
-    ok &= encode2t(m + 8, b.dtsi, F64, 8, b.ld1, b.ld2, bx, by);
+    ok &= encode2t(m + 6, b.geo4, F32, 4, 4 * b.ld1, b.ld2, 4 * bx, by);
+    ok &= encode2t(m + 7, b.dtsi, F64, 8, b.ld1, b.ld2, bx, by);
     if (!ok) return efail(e, HYC_ERR_CUDA, "cuTensorMapEncodeTiled failed for the strip maps (basin %zu)", i);
   }
   ECK(cudaMemcpy(e->d_cmaps, h.data(), h.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "strip maps copy");
@@ -247,6 +245,7 @@ int build_tables(hyc_ens *e, double dt2) {
       if (!b.dsqs) ECK(cudaMalloc(&b.dsqs, b.slice * sizeof(float2)), "dsqs");
       ECK(hyc::launch_dsqs(b.scp2, b.scp2i, dt2, b.slice, b.dsqs, e->stream), "dsqs");
       if (b.dtsi) ECK(hyc::launch_dtsi(b.scp2i, dt2, b.slice, b.dtsi, e->stream), "dtsi");
+      if (b.geo4) ECK(hyc::launch_geo4(b.scp2, b.scp2i, b.msk, dt2, b.slice, b.geo4, e->stream), "geo4");
     }
   for (int r = 0; r < 3; r++) {
     const int lo = r, lc = (r + 1) % 3, ln = (r + 2) % 3;
@@ -280,15 +279,14 @@ int build_tables(hyc_ens *e, double dt2) {
         m.seg = e->shape.ty;
         m.dsqs = b.dsqs;
         if (e->d_cmaps) {
-          const CUtensorMap *c = e->d_cmaps + i * 9;
+          const CUtensorMap *c = e->d_cmaps + i * 8;
           m.c2_old = c + lo;
           m.c2_cur = c + lc;
           m.c2_u = c + 3;
           m.c2_v = c + 4;
           m.c2_dp = c + 5;
-          m.c2_dq = c + 6;
-          m.c2_mk = c + 7;
-          m.c2_si = c + 8;
+          m.c2_ge = c + 6;
+          m.c2_si = c + 7;
         }
         if (e->d_tmaps) {
           m.tm_old = e->d_tmaps + i * 6 + lo;
@@ -509,8 +507,8 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
     for (int l = 0; l < 3 && ok; l++) ok = cudaMalloc(&b.lev[l], b.slice * b.kdm * b.ntr * es) == cudaSuccess;
     if (ok && precision == HYC_PREC_MIXED)
       ok = cudaMalloc(&b.dsqs, b.slice * sizeof(float2)) == cudaSuccess &&
-           cudaMalloc(&b.msk32, b.slice * sizeof(uint32_t)) == cudaSuccess &&
-           cudaMalloc(&b.dtsi, b.slice * sizeof(double)) == cudaSuccess;
+           cudaMalloc(&b.dtsi, b.slice * sizeof(double)) == cudaSuccess &&
+           cudaMalloc(&b.geo4, b.slice * sizeof(float4)) == cudaSuccess;
     e->b.push_back(b);
     if (!ok) return bail(efail(nullptr, HYC_ERR_NOMEM, "basin %d: device allocation failed", i));
     EBasin &bb = e->b.back();
@@ -521,10 +519,6 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
               cudaMemset(bb.vflx, 0, bb.slice * bb.kdm * es) == cudaSuccess &&
               cudaMemset(bb.dp, 0, bb.slice * bb.kdm * 8) == cudaSuccess;
     for (int l = 0; l < 3 && cp; l++) cp = cudaMemset(bb.lev[l], 0, bb.slice * bb.kdm * bb.ntr * es) == cudaSuccess;
-    if (cp && bb.msk32) {
-      std::vector<uint32_t> m32(m.begin(), m.end());
-      cp = cudaMemcpy(bb.msk32, m32.data(), bb.slice * sizeof(uint32_t), cudaMemcpyHostToDevice) == cudaSuccess;
-    }
     if (!cp) return bail(efail(nullptr, HYC_ERR_CUDA, "basin %d: upload failed", i));
   }
   for (int r = 0; r < 3; r++) {
@@ -543,7 +537,7 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
     if (all6 && encode_fn() && cudaMalloc(&e->d_tmaps, nbasin * 6 * sizeof(CUtensorMap)) == cudaSuccess)
       e->use_tma = true;
     e->shape = hyc::TileShape{hyc::kColStrip, 64};  // column-strip kernel
-    if (encode_fn() && cudaMalloc(&e->d_cmaps, nbasin * 9 * sizeof(CUtensorMap)) == cudaSuccess) {
+    if (encode_fn() && cudaMalloc(&e->d_cmaps, nbasin * 8 * sizeof(CUtensorMap)) == cudaSuccess) {
       if (encode_strip_maps(e) == HYC_OK) {
         e->shape = hyc::TileShape{hyc::kCol2Strip, 64};  // two-column strip kernel
       } else {

@@ -9,9 +9,9 @@
 //
 // Memory: lane 0 of each warp keeps kNS blocks of kRB rows in flight.  A
 // block holds, per row, the old and centre levels of the pass's tracers,
-// uflx, vflx (FP32), dp (FP64), the metric factors (dt2*scp2i, scp2/dt2 as
-// FP32), the cell masks (u32) and, with the FP64 thickness prep, dt2*scp2i
-// in FP64 -- one cp.async.bulk.tensor per array, one mbarrier per slot.
+// uflx, vflx (FP32), dp (FP64), the per-cell factors (dt2*scp2i, scp2/dt2
+// with 0 marking land, iu, iv as FP32) and, with the FP64 thickness prep,
+// dt2*scp2i in FP64 -- one cp.async.bulk.tensor per array, one mbarrier per slot.
 // Out-of-range rows and columns arrive as zeros (TMA fill), so the kernel
 // has no bounds tests on loads.
 //
@@ -25,8 +25,9 @@
 // The flux divergences use two-sum compensation.  The thickness factors
 // W = (fco+onemu)/(fcn+onemu), R = 1/(fcn+onemu), QF = fcn*scp2/dt2 of
 // mod_tsadvc.F90:1905-1942 are formed once per cell and layer, in FP64
-// (PREP64: continuity divergence, thickness and the reciprocal by one
-// Newton step from an FP32 seed) or in compensated FP32.
+// (PREP64: the thickness update, the reciprocal by one Newton step from an
+// FP32 seed and W; the face-flux differences by two-sum in FP32) or in
+// compensated FP32.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -54,9 +55,8 @@ struct Ring {
   static constexpr int OFF_U = OFF_FC + NQ * kRB * FROW;
   static constexpr int OFF_V = OFF_U + kRB * FROW;
   static constexpr int OFF_DP = OFF_V + kRB * FROW;        // double per cell
-  static constexpr int OFF_DQ = OFF_DP + kRB * kW * 8;     // float2 per cell
-  static constexpr int OFF_MK = OFF_DQ + kRB * kW * 8;     // u32 per cell
-  static constexpr int OFF_SI = OFF_MK + kRB * kW * 4;     // double per cell (PREP64)
+  static constexpr int OFF_GE = OFF_DP + kRB * kW * 8;     // float4 per cell
+  static constexpr int OFF_SI = OFF_GE + kRB * kW * 16;    // double per cell (PREP64)
   static constexpr int TX_BYTES = OFF_SI + (PREP64 ? kRB * kW * 8 : 0);
   static constexpr int SLOT = (TX_BYTES + 127) / 128 * 128;
   static constexpr int WARP = kNS * SLOT;
@@ -103,17 +103,13 @@ __device__ __forceinline__ float2 comp_div2(float2 a, float2 b, float2 c, float2
 // the column west / east of each of this lane's two columns
 __device__ __forceinline__ float2 west(float2 x) { return make_float2(__shfl_up_sync(kFull, x.y, 1), x.x); }
 __device__ __forceinline__ float2 east(float2 x) { return make_float2(x.y, __shfl_down_sync(kFull, x.x, 1)); }
-__device__ __forceinline__ double east_d(double x) { return __shfl_down_sync(kFull, x, 1); }
 __device__ __forceinline__ float2 sel(bool pa, bool pb, float2 a, float2 b) {
   return make_float2(pa ? a.x : b.x, pb ? a.y : b.y);
 }
+__device__ __forceinline__ float2 min2(float2 a, float2 b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
 __device__ __forceinline__ float2 pos2(float2 a) { return make_float2(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f)); }
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(fminf(a.x, 0.f), fminf(a.y, 0.f)); }
 
-// packed masks of one row: 3 bits (ip, iu, iv) for column A, column B and
-// the east neighbour of column B
-constexpr int kSA = 3, kSB = 6, kSE = 9;
-__device__ __forceinline__ bool bit(uint32_t m, int shift, uint32_t b) { return (m >> shift) & b; }
 
 // pipeline registers of one tracer, both columns.  Land neighbours drop
 // out of the 5-point extrema by carrying masked copies of the fields:
@@ -131,7 +127,6 @@ struct St2 {
   float2 qx3, qn3;           // fqmax/fqmin at J-3
 };
 constexpr float kBig = 1.0e30f;   // land sentinel of the masked extrema (finite: no inf*0)
-constexpr float kTiny = 1.0e-30f;  // floor of the Zalesak denominators
 
 }  // namespace
 
@@ -160,7 +155,8 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     if (it >= nitems) break;
     const int4 w = items[it];
     const MixBasin &B = basins[w.x];
-    const int ii = B.ii, jj = B.jj, nb = B.nbdy, ld1 = B.ld1, kdm = B.kdm, ntr = B.ntr;
+    const int ii = B.ii, jj = B.jj, nb = B.nbdy, ld1 = B.ld1, kdm = B.kdm, ntr = B.ntr, images = B.images;
+    float *const fnew = B.fnew;
     const long long sl = B.slice;
     const int s0 = 56 * w.y;  // strip start (padded column)
     const int j0 = 1 + w.z * B.seg, j1 = min(j0 + B.seg, jj + 1);
@@ -191,8 +187,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
       tma::load3(slot + RG::OFF_U, B.c2_u, b, s0, y, k);
       tma::load3(slot + RG::OFF_V, B.c2_v, b, s0, y, k);
       tma::load3(slot + RG::OFF_DP, B.c2_dp, b, s0, y, k);
-      tma::load2(slot + RG::OFF_DQ, B.c2_dq, b, 2 * s0, y);
-      tma::load2(slot + RG::OFF_MK, B.c2_mk, b, s0, y);
+      tma::load2(slot + RG::OFF_GE, B.c2_ge, b, 4 * s0, y);
       if (PREP64) tma::load2(slot + RG::OFF_SI, B.c2_si, b, s0, y);
     };
     if (lane == 0)
@@ -205,14 +200,15 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
         const int nq = min(NQ, ntr - qp * NQ);
         float *fn[NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; q++) fn[q] = B.fnew + ((long long)(qp * NQ + (q < nq ? q : 0)) * kdm + k) * sl;
+        for (int q = 0; q < NQ; q++) fn[q] = fnew + ((long long)(qp * NQ + (q < nq ? q : 0)) * kdm + k) * sl;
         St2 S[NQ];
 #pragma unroll
         for (int q = 0; q < NQ; q++) S[q] = St2{};
         const float2 z2 = make_float2(0.f, 0.f);
-        uint32_t m1 = 0, m2 = 0, m3 = 0;
         float2 u1 = z2, u1m = z2, v1 = z2, R2 = z2, nR3 = z2, QF2 = z2, DS1 = z2, DS2 = z2, DS3 = z2, QS1 = z2;
-        double dA1 = 0.0, dB1 = 0.0, sA1 = 0.0, sB1 = 0.0, vA1 = 0.0, vB1 = 0.0, uA1 = 0.0, uB1 = 0.0;
+        float2 L1 = z2, L2 = z2, L3 = z2;  // land flags (1 = land) of rows J-1, J-2, J-3
+        float L2e = 0.f;                   // land flag east of column B, row J-2
+        double dA1 = 0.0, dB1 = 0.0, sA1 = 0.0, sB1 = 0.0;
         for (int blk = 0; blk < nblk; blk++, t++) {
           const uint32_t g = tg + t;
           if (!__all_sync(kFull, tma::wait(bar + (g % kNS), (g / kNS) & 1u, err))) {
@@ -222,18 +218,15 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
             break;
           }
           const unsigned char *slot = ring + (g % kNS) * RG::SLOT;
-#pragma unroll
+#pragma unroll 2
           for (int rr = 0; rr < kRB; rr++) {
             const int J = j0 - 3 + blk * kRB + rr;
             // ---- inputs of row J
-            const uint32_t *mk = (const uint32_t *)(slot + RG::OFF_MK + rr * kW * 4);
-            const uint2 mab = ((const uint2 *)mk)[lane];
-            const uint32_t me = mk[lane < 31 ? 2 * lane + 2 : 63];
-            const uint32_t m0 = ((mab.x & 7u) << kSA) | ((mab.y & 7u) << kSB) | ((me & 7u) << kSE);
             const float2 u0 = ((const float2 *)(slot + RG::OFF_U + rr * RG::FROW))[lane];
             const float2 v0 = ((const float2 *)(slot + RG::OFF_V + rr * RG::FROW))[lane];
             const double2 d0 = ((const double2 *)(slot + RG::OFF_DP + rr * kW * 8))[lane];
-            const float4 dq0 = ((const float4 *)(slot + RG::OFF_DQ + rr * kW * 8))[lane];
+            const float4 gA = ((const float4 *)(slot + RG::OFF_GE + rr * kW * 16))[2 * lane];
+            const float4 gB = ((const float4 *)(slot + RG::OFF_GE + rr * kW * 16))[2 * lane + 1];
             float2 f0[NQ], c0[NQ];
 #pragma unroll
             for (int q = 0; q < NQ; q++) {
@@ -244,25 +237,24 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
             // ---- thickness factors of row J-1 (mod_tsadvc.F90:1905-1942)
             float2 W1, R1, QF1;
             if (PREP64) {
+              // continuity (:1931-1936): the face-flux differences and their sum by
+              // two-sum in FP32 (exact differences, the sum rounded once relative to
+              // the divergence), scaled by dt2*scp2i and added to dp in FP64
               const double2 si0 = ((const double2 *)(slot + RG::OFF_SI + rr * kW * 8))[lane];
-              const double uA0 = (double)u0.x, uB0 = (double)u0.y, vA0 = (double)v0.x, vB0 = (double)v0.y;
-              const double uE1 = east_d(uA1);  // west face of the column east of B, row J-1
-              const double dvA = ((uB1 - uA1) + (vA0 - vA1)) * sA1;
-              const double dvB = ((uE1 - uB1) + (vB0 - vB1)) * sB1;
-              const double fcoA = kmax(dA1 + dvA, 0.0), fcnA = kmax(dA1, 0.0);
-              const double fcoB = kmax(dB1 + dvB, 0.0), fcnB = kmax(dB1, 0.0);
+              const float2 dv = comp_div2(east(u1), u1, v0, v1);
+              const double fdvA = (double)dv.x * sA1, fdvB = (double)dv.y * sB1;
+              const double fcoA = kmax(dA1 + fdvA, 0.0), fcnA = kmax(dA1, 0.0);
+              const double fcoB = kmax(dB1 + fdvB, 0.0), fcnB = kmax(dB1, 0.0);
               const double hA = fcnA + kOnemu, hB = fcnB + kOnemu;
-              // 1/h: FP32 seed, one Newton step (relative error ~2^-46)
-              double rA = (double)rcp_approx((float)hA), rB = (double)rcp_approx((float)hB);
+              // 1/h: FP32 seed, one Newton step in FP64 (relative error ~2^-44)
+              const float2 fcnf = pos2(make_float2((float)dA1, (float)dB1));
+              double rA = (double)rcp_approx(fcnf.x + onemu), rB = (double)rcp_approx(fcnf.y + onemu);
               rA = __fma_rn(rA, __fma_rn(-hA, rA, 1.0), rA);
               rB = __fma_rn(rB, __fma_rn(-hB, rB, 1.0), rB);
-              W1 = make_float2((float)((fcoA + kOnemu) * rA), (float)((fcoB + kOnemu) * rB));
+              // W = (fco+onemu)/(fcn+onemu) = 1 + (fco-fcn)/(fcn+onemu)
+              W1 = make_float2((float)__fma_rn(fcoA - fcnA, rA, 1.0), (float)__fma_rn(fcoB - fcnB, rB, 1.0));
               R1 = make_float2((float)rA, (float)rB);
-              QF1 = mul2(make_float2((float)fcnA, (float)fcnB), QS1);
-              uA1 = uA0;
-              uB1 = uB0;
-              vA1 = vA0;
-              vB1 = vB0;
+              QF1 = mul2(fcnf, QS1);
               sA1 = si0.x;
               sB1 = si0.y;
             } else {
@@ -278,18 +270,19 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
             }
             const float2 nR1 = make_float2(-R1.x, -R1.y);
             // face fluxes with the face masks applied (iu/iv = 0 faces carry no
-            // advective or antidiffusive flux, mod_tsadvc.F90:738-758), split
-            // for the upwind choice: u*f_upwind = max(u,0)*f_west + min(u,0)*f
-            // (one of the two products is zero, so the rounding is that of u*f)
-            const float2 u0m = make_float2(bit(m0, kSA, kIU) ? u0.x : 0.f, bit(m0, kSB, kIU) ? u0.y : 0.f);
-            const float2 v0m = make_float2(bit(m0, kSA, kIV) ? v0.x : 0.f, bit(m0, kSB, kIV) ? v0.y : 0.f);
-            const float2 up0 = pos2(u0m), un0 = neg2(u0m), vp0 = pos2(v0m), vn0 = neg2(v0m);
+            // advective or antidiffusive flux, mod_tsadvc.F90:738-758), split for the
+            // upwind choice: u*f_upwind = max(u,0)*f_west + min(u,0)*f (one of the two
+            // products is zero, so the rounding is that of u*f)
+            const float2 u0m = mul2(u0, make_float2(gA.z, gB.z)), v0m = mul2(v0, make_float2(gA.w, gB.w));
+            const float2 un0 = neg2(u0m), vn0 = neg2(v0m);
+            const float2 up0 = sub2(u0m, un0), vp0 = sub2(v0m, vn0);  // max(x,0) = x - min(x,0), exact
             const float2 half = make_float2(0.5f, 0.5f);
             const float2 u1h = mul2(u1m, half), v0h = mul2(v0m, half);
-            const bool ip0A = bit(m0, kSA, kIP), ip0B = bit(m0, kSB, kIP);
-            const bool ip1A = bit(m1, kSA, kIP), ip1B = bit(m1, kSB, kIP);
-            const bool ip2B = bit(m2, kSB, kIP), ip2E = bit(m2, kSE, kIP);
-            const bool ip3A = bit(m3, kSA, kIP), ip3B = bit(m3, kSB, kIP);
+            // land flags (1 = land): scp2/dt2 is stored as 0 on land
+            const float2 L0 = make_float2(gA.y > 0.f ? 0.f : 1.f, gB.y > 0.f ? 0.f : 1.f);
+            const bool ip1A = L1.x == 0.f, ip1B = L1.y == 0.f;
+            const bool ip2B = L2.y == 0.f, ip2E = L2e == 0.f;  // column B and its east neighbour, row J-2
+            const bool ip3A = L3.x == 0.f, ip3B = L3.y == 0.f;
             const int jo = J - 3;
             const bool rowout = jo >= j0 && jo < j1;
             const bool stA = rowout && outA && ip3A, stB = rowout && outB && ip3B;
@@ -301,7 +294,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               // S1: low-order fluxes of row J (:686-720)
               const float2 fx0 = fma2(up0, west(f0[q]), mul2(un0, f0[q]));
               const float2 fy0 = fma2(vp0, s.f1, mul2(vn0, f0[q]));
-              const float2 fA0 = sel(ip0A, ip0B, f0[q], nbig), fB0 = sel(ip0A, ip0B, f0[q], pbig);
+              const float2 fA0 = fma2(L0, nbig, f0[q]), fB0 = fma2(L0, pbig, f0[q]);  // exact at sea cells
               // S2: low-order solution of row J-1 (:778-791), extrema over sea neighbours
               const float2 c = s.f1;
               const float2 aw = west(s.fA1), ae = east(s.fA1), bw = west(s.fB1), be = east(s.fB1);
@@ -317,7 +310,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               const float2 ay0 = sub2(mul2(v0h, add2(c0[q], s.c1)), fy0);
               const float2 mx1 = make_float2(max3f(c.x, s.c1.x, lo1.x), max3f(c.y, s.c1.y, lo1.y));  // :792-793
               const float2 mn1 = make_float2(min3f(c.x, s.c1.x, lo1.x), min3f(c.y, s.c1.y, lo1.y));
-              const float2 mxA1 = sel(ip1A, ip1B, mx1, nbig), mnB1 = sel(ip1A, ip1B, mn1, pbig);
+              const float2 mxA1 = fma2(L1, nbig, mx1), mnB1 = fma2(L1, pbig, mn1);
               // S4: Zalesak ratios of row J-2 (:863-909)
               const float2 xw = west(s.mxA2), xe = east(s.mxA2), nw = west(s.mnB2), ne = east(s.mnB2);
               const float2 fqmax = make_float2(max3f(max3f(s.mxA2.x, xw.x, xe.x), s.mxA3.x, mxA1.x),
@@ -326,23 +319,28 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
                                                min3f(min3f(s.mnB2.y, nw.y, ne.y), s.mnB3.y, mnB1.y));
               const float2 fxa = s.ax2, fxb = sel(ip2B, ip2E, east(s.ax2), s.ax2);  // ipip1 quirk (:873-883)
               const float2 fya = s.ay2, fyb = sel(ip1A, ip1B, s.ay1, s.ay2);
-              const float2 famax = sub2(add2(sub2(pos2(fxa), neg2(fxb)), pos2(fya)), neg2(fyb));
-              const float2 famin = sub2(add2(sub2(pos2(fxb), neg2(fxa)), pos2(fyb)), neg2(fya));
-              // rp = (qp < famax) ? qp/famax : 1, and 0 when famax <= 0 (:884-903).  Written as
-              // min(1, qp/max(famax,tiny)): equal where it matters (famax <= 0 means no
-              // antidiffusive inflow, so rp multiplies only zero fluxes)
-              const float2 qpv = pos2(mul2(sub2(fqmax, s.lo2), QF2)), qmv = pos2(mul2(sub2(s.lo2, fqmin), QF2));
-              const float2 rp2 = make_float2(fminf(1.f, qpv.x * rcp_approx(fmaxf(famax.x, kTiny))),
-                                             fminf(1.f, qpv.y * rcp_approx(fmaxf(famax.y, kTiny))));
-              const float2 rm2 = make_float2(fminf(1.f, qmv.x * rcp_approx(fmaxf(famin.x, kTiny))),
-                                             fminf(1.f, qmv.y * rcp_approx(fmaxf(famin.y, kTiny))));
+              const float2 nxa = neg2(fxa), nxb = neg2(fxb), nya = neg2(fya), nyb = neg2(fyb);
+              const float2 pxa = sub2(fxa, nxa), pxb = sub2(fxb, nxb), pya = sub2(fya, nya), pyb = sub2(fyb, nyb);
+              const float2 famax = sub2(add2(sub2(pxa, nxb), pya), nyb);
+              const float2 famin = sub2(add2(sub2(pxb, nxa), pyb), nya);
+              // rp = (qp < famax) ? qp/famax : 1, and 0 when famax <= 0 (:884-903), written
+              // as min(1, qp*(1/famax)).  famax >= 0; where it is 0 the product is inf or
+              // NaN and fminf returns 1, which only ever multiplies zero fluxes (no
+              // antidiffusive inflow).  qp >= 0 at sea cells and 0 at land cells (scp2/dt2
+              // is stored as 0 there), so every ratio is finite.
+              const float2 qpv = mul2(sub2(fqmax, s.lo2), QF2), qmv = mul2(sub2(s.lo2, fqmin), QF2);
+              const float2 rp2 = make_float2(fminf(1.f, qpv.x * rcp_approx(famax.x)),
+                                             fminf(1.f, qpv.y * rcp_approx(famax.y)));
+              const float2 rm2 = make_float2(fminf(1.f, qmv.x * rcp_approx(famin.x)),
+                                             fminf(1.f, qmv.y * rcp_approx(famin.y)));
               // S5: limited fluxes of row J-2 (:922-946)
               const float2 rp2w = west(rp2), rm2w = west(rm2);
-              const float2 cx = make_float2(s.ax2.x < 0.f ? fminf(rp2w.x, rm2.x) : fminf(rp2.x, rm2w.x),
-                                            s.ax2.y < 0.f ? fminf(rp2w.y, rm2.y) : fminf(rp2.y, rm2w.y));
-              const float2 cy = make_float2(s.ay2.x < 0.f ? fminf(s.rp3.x, rm2.x) : fminf(rp2.x, s.rm3.x),
-                                            s.ay2.y < 0.f ? fminf(s.rp3.y, rm2.y) : fminf(rp2.y, s.rm3.y));
-              const float2 lx2 = mul2(cx, s.ax2), ly2 = mul2(cy, s.ay2);
+              // lx = max(ax,0)*min(rp,rm_w) + min(ax,0)*min(rp_w,rm): one product is
+              // zero, so the rounding is that of the reference's single product
+              const float2 nax = neg2(s.ax2), pax = sub2(s.ax2, nax);
+              const float2 nay = neg2(s.ay2), pay = sub2(s.ay2, nay);
+              const float2 lx2 = fma2(pax, min2(rp2, rm2w), mul2(nax, min2(rp2w, rm2)));
+              const float2 ly2 = fma2(pay, min2(rp2, s.rm3), mul2(nay, min2(s.rp3, rm2)));
               // S6: update of row J-3 (:962-982)
               const float2 fd3 = mul2(comp_div2(east(s.lx3), s.lx3, ly2, s.ly3), DS3);
               const float2 t3 = fma2(fd3, nR3, s.lo3);
@@ -352,11 +350,11 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
                 float *p = fn[q] + (long long)a0 + (long long)(jo + nb - 1) * ld1;
                 if (stA) p[0] = resA;
                 if (stB) p[1] = resB;
-                if (B.images) {
-                  if (stA && iA <= B.images) p[ii] = resA;
-                  if (stA && iA > ii - B.images) p[-ii] = resA;
-                  if (stB && iB <= B.images) p[1 + ii] = resB;
-                  if (stB && iB > ii - B.images) p[1 - ii] = resB;
+                if (images) {
+                  if (stA && iA <= images) p[ii] = resA;
+                  if (stA && iA > ii - images) p[-ii] = resA;
+                  if (stB && iB <= images) p[1 + ii] = resB;
+                  if (stB && iB > ii - images) p[1 - ii] = resB;
                 }
               }
               // shift the pipeline one row
@@ -385,16 +383,17 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               s.f1 = f0[q];
             }
             // shared per-row state
-            m3 = m2;
-            m2 = m1;
-            m1 = m0;
+            L3 = L2;
+            L2 = L1;
+            L2e = __shfl_down_sync(kFull, L1.x, 1);  // the column east of B
             nR3 = make_float2(-R2.x, -R2.y);
             R2 = R1;
             QF2 = QF1;
             DS3 = DS2;
             DS2 = DS1;
-            DS1 = make_float2(dq0.x, dq0.z);
-            QS1 = make_float2(dq0.y, dq0.w);
+            DS1 = make_float2(gA.x, gB.x);
+            QS1 = make_float2(gA.y, gB.y);
+            L1 = L0;
             u1 = u0;
             u1m = u0m;
             v1 = v0;
@@ -409,6 +408,25 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     if (!ok) return;
     tg += T;
   }
+}
+
+// per-cell factors of the strip kernel: dt2*scp2i, scp2/dt2 (0 on land, so
+// the Zalesak ratios of land cells stay finite), iu and iv as 0/1
+__global__ void geo4_kernel(const double *scp2, const double *scp2i, const uint8_t *msk, double dt2, long long n,
+                            float4 *out) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const uint8_t m = msk[t];
+    out[t] = make_float4((float)(dt2 * scp2i[t]), (m & kIP) ? (float)(scp2[t] / dt2) : 0.f, (m & kIU) ? 1.f : 0.f,
+                         (m & kIV) ? 1.f : 0.f);
+  }
+}
+
+cudaError_t launch_geo4(const double *scp2, const double *scp2i, const uint8_t *msk, double dt2, long long n,
+                        float4 *out, cudaStream_t s) {
+  int bx = (int)((n + 255) / 256);
+  if (bx > 2048) bx = 2048;
+  geo4_kernel<<<bx, 256, 0, s>>>(scp2, scp2i, msk, dt2, n, out);
+  return cudaGetLastError();
 }
 
 __global__ void dtsi_kernel(const double *scp2i, double dt2, long long n, double *out) {
