@@ -48,6 +48,9 @@ WORKLOADS = {
     "c2": dict(nx=4500, ny=3298, kdm=41, periodic=True, courant=0.8, delt1=240.0, seed=1, ntr=10),
     # batching form: 96 closed basins, nx 120-1500, ny 90-1100, kdm 22/32/41, 2-6 tracers
     "c3": dict(nbasin=96, periodic=False, courant=0.5, delt1=1800.0, seed=3, steps=30),
+    # combined: 48 closed regional basins 800x600 .. 3000x2000, kdm 41, T, S + 8 passive tracers,
+    # FP32-mixed FCT2 and MPDATA, Courant 0.9, 100 steps; more state than HBM, so resident waves
+    "c4": dict(nbasin=48, periodic=False, courant=0.9, delt1=1800.0, seed=4, steps=100, kdm=41, ntr=10),
 }
 SCHEME_NAMES = {0: "PCM", 1: "MPDATA", 2: "FCT2", 4: "FCT4"}
 FALLBACK_HBM_GBS = 6800.0
@@ -272,7 +275,12 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
         prec, _ = ENS_FORMS[form]
         ens = make_ensemble(spec, form, stream)
         put_basin(ens, case, kdm)
-        tx, ty, _ = ens.tune(2, wl["delt1"])
+        if args.tile and prec == "mixed":  # fixed shape (profiling): no tuner launches
+            tx, ty, nq_ = args.tile
+            ens.set_tile(tx, ty)
+            ens.set_strip_tracers(nq_)
+        else:
+            tx, ty, _ = ens.tune(2, wl["delt1"])
         nq = ens.option("strip_tracers") if prec == "mixed" else None
         c_old = [ens.content(0, q, "old", wl["delt1"]) for q in range(2)]
         ens.step(2, wl["delt1"], 1)  # from the inputs: compare one step
@@ -639,6 +647,193 @@ def run_ensemble_workload(args, wl, dev):
     return 0
 
 
+def c4_members(wl, layers=0):
+    """Seeded sizes of the 48-basin combined workload."""
+    import numpy as np
+
+    rng = np.random.default_rng(wl["seed"])
+    return [dict(nx=int(rng.integers(800, 3001)), ny=int(rng.integers(600, 2001)), kdm=layers or wl["kdm"],
+                 ntr=wl["ntr"], seed=2000 + bi) for bi in range(wl["nbasin"])]
+
+
+def mixed_state_bytes(spec):
+    """Device bytes of one FP32-mixed ensemble basin (three tracer levels,
+    fluxes, dp and the per-cell tables)."""
+    ld1 = (spec["idm"] + 2 * spec["nbdy"] + 3) // 4 * 4
+    sl = ld1 * (spec["jdm"] + 2 * spec["nbdy"])
+    return sl * spec["kdm"] * (3 * spec["ntr"] * 4 + 2 * 4 + 8) + sl * (1 + 8 + 8 + 8 + 16 + 8)
+
+
+def run_c4(args, wl, dev):
+    """Combined workload: FP32-mixed FCT2 and MPDATA (compensated FP32 prep)
+    over 48 basins advanced in resident waves (each wave: load, then all
+    steps replayed from a 10-step CUDA graph).  The error against the FP64
+    form, the content change and the new-extrema check come from one step of
+    the smallest basin; the FP64 form's rate from the same basin; the CPU
+    baseline from the oracle on that basin with 4 layers."""
+    import torch
+
+    import hycadv
+
+    t_start = time.perf_counter()
+    members = c4_members(wl, args.layers)
+    steps = args.c4_steps
+    gsteps = min(10, steps)
+    reps = max(1, steps // gsteps)
+    geos = [member_geometry(m, wl) for m in members]
+    specs = [g[2] for g in geos]
+    free, _ = torch.cuda.mem_get_info(dev)
+    budget = 0.75 * free - 24e9  # room for generating one basin in FP64
+    waves, cur, tot = [], [], 0.0
+    for i, sp in enumerate(specs):
+        nbytes = mixed_state_bytes(sp)
+        if cur and tot + nbytes > budget:
+            waves.append(cur)
+            cur, tot = [], 0.0
+        cur.append(i)
+        tot += nbytes
+    waves.append(cur)
+    ups_step = sum(sp["idm"] * sp["jdm"] * sp["kdm"] * sp["ntr"] for sp in specs)
+    peak, peak_kind = peak_hbm()
+    small = min(range(len(specs)), key=lambda i: specs[i]["idm"] * specs[i]["jdm"])
+    schemes = {"fct2": 2, "mpdata": 1}
+    res = {}
+    for name, adv in schemes.items():
+        # accuracy on the smallest basin: FP64 ensemble vs FP32-mixed, one step from the same inputs
+        acc = {}
+        refs = {}
+        for prec in ("fp64", "mixed"):
+            ens = hycadv.Ensemble([specs[small]], precision=prec)
+            if prec == "mixed":
+                ens.set_prep64(False)
+            ens.set_posdef(0, 0, 256.0)
+            bounds = load_member(ens, 0, members[small], geos[small], wl, dev)
+            ens.tune(adv, wl["delt1"])
+            sp = specs[small]
+            c_old = [ens.content(0, q, "old", wl["delt1"]) for q in range(sp["ntr"])]
+            ens.step(adv, wl["delt1"], 1)
+            b, masks, _ = geos[small]
+            sea = sea_mask(b, masks, dev)
+            buf = torch.empty((sp["kdm"], b.ld2, b.ld1), dtype=torch.float64, device=dev)
+            per = []
+            for q in range(sp["ntr"]):
+                ens.get(0, "cur", buf, s0=q * sp["kdm"], ns=sp["kdm"])
+                new = buf[:, sea].clone()
+                lo, hi = bounds[q]
+                r = {"content_change_one_step": abs(ens.content(0, q, "cur", wl["delt1"]) - c_old[q]) / abs(c_old[q]),
+                     "new_extrema_rel": float(max(lo - new.min(), new.max() - hi, 0.0)) / max(abs(lo), abs(hi))}
+                if prec == "fp64":
+                    refs[q] = new
+                else:
+                    d = new - refs[q]
+                    scale = float(refs[q].abs().max())
+                    r["max_rel_err_vs_fp64"] = float(d.abs().max()) / scale
+                    r["rms_rel_err_vs_fp64"] = float(d.pow(2).mean().sqrt()) / scale
+                per.append(r)
+            if prec == "fp64":  # the FP64 form's rate on this basin
+                ens.step(adv, wl["delt1"], 3, graph=True)
+                torch.cuda.synchronize(dev)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                st = torch.cuda.current_stream(dev)
+                e0.record(st)
+                ens.step(adv, wl["delt1"], 3, graph=True)
+                e1.record(st)
+                torch.cuda.synchronize(dev)
+                acc["fp64_rate_smallest_basin"] = sp["idm"] * sp["jdm"] * sp["kdm"] * sp["ntr"] * 3 / (
+                    e0.elapsed_time(e1) / 1e3)
+            acc[prec] = per
+            ens.close()
+            del ens, buf
+            torch.cuda.empty_cache()
+        refs.clear()
+        # throughput over all basins, wave by wave
+        t_ms, t_ups, load_s, tile, nq, clk_all = 0.0, 0.0, 0.0, None, None, []
+        for wv in waves:
+            ens = hycadv.Ensemble([specs[i] for i in wv], precision="mixed")
+            ens.set_prep64(False)
+            for j in range(len(wv)):
+                ens.set_posdef(j, 0, 256.0)
+            t0 = time.perf_counter()
+            for j, i in enumerate(wv):
+                load_member(ens, j, members[i], geos[i], wl, dev)
+            torch.cuda.synchronize(dev)
+            torch.cuda.empty_cache()
+            load_s += time.perf_counter() - t0
+            if tile is None:
+                tx, ty, _ = ens.tune(adv, wl["delt1"])
+                tile, nq = (tx, ty), ens.option("strip_tracers")
+            else:
+                ens.set_tile(*tile)
+                ens.set_strip_tracers(nq)
+            ens.step(adv, wl["delt1"], gsteps, graph=True)  # capture + warm-up
+            torch.cuda.synchronize(dev)
+            st = torch.cuda.current_stream(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with ClockSampler(0) as clk:
+                e0.record(st)
+                for _ in range(reps):
+                    ens.step(adv, wl["delt1"], gsteps, graph=True)
+                e1.record(st)
+                torch.cuda.synchronize(dev)
+            clk_all.append(clk.summary())
+            t_ms += e0.elapsed_time(e1)
+            t_ups += sum(specs[i]["idm"] * specs[i]["jdm"] * specs[i]["kdm"] * specs[i]["ntr"] for i in wv) * gsteps * reps
+            ens.close()
+            del ens
+            torch.cuda.empty_cache()
+        rate = t_ups / (t_ms / 1e3)
+        nbytes = sum(sp["idm"] * sp["jdm"] * sp["kdm"] * sp["ntr"] *
+                     (bytes_per_update(4, 4, 8, sp["ntr"], sp["kdm"]) - (4 if adv == 1 else 0)) for sp in specs)
+        ach = nbytes * (t_ups / ups_step) / (t_ms / 1e3) / 1e9
+        res[name] = {"value": rate, "unit": UNIT, "ms_per_step_all_basins": t_ms / (gsteps * reps), "tile": list(tile),
+                     "tracers_per_pass": nq, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
+                     "waves": len(waves), "load_seconds": load_s, "steps_per_wave": gsteps * reps,
+                     "accuracy_smallest_basin": acc, "clocks": clk_all[0]}
+    # CPU baseline: the oracle on the smallest basin, 4 layers, T, S + 8 tracers
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        from oracle import oracle
+
+        from hycadv import synth
+
+        m = members[small]
+        b, masks, _ = geos[small]
+        sc, si = b.metrics()
+        g = oracle.Grid(b.depth, sc, si, nbdy=b.nbdy, threads=threads)
+        c = synth.build_case(b, g.masks, kdm=4, ntracr=8, seed=m["seed"], courant=wl["courant"], delt1=wl["delt1"],
+                             device=dev)
+        h = {k: getattr(c, k).cpu().numpy().copy() for k in ("temp", "saln", "th3d", "uflx", "vflx", "dp", "tracer")}
+        del c
+        import numpy as np
+
+        tf = np.zeros(8, np.int32)
+        n, t0 = 0, time.perf_counter()
+        while n < 2 or time.perf_counter() - t0 < args.cpu_seconds:
+            n += 1
+            mm, nn = ((n + 1) % 2) + 1, (n % 2) + 1
+            g.tsadvc(mm, nn, temp=h["temp"], saln=h["saln"], th3d=h["th3d"], uflx=h["uflx"], vflx=h["vflx"],
+                     dp=h["dp"], delt1=wl["delt1"], advtyp=2, tracer=h["tracer"], trcflg=tf, nstep=n)
+        dt = time.perf_counter() - t0
+        cpu = {"value": b.nx * b.ny * 4 * 10 * n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"smallest basin {b.nx}x{b.ny}, 4 of 41 layers, T, S + 8 tracers, FCT2, {n} steps"}
+    head = res["fct2"]
+    desc = (f"c4: {len(members)} closed basins 800x600..3000x2000, kdm {members[0]['kdm']}, T, S + 8 passive tracers, "
+            f"FP32-mixed FCT2 and MPDATA, max Courant {wl['courant']}, delt1 {wl['delt1']} s, {steps} steps per basin, "
+            f"{len(waves)} resident waves")
+    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": gsteps,
+            "ms_per_step": head["ms_per_step_all_basins"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-mixed", "data": "synthetic (seeded generator, HYCOM units/layout)",
+            "impl": "ensemble-c4",
+            "config": {"workload": desc, "form": "mixed-fp32prep", "updates_per_step": ups_step,
+                       "l2": "inputs larger than L2 (state resident in HBM)"},
+            "roofline": {"bound": "hbm", "achieved": head["achieved_GBs"], "peak": peak, "unit": "GB/s",
+                         "frac": head["frac_of_measured_hbm"], "traffic": None, "peak_kind": peak_kind},
+            "cpu_baseline": cpu, "clocks": head["clocks"], "forms": res, "wall_seconds": time.perf_counter() - t_start}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def config_of(args, wl, form):
     kind = "periodic-x" if wl["periodic"] else "closed"
     return {"workload": f"{args.workload}: {kind} basin {wl['nx']}x{wl['ny']}x{wl['kdm']}, T+S, "
@@ -665,6 +860,8 @@ def main():
                     help="forms measured beside the headline (tsadvc[-fct4|-mpdata|-pcm] = FP64 plain through "
                          "hyc_tsadvc, FCT2 unless named)")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--c4-steps", type=int, default=100, help="c4: steps per basin")
+    ap.add_argument("--tile", default="", help="mixed forms: fixed tile 'tx,ty,tracers_per_pass' instead of the tuner")
     ap.add_argument("--ref-layers", type=int, default=4, help="layers in the CPU sample")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -673,6 +870,7 @@ def main():
                     help="c2/c3: ensemble forms to run, fp64 first")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    args.tile = tuple(int(x) for x in args.tile.split(",")) if args.tile else None
     wl = dict(WORKLOADS[args.workload])
     if args.layers > 0:
         wl["kdm"] = args.layers
@@ -681,10 +879,12 @@ def main():
 
     import torch
 
-    if args.workload in ("c2", "c3"):
+    if args.workload in ("c2", "c3", "c4"):
         import build as hbuild
 
         hbuild.build()
+        if args.workload == "c4":
+            return run_c4(args, wl, torch.device("cuda:0"))
         return run_ensemble_workload(args, wl, torch.device("cuda:0"))
     ws, rank, local = dist_setup()
     dist = None

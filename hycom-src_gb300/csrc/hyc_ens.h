@@ -33,7 +33,8 @@ struct MixBasin {
   // column kernel: (dt2*scp2i, scp2/dt2) per cell, rows per segment
   const float2 *dsqs;
   int seg;
-  int pad2;
+  int kchunk;  // two-column strip kernel: layers per work item
+  float posdef[kMaxFields];  // MPDATA offset of each tracer (mod_tsadvc.F90:1755-1763)
   // two-column strip kernel: TMA maps (box 64 x 4 rows) of the old and
   // centre levels, uflx, vflx, dp, the per-cell factors (float4 as 4*ld1
   // floats per row) and dt2*scp2i (FP64)
@@ -54,8 +55,8 @@ cudaError_t launch_mix_fct2_col(const MixBasin *basins, const int4 *items, int n
 // two columns per lane, 64-column strips (56 updated) streamed by TMA
 constexpr int kCol2Strip = 56;
 constexpr int kCol2Box = 64, kCol2Rows = 4;
-cudaError_t launch_mix_fct2_col2(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm, int nq,
-                                 bool prep64, int *err, cudaStream_t s);
+cudaError_t launch_mix_col2(int scheme, const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm,
+                            int nq, bool prep64, int *err, cudaStream_t s);
 cudaError_t launch_geo4(const double *scp2, const double *scp2i, const uint8_t *msk, double dt2, long long n,
                         float4 *out, cudaStream_t s);
 cudaError_t launch_dtsi(const double *scp2i, double dt2, long long n, double *out, cudaStream_t s);

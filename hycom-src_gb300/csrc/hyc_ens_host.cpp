@@ -34,6 +34,7 @@ struct EBasin {
   double *dtsi = nullptr;                       // dt2*scp2i (strip kernel, FP64 thickness prep)
   float4 *geo4 = nullptr;                       // strip kernel per-cell factors
   long long work = 0;                           // cells*layers*tracers, for queue ordering
+  std::vector<double> posdef;                   // MPDATA offset per tracer (0 unless set)
 };
 
 }  // namespace
@@ -58,6 +59,7 @@ struct hyc_ens {
   // device tables, one per rotation
   MixBasin *d_mix[3] = {nullptr, nullptr, nullptr};
   TileArgs *d_targs[3] = {nullptr, nullptr, nullptr};
+  std::vector<TileArgs> h_targs[3];  // host copies (FP64 PCM/MPDATA run the plain tile kernel per basin)
   double tbl_dt2 = -1.0;
   int4 *d_items = nullptr;
   int nitems = 0;
@@ -235,6 +237,22 @@ int encode_maps(hyc_ens *e) {
   return HYC_OK;
 }
 
+// Layers per work item of the two-column strip kernel: enough items for
+// about 16 per resident warp over the whole ensemble (so the last wave of
+// the queue is short), and no more than 8 layers per item unless the
+// ensemble is small.
+int col2_kchunk(const hyc_ens *e, const EBasin &) {
+  long long cols = 0;  // (strip, segment, layer) units over the ensemble
+  for (const auto &b : e->b) {
+    const long long nstrip = (b.nbdy + b.idm - 4 + hyc::kCol2Strip - 1) / hyc::kCol2Strip;
+    const long long nseg = (b.jdm + e->shape.ty - 1) / e->shape.ty;
+    cols += nstrip * nseg * b.kdm;
+  }
+  const long long want = 16LL * e->nsm * 8;  // ~16 items per warp at 8 warps per SM
+  long long kc = cols / std::max(want, 1LL);
+  return (int)std::max(1LL, std::min(8LL, kc));
+}
+
 // device tables for the three rotations (rebuilt when delt1 changes)
 int build_tables(hyc_ens *e, double dt2) {
   if (e->tbl_dt2 == dt2) return HYC_OK;
@@ -277,6 +295,8 @@ int build_tables(hyc_ens *e, double dt2) {
         m.fcur = (const float *)b.lev[lc];
         m.fnew = (float *)b.lev[ln];
         m.seg = e->shape.ty;
+        m.kchunk = col2_kchunk(e, b);
+        for (int q = 0; q < b.ntr && q < hyc::kMaxFields; q++) m.posdef[q] = (float)b.posdef[q];
         m.dsqs = b.dsqs;
         if (e->d_cmaps) {
           const CUtensorMap *c = e->d_cmaps + i * 8;
@@ -326,13 +346,14 @@ int build_tables(hyc_ens *e, double dt2) {
           a.f[q].k_off = 0;
           a.f[q].kmin = 1;
           a.f[q].kmax = b.kdm;
-          a.f[q].posdef = 0.0;
+          a.f[q].posdef = b.posdef[q];
         }
         a.out = (double *)b.lev[ln];
         a.kdm = b.kdm;
         a.images = b.nreg == 1 ? std::min(5, b.nbdy) : 0;
       }
       ECK(cudaMemcpy(e->d_targs[r], t.data(), nb * sizeof(TileArgs), cudaMemcpyHostToDevice), "fp64 table");
+      e->h_targs[r] = t;
     }
   }
   e->tbl_dt2 = dt2;
@@ -351,10 +372,13 @@ int build_items(hyc_ens *e) {
   for (int i = 0; i < (int)e->b.size(); i++) {
     const EBasin &b = e->b[i];
     const int ntx = (b.idm + e->shape.tx - 1) / e->shape.tx, nty = (b.jdm + e->shape.ty - 1) / e->shape.ty;
-    if (is_col2(e->shape)) {  // (basin, 56-column strip, segment), all layers and tracers
+    if (is_col2(e->shape)) {  // (basin, 56-column strip, segment, chunk of layers), all tracers
       const int nstrip = (b.nbdy + b.idm - 4 + hyc::kCol2Strip - 1) / hyc::kCol2Strip;
-      for (int sg = 0; sg < nty; sg++)
-        for (int st = 0; st < nstrip; st++) w.push_back({(long long)b.kdm * b.ntr, make_int4(i, st, sg, 0)});
+      const int kc = col2_kchunk(e, b), nkc = (b.kdm + kc - 1) / kc;
+      for (int kq = 0; kq < nkc; kq++)
+        for (int sg = 0; sg < nty; sg++)
+          for (int st = 0; st < nstrip; st++)
+            w.push_back({(long long)(std::min(b.kdm, (kq + 1) * kc) - kq * kc) * b.ntr, make_int4(i, st, sg, kq)});
       continue;
     }
     if (is_col(e->shape)) {  // (basin, strip, segment), all layers and tracers
@@ -411,8 +435,19 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
   ECK(cudaMemsetAsync(e->d_head + h, 0, sizeof(int), st), "queue reset");
   cudaError_t c;
   if (e->prec == HYC_PREC_MIXED && is_col2(e->shape))
-    c = hyc::launch_mix_fct2_col2(e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm,
-                                  std::min(e->strip_nq, e->maxntr), e->prep64, e->d_err, st);
+    c = hyc::launch_mix_col2(advtyp, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm,
+                             std::min(e->strip_nq, e->maxntr), e->prep64, e->d_err, st);
+  else if (e->prec != HYC_PREC_MIXED && (advtyp == 0 || advtyp == 1)) {
+    // FP64 PCM/MPDATA: the plain form's tile kernel per basin, then the periodic halo
+    c = cudaSuccess;
+    for (size_t i = 0; i < e->b.size() && c == cudaSuccess; i++) {
+      const EBasin &b = e->b[i];
+      c = hyc::launch_advect_tiles(advtyp, e->h_targs[r][i], b.kdm, e->shape, st);
+      if (c == cudaSuccess && b.nreg == 1)
+        c = hyc::launch_xctilr((double *)b.lev[(r + 2) % 3], b.slice, b.ntr * b.kdm, b.idm, b.jdm, b.nbdy, b.ld1,
+                               std::min(5, b.nbdy), std::min(5, b.nbdy), b.nreg, st);
+    }
+  }
   else if (e->prec == HYC_PREC_MIXED && is_col(e->shape))
     c = hyc::launch_mix_fct2_col(e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->maxntr, e->prep64,
                                  e->shape.ty, st);
@@ -428,8 +463,17 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
   return HYC_OK;
 }
 
+// Schemes per form and kernel: FP64 FCT2/FCT4 (queue kernel) and PCM/MPDATA
+// (plain tile kernel); FP32-mixed FCT2 (every kernel) and MPDATA (two-column
+// strip kernel).
+bool scheme_ok(const hyc_ens *e, int advtyp, hyc::TileShape t) {
+  if (e->prec == HYC_PREC_MIXED) return advtyp == 2 || (advtyp == 1 && is_col2(t));
+  return advtyp == 0 || advtyp == 1 || advtyp == 2 || advtyp == 4;
+}
+
 bool shape_ok(const hyc_ens *e, hyc::TileShape t) {
-  if (e->prec == HYC_PREC_MIXED && is_col2(t)) return e->d_cmaps && (t.ty == 32 || t.ty == 64 || t.ty == 128);
+  if (e->prec == HYC_PREC_MIXED && is_col2(t))
+    return e->d_cmaps && (t.ty == 32 || t.ty == 64 || t.ty == 128 || t.ty == 256 || t.ty == 512);
   if (e->prec == HYC_PREC_MIXED && is_col(t)) return t.ty == 32 || t.ty == 64 || t.ty == 128;
   if (e->prec == HYC_PREC_MIXED) return e->use_tma ? hyc::mix_tma_shape_ok(t) : hyc::mix_shape_ok(t);
   return (t.tx == 32 && t.ty == 16) || (t.tx == 16 && t.ty == 16);
@@ -481,6 +525,7 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
     b.ld2 = s.jdm + 2 * s.nbdy;
     b.slice = (long long)b.ld1 * b.ld2;
     b.work = (long long)s.idm * s.jdm * s.kdm * s.ntr;
+    b.posdef.assign(s.ntr, 0.0);
     maxk = std::max(maxk, s.kdm);
     e->maxntr = std::max(e->maxntr, s.ntr);
     // masks (validated like hyc_adv_init) and metrics, repitched
@@ -539,7 +584,7 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
     e->shape = hyc::TileShape{hyc::kColStrip, 64};  // column-strip kernel
     if (encode_fn() && cudaMalloc(&e->d_cmaps, nbasin * 8 * sizeof(CUtensorMap)) == cudaSuccess) {
       if (encode_strip_maps(e) == HYC_OK) {
-        e->shape = hyc::TileShape{hyc::kCol2Strip, 64};  // two-column strip kernel
+        e->shape = hyc::TileShape{hyc::kCol2Strip, 128};  // two-column strip kernel
       } else {
         cudaFree(e->d_cmaps);
         e->d_cmaps = nullptr;
@@ -706,6 +751,22 @@ int hyc_ens_set_option(hyc_ens *e, int32_t option, int32_t value) {
   return efail(e, HYC_ERR_ARG, "unknown option %d", option);
 }
 
+int hyc_ens_set_posdef(hyc_ens *e, int32_t basin, int32_t tracer, double posdef) {
+  if (!e || basin < 0 || basin >= (int)e->b.size() || tracer < 0 || tracer >= e->b[basin].ntr)
+    return efail(e, HYC_ERR_ARG, "hyc_ens_set_posdef: bad basin or tracer");
+  if (e->b[basin].posdef[tracer] != posdef) {
+    Dev g(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);  // steps in flight read the tables
+    e->b[basin].posdef[tracer] = posdef;
+    e->tbl_dt2 = -1.0;
+    if (e->gexec) {
+      cudaGraphExecDestroy(e->gexec);
+      e->gexec = nullptr;
+    }
+  }
+  return HYC_OK;
+}
+
 int hyc_ens_get_option(hyc_ens *e, int32_t option, int32_t *value) {
   if (!e || !value) return efail(e, HYC_ERR_ARG, "null argument");
   switch (option) {
@@ -747,8 +808,8 @@ int hyc_ens_stats(hyc_ens *e, hyc_stats *out, int32_t reset) {
 int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32_t use_graph) {
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   if (nsteps < 1) return efail(e, HYC_ERR_ARG, "nsteps < 1");
-  if (e->prec == HYC_PREC_MIXED ? advtyp != 2 : (advtyp != 2 && advtyp != 4))
-    return efail(e, HYC_ERR_UNSUPPORTED, "ensemble advtyp %d not available for this precision", advtyp);
+  if (!scheme_ok(e, advtyp, e->shape))
+    return efail(e, HYC_ERR_UNSUPPORTED, "ensemble advtyp %d not available for this precision and tile", advtyp);
   Dev g(e->device);
   int rc;
   if ((rc = build_items(e)) || (e->use_tma && !is_strip(e->shape) && (rc = encode_maps(e))) ||
@@ -816,7 +877,8 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   Dev g(e->device);
   static const hyc::TileShape cands[] = {{32, 16}, {64, 16}, {32, 32}, {64, 8}, {128, 8}, {16, 16}, {32, 8},
-                                         {26, 32}, {26, 64}, {26, 128}, {56, 32}, {56, 64}, {56, 128}};
+                                         {26, 32}, {26, 64}, {26, 128}, {56, 32}, {56, 64}, {56, 128}, {56, 256},
+                                         {56, 512}};
   hyc::TileShape best = e->shape;
   float best_ms = 1e30f;
   const hyc::TileShape keep = e->shape;
@@ -829,7 +891,7 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
   const int keep_nq = e->strip_nq;
   std::vector<std::pair<hyc::TileShape, int>> trials;
   for (const auto &c : cands) {
-    if (!shape_ok(e, c)) continue;
+    if (!shape_ok(e, c) || !scheme_ok(e, advtyp, c)) continue;
     if (is_col2(c) && e->maxntr > 1) trials.push_back({c, 1});
     trials.push_back({c, 2});
   }

@@ -1,8 +1,8 @@
-// hyc_mixed_col2.cu -- FP32-mixed FCT2 ensemble kernel: a warp marches a
+// hyc_mixed_col2.cu -- FP32-mixed FCT2 and MPDATA ensemble kernel: a warp marches a
 // 64-column strip north through the rows, two columns per lane, with the
 // rows streamed into a per-warp shared-memory ring by TMA.
 //
-// Work item: (basin, strip, segment of rows), all layers and tracers.  The
+// Work item: (basin, strip, segment of rows, chunk of layers), all tracers.  The
 // strip starts at padded column s = 56*w (a multiple of 4, so every TMA box
 // starts on a 16-byte boundary), lane l owns columns s+2l and s+2l+1, and
 // the 56 columns s+4 .. s+59 are updated (the scheme reaches 3 cells).
@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "hyc_device.cuh"
 #include "hyc_ens.h"
@@ -41,18 +42,19 @@ namespace hyc {
 
 namespace {
 
-constexpr int kW = 64;      // staged columns per warp, two per lane
-constexpr int kRB = 4;      // rows per TMA block
+constexpr int kW = kCol2Box;  // staged columns per warp, two per lane
+constexpr int kRB = kCol2Rows;  // rows per TMA block (the box height of the host's maps)
 constexpr int kNS = 2;      // ring slots per warp
 constexpr int kWarps = 4;   // warps per CTA
 constexpr unsigned kFull = 0xffffffffu;
 
-template <int NQ, bool PREP64>
+template <int SCHEME, int NQ, bool PREP64>
 struct Ring {
+  static constexpr int NC = SCHEME == kMPDATA ? 0 : NQ;  // centre-level rows (leapfrog schemes)
   static constexpr int FROW = kW * 4;  // one FP32 row
   static constexpr int OFF_FO = 0;
   static constexpr int OFF_FC = OFF_FO + NQ * kRB * FROW;
-  static constexpr int OFF_U = OFF_FC + NQ * kRB * FROW;
+  static constexpr int OFF_U = OFF_FC + NC * kRB * FROW;
   static constexpr int OFF_V = OFF_U + kRB * FROW;
   static constexpr int OFF_DP = OFF_V + kRB * FROW;        // double per cell
   static constexpr int OFF_GE = OFF_DP + kRB * kW * 8;     // float4 per cell
@@ -126,15 +128,31 @@ struct St2 {
   float2 lx3, ly3;           // limited fluxes of row J-3
   float2 qx3, qn3;           // fqmax/fqmin at J-3
 };
+// MPDATA pipeline registers of one tracer, both columns (f-space: the
+// posdef offset enters through the mass-flux divergence only)
+struct StM {
+  float2 f1;                  // fld at J-1
+  float2 fA1, fB1, fA2, fB2;  // fld at J-1, J-2 masked for maxima (A) / minima (B)
+  float2 fx1, fy1;            // low-order x (west face) / y (south face) fluxes of row J-1, f part
+  float2 tx1, ty1;            // .5|u|(f-f_w) of row J-1 (x), .5|v|(f-f_s) of the south face of J-1
+  float2 fg2;                 // flxdiv (with posdef) of row J-2
+  float2 lo2, lo3;            // fldlo - posdef at J-2, J-3
+  float2 mx2, mn2, mx3, mn3;  // fmx/fmn - posdef at J-2, J-3
+  float2 ax2, ay2;            // antidiffusive x-flux of row J-2, y-flux of the south face of J-2
+  float2 rp3, rm3;            // ratios at J-3
+  float2 lx3, ly3;            // limited fluxes of row J-3
+};
 constexpr float kBig = 1.0e30f;   // land sentinel of the masked extrema (finite: no inf*0)
 
 }  // namespace
 
-template <int NQ, bool PREP64>
+template <int SCHEME, int NQ, bool PREP64>
 __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
-    mix_fct2_col2_kernel(const MixBasin *__restrict__ basins, const int4 *__restrict__ items, int nitems, int *head,
-                         int *err) {
-  using RG = Ring<NQ, PREP64>;
+    mix_col2_kernel(const MixBasin *__restrict__ basins, const int4 *__restrict__ items, int nitems, int *head,
+                    int *err) {
+  using RG = Ring<SCHEME, NQ, PREP64>;
+  constexpr bool MP = SCHEME == kMPDATA;
+  using St = typename std::conditional<MP, StM, St2>::type;
   extern __shared__ unsigned char c2raw_[];
   unsigned char *sm = (unsigned char *)(((uintptr_t)c2raw_ + 127) & ~(uintptr_t)127);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -162,7 +180,8 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     const int j0 = 1 + w.z * B.seg, j1 = min(j0 + B.seg, jj + 1);
     const int nblk = (j1 - j0 + 6 + kRB - 1) / kRB;
     const int nqp = (ntr + NQ - 1) / NQ;
-    const int T = kdm * nqp * nblk;
+    const int ka = w.w * B.kchunk, kb = min(kdm, ka + B.kchunk);  // this item's layers
+    const int T = (kb - ka) * nqp * nblk;
     // this lane's columns: padded a0 = s0 + 2*lane (A) and a0 + 1 (B)
     const int a0 = s0 + 2 * lane;
     const int iA = a0 - nb + 1, iB = iA + 1;  // Fortran indices
@@ -170,8 +189,9 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     const bool outB = lane >= 2 && lane < 30 && iB >= 1 && iB <= ii;
 
     auto issue = [&](int t) {  // lane 0: block t of this item into its slot
-      const int k = t / (nqp * nblk);
-      const int rem = t - k * nqp * nblk;
+      const int kk = t / (nqp * nblk);
+      const int rem = t - kk * nqp * nblk;
+      const int k = ka + kk;
       const int qp = rem / nblk, blk = rem - qp * nblk;
       const int y = j0 - 3 + blk * kRB + nb - 1;
       const uint32_t g = tg + t;
@@ -182,7 +202,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
       for (int q = 0; q < NQ; q++) {
         const int qq = min(qp * NQ + q, ntr - 1);
         tma::load3(slot + RG::OFF_FO + q * kRB * RG::FROW, B.c2_old, b, s0, y, qq * kdm + k);
-        tma::load3(slot + RG::OFF_FC + q * kRB * RG::FROW, B.c2_cur, b, s0, y, qq * kdm + k);
+        if (!MP) tma::load3(slot + RG::OFF_FC + q * kRB * RG::FROW, B.c2_cur, b, s0, y, qq * kdm + k);
       }
       tma::load3(slot + RG::OFF_U, B.c2_u, b, s0, y, k);
       tma::load3(slot + RG::OFF_V, B.c2_v, b, s0, y, k);
@@ -195,17 +215,22 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
 
     int t = 0;
     bool ok = true;
-    for (int k = 0; k < kdm && ok; k++) {
+    for (int k = ka; k < kb && ok; k++) {
       for (int qp = 0; qp < nqp && ok; qp++) {
         const int nq = min(NQ, ntr - qp * NQ);
         float *fn[NQ];
 #pragma unroll
         for (int q = 0; q < NQ; q++) fn[q] = fnew + ((long long)(qp * NQ + (q < nq ? q : 0)) * kdm + k) * sl;
-        St2 S[NQ];
+        St S[NQ];
+        float P[NQ];  // posdef of each tracer of the pass (MPDATA)
 #pragma unroll
-        for (int q = 0; q < NQ; q++) S[q] = St2{};
+        for (int q = 0; q < NQ; q++) {
+          S[q] = St{};
+          P[q] = B.posdef[min(qp * NQ + q, ntr - 1)];
+        }
         const float2 z2 = make_float2(0.f, 0.f);
         float2 u1 = z2, u1m = z2, v1 = z2, R2 = z2, nR3 = z2, QF2 = z2, DS1 = z2, DS2 = z2, DS3 = z2, QS1 = z2;
+        float2 v1m = z2, H2 = z2;  // MPDATA: masked v of row J-1, fco+fcn of row J-2
         float2 L1 = z2, L2 = z2, L3 = z2;  // land flags (1 = land) of rows J-1, J-2, J-3
         float L2e = 0.f;                   // land flag east of column B, row J-2
         double dA1 = 0.0, dB1 = 0.0, sA1 = 0.0, sB1 = 0.0;
@@ -231,11 +256,11 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
 #pragma unroll
             for (int q = 0; q < NQ; q++) {
               f0[q] = ((const float2 *)(slot + RG::OFF_FO + (q * kRB + rr) * RG::FROW))[lane];
-              c0[q] = ((const float2 *)(slot + RG::OFF_FC + (q * kRB + rr) * RG::FROW))[lane];
+              c0[q] = MP ? z2 : ((const float2 *)(slot + RG::OFF_FC + (q * kRB + rr) * RG::FROW))[lane];
             }
 
             // ---- thickness factors of row J-1 (mod_tsadvc.F90:1905-1942)
-            float2 W1, R1, QF1;
+            float2 W1, R1, QF1, Wm1, H1;  // Wm1 = W-1 and H1 = fco+fcn (MPDATA only)
             if (PREP64) {
               // continuity (:1931-1936): the face-flux differences and their sum by
               // two-sum in FP32 (exact differences, the sum rounded once relative to
@@ -255,18 +280,28 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               W1 = make_float2((float)__fma_rn(fcoA - fcnA, rA, 1.0), (float)__fma_rn(fcoB - fcnB, rB, 1.0));
               R1 = make_float2((float)rA, (float)rB);
               QF1 = mul2(fcnf, QS1);
+              if (MP) {
+                Wm1 = make_float2((float)((fcoA - fcnA) * rA), (float)((fcoB - fcnB) * rB));
+                H1 = make_float2((float)(fcoA + fcnA), (float)(fcoB + fcnB));
+              }
               sA1 = si0.x;
               sB1 = si0.y;
             } else {
               const float2 fdv = mul2(comp_div2(east(u1), u1, v0, v1), DS1);
               const float2 d = make_float2((float)dA1, (float)dB1);
               const float2 fcn = pos2(d);
-              const float2 r = make_float2(__frcp_rn(fcn.x + onemu), __frcp_rn(fcn.y + onemu));
+              const float2 r = make_float2(rcp_approx(fcn.x + onemu), rcp_approx(fcn.y + onemu));
               const float2 w1 = fma2(fdv, r, make_float2(1.f, 1.f));
               W1.x = (d.x + fdv.x > 0.f) ? (d.x >= 0.f ? w1.x : (d.x + fdv.x + onemu) * r.x) : onemu * r.x;
               W1.y = (d.y + fdv.y > 0.f) ? (d.y >= 0.f ? w1.y : (d.y + fdv.y + onemu) * r.y) : onemu * r.y;
               R1 = r;
               QF1 = mul2(fcn, QS1);
+              if (MP) {
+                const float2 wm = mul2(fdv, r);  // W-1 without the rounding of W
+                Wm1.x = (d.x + fdv.x > 0.f && d.x >= 0.f) ? wm.x : W1.x - 1.f;
+                Wm1.y = (d.y + fdv.y > 0.f && d.y >= 0.f) ? wm.y : W1.y - 1.f;
+                H1 = add2(pos2(add2(d, fdv)), fcn);
+              }
             }
             const float2 nR1 = make_float2(-R1.x, -R1.y);
             // face fluxes with the face masks applied (iu/iv = 0 faces carry no
@@ -287,10 +322,29 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
             const bool rowout = jo >= j0 && jo < j1;
             const bool stA = rowout && outA && ip3A, stB = rowout && outB && ip3B;
             const float2 nbig = make_float2(-kBig, -kBig), pbig = make_float2(kBig, kBig);
+            // MPDATA (mod_tsadvc.F90:207-493), shared by the tracers:
+            //  du1  divergence of the masked mass fluxes of row J-1 (the posdef part of
+            //       flxdiv is posdef*du1);
+            //  Z1   (W-1) - du1*R: lo = f*W - fdiv*R + posdef*Z1 is the low-order
+            //       solution with posdef taken out (Z1 = 0 when the mass fluxes at
+            //       closed faces are zero);
+            //  uD1, vD1  u/((fco2+fcn2)+onemu) of the west and south faces of row J-1
+            //       (:377-387);  ua0, va0  .5|u|, .5|v| of row J (:255, :264)
+            float2 du1, Z1, uD1, vD1, ua0, va0;
+            if (MP) {
+              du1 = mul2(comp_div2(east(u1m), u1m, v0m, v1m), DS1);
+              Z1 = fma2(du1, nR1, Wm1);
+              const float2 Hw = west(H1);
+              uD1 = make_float2(u1m.x * rcp_approx((H1.x + Hw.x) + onemu), u1m.y * rcp_approx((H1.y + Hw.y) + onemu));
+              vD1 = make_float2(v1m.x * rcp_approx((H1.x + H2.x) + onemu), v1m.y * rcp_approx((H1.y + H2.y) + onemu));
+              ua0 = mul2(make_float2(fabsf(u0m.x), fabsf(u0m.y)), half);
+              va0 = mul2(make_float2(fabsf(v0m.x), fabsf(v0m.y)), half);
+            }
 
+            if constexpr (!MP) {
 #pragma unroll
             for (int q = 0; q < NQ; q++) {
-              St2 &s = S[q];
+              St &s = S[q];
               // S1: low-order fluxes of row J (:686-720)
               const float2 fx0 = fma2(up0, west(f0[q]), mul2(un0, f0[q]));
               const float2 fy0 = fma2(vp0, s.f1, mul2(vn0, f0[q]));
@@ -382,6 +436,88 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               s.fB1 = fB0;
               s.f1 = f0[q];
             }
+            } else {
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+              St &s = S[q];
+              // P1: low-order fluxes (f part) of row J, tx/ty (:249-271), masked copies
+              const float2 f0w = west(f0[q]);
+              const float2 fx0 = fma2(up0, f0w, mul2(un0, f0[q]));
+              const float2 fy0 = fma2(vp0, s.f1, mul2(vn0, f0[q]));
+              const float2 tx0 = mul2(ua0, sub2(f0[q], f0w));
+              const float2 ty0 = mul2(va0, sub2(f0[q], s.f1));
+              const float2 fA0 = fma2(L0, nbig, f0[q]), fB0 = fma2(L0, pbig, f0[q]);
+              // P1/P2: extrema of row J-1 (:272-281) and its low-order solution (:345-353)
+              const float2 c = s.f1;
+              const float2 aw = west(s.fA1), ae = east(s.fA1), bw = west(s.fB1), be = east(s.fB1);
+              const float2 mx1 = make_float2(max3f(max3f(c.x, aw.x, ae.x), s.fA2.x, fA0.x),
+                                             max3f(max3f(c.y, aw.y, ae.y), s.fA2.y, fA0.y));
+              const float2 mn1 = make_float2(min3f(min3f(c.x, bw.x, be.x), s.fB2.x, fB0.x),
+                                             min3f(min3f(c.y, bw.y, be.y), s.fB2.y, fB0.y));
+              const float2 fdf = mul2(comp_div2(east(s.fx1), s.fx1, fy0, s.fy1), DS1);
+              const float2 Pq = make_float2(P[q], P[q]);
+              const float2 t1 = fma2(Pq, Z1, fma2(c, W1, mul2(fdf, nR1)));
+              const float2 lo1 = make_float2(fmaxf(mn1.x, fminf(mx1.x, t1.x)), fmaxf(mn1.y, fminf(mx1.y, t1.y)));
+              const float2 fg1 = fma2(Pq, du1, fdf);  // flxdiv with posdef
+              // P3: antidiffusive fluxes of the west and south faces of row J-1 (:369-392)
+              const float2 ax1 = sub2(s.tx1, mul2(uD1, add2(fg1, west(fg1))));
+              const float2 ay1 = sub2(s.ty1, mul2(vD1, add2(fg1, s.fg2)));
+              // P4: ratios of row J-2 (:405-423); ay1 is the north face of row J-2
+              const float2 axe = east(s.ax2);
+              const float2 nxw = neg2(s.ax2), nxe = neg2(axe), nys = neg2(s.ay2), nyn = neg2(ay1);
+              const float2 pxw = sub2(s.ax2, nxw), pxe = sub2(axe, nxe), pys = sub2(s.ay2, nys), pyn = sub2(ay1, nyn);
+              const float2 dp_ = add2(sub2(nxe, pxw), sub2(nyn, pys));   // flxdp + flydp
+              const float2 dn_ = add2(sub2(pxe, nxw), sub2(pyn, nys));   // flxdn + flydn
+              const float2 qpv = mul2(sub2(s.mx2, s.lo2), QF2), qmv = mul2(sub2(s.lo2, s.mn2), QF2);
+              const float2 rp2 = make_float2(qpv.x * rcp_approx(onemu - dp_.x), qpv.y * rcp_approx(onemu - dp_.y));
+              const float2 rm2 = make_float2(qmv.x * rcp_approx(onemu + dn_.x), qmv.y * rcp_approx(onemu + dn_.y));
+              // P5: limited fluxes of row J-2 (:433-449)
+              const float2 rp2w = west(rp2), rm2w = west(rm2);
+              const float2 lx2 = fma2(pxw, make_float2(min3f(1.f, rp2.x, rm2w.x), min3f(1.f, rp2.y, rm2w.y)),
+                                      mul2(nxw, make_float2(min3f(1.f, rp2w.x, rm2.x), min3f(1.f, rp2w.y, rm2.y))));
+              const float2 ly2 = fma2(pys, make_float2(min3f(1.f, rp2.x, s.rm3.x), min3f(1.f, rp2.y, s.rm3.y)),
+                                      mul2(nys, make_float2(min3f(1.f, s.rp3.x, rm2.x), min3f(1.f, s.rp3.y, rm2.y))));
+              // P6: update of row J-3 (:465-486), posdef already out
+              const float2 fd3 = mul2(comp_div2(east(s.lx3), s.lx3, ly2, s.ly3), DS3);
+              const float2 t3 = fma2(fd3, nR3, s.lo3);
+              const float resA = fmaxf(s.mn3.x, fminf(s.mx3.x, t3.x));
+              const float resB = fmaxf(s.mn3.y, fminf(s.mx3.y, t3.y));
+              if ((stA || stB) && q < nq) {
+                float *p = fn[q] + (long long)a0 + (long long)(jo + nb - 1) * ld1;
+                if (stA) p[0] = resA;
+                if (stB) p[1] = resB;
+                if (images) {
+                  if (stA && iA <= images) p[ii] = resA;
+                  if (stA && iA > ii - images) p[-ii] = resA;
+                  if (stB && iB <= images) p[1 + ii] = resB;
+                  if (stB && iB > ii - images) p[1 - ii] = resB;
+                }
+              }
+              // shift the pipeline one row
+              s.lx3 = lx2;
+              s.ly3 = ly2;
+              s.rp3 = rp2;
+              s.rm3 = rm2;
+              s.ax2 = ax1;
+              s.ay2 = ay1;
+              s.mx3 = s.mx2;
+              s.mn3 = s.mn2;
+              s.mx2 = mx1;
+              s.mn2 = mn1;
+              s.lo3 = s.lo2;
+              s.lo2 = lo1;
+              s.fg2 = fg1;
+              s.tx1 = tx0;
+              s.ty1 = ty0;
+              s.fx1 = fx0;
+              s.fy1 = fy0;
+              s.fA2 = s.fA1;
+              s.fB2 = s.fB1;
+              s.fA1 = fA0;
+              s.fB1 = fB0;
+              s.f1 = f0[q];
+            }
+            }
             // shared per-row state
             L3 = L2;
             L2 = L1;
@@ -396,6 +532,10 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
             L1 = L0;
             u1 = u0;
             u1m = u0m;
+            if (MP) {
+              v1m = v0m;
+              H2 = H1;
+            }
             v1 = v0;
             dA1 = d0.x;
             dB1 = d0.y;
@@ -441,13 +581,8 @@ cudaError_t launch_dtsi(const double *scp2i, double dt2, long long n, double *ou
   return cudaGetLastError();
 }
 
-size_t mix_col2_smem(int nq, bool prep64) {
-  if (nq >= 2) return prep64 ? Ring<2, true>::SMEM : Ring<2, false>::SMEM;
-  return prep64 ? Ring<1, true>::SMEM : Ring<1, false>::SMEM;
-}
-
-cudaError_t launch_mix_fct2_col2(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm, int nq,
-                                 bool prep64, int *err, cudaStream_t s) {
+cudaError_t launch_mix_col2(int scheme, const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm,
+                            int nq, bool prep64, int *err, cudaStream_t s) {
   auto pick = [&](auto kern, size_t smem) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -458,11 +593,17 @@ cudaError_t launch_mix_fct2_col2(const MixBasin *basins, const int4 *items, int 
     kern<<<nsm * per_sm, kWarps * 32, smem, s>>>(basins, items, nitems, head, err);
     return cudaGetLastError();
   };
-  if (nq >= 2)
-    return prep64 ? pick(mix_fct2_col2_kernel<2, true>, Ring<2, true>::SMEM)
-                  : pick(mix_fct2_col2_kernel<2, false>, Ring<2, false>::SMEM);
-  return prep64 ? pick(mix_fct2_col2_kernel<1, true>, Ring<1, true>::SMEM)
-                : pick(mix_fct2_col2_kernel<1, false>, Ring<1, false>::SMEM);
+#define HYC_COL2(S, Q, P) pick(mix_col2_kernel<S, Q, P>, Ring<S, Q, P>::SMEM)
+  if (scheme == kFCT2) {
+    if (nq >= 2) return prep64 ? HYC_COL2(kFCT2, 2, true) : HYC_COL2(kFCT2, 2, false);
+    return prep64 ? HYC_COL2(kFCT2, 1, true) : HYC_COL2(kFCT2, 1, false);
+  }
+  if (scheme == kMPDATA) {
+    if (nq >= 2) return prep64 ? HYC_COL2(kMPDATA, 2, true) : HYC_COL2(kMPDATA, 2, false);
+    return prep64 ? HYC_COL2(kMPDATA, 1, true) : HYC_COL2(kMPDATA, 1, false);
+  }
+#undef HYC_COL2
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace hyc

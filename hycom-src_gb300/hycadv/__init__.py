@@ -44,7 +44,7 @@ EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "
            "hyc_ens_destroy", "hyc_ens_set_stream", "hyc_ens_put", "hyc_ens_get",
            "hyc_ens_put_slices", "hyc_ens_get_slices", "hyc_ens_set_tile",
            "hyc_ens_tune", "hyc_ens_step", "hyc_ens_content", "hyc_ens_stats", "hyc_ens_enable_timers",
-           "hyc_ens_last_error", "hyc_ens_set_option", "hyc_ens_get_option")
+           "hyc_ens_last_error", "hyc_ens_set_option", "hyc_ens_get_option", "hyc_ens_set_posdef")
 ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
 TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4}
@@ -118,6 +118,7 @@ def lib() -> C.CDLL:
         L.hyc_ens_enable_timers.argtypes = [vp, C.c_int32]
         L.hyc_ens_set_option.argtypes = [vp, C.c_int32, C.c_int32]
         L.hyc_ens_get_option.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
+        L.hyc_ens_set_posdef.argtypes = [vp, C.c_int32, C.c_int32, C.c_double]
         L.hyc_ens_last_error.argtypes = [vp]
         L.hyc_ens_last_error.restype = C.c_char_p
         L.hyc_advem_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp,
@@ -445,6 +446,10 @@ class Ensemble(_StreamFollower):
     def set_prep64(self, on: bool):
         """Mixed form: thickness prep in FP64 (True, default) or compensated FP32."""
         self._chk(lib().hyc_ens_set_option(self._h, 1, int(bool(on))))
+
+    def set_posdef(self, b: int, q: int, posdef: float):
+        """MPDATA offset of tracer q of basin b (mod_tsadvc.F90:1755-1763)."""
+        self._chk(lib().hyc_ens_set_posdef(self._h, b, q, float(posdef)))
 
     def set_strip_tracers(self, n: int):
         """Two-column strip kernel: tracers advanced per pass (1 or 2)."""

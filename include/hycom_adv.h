@@ -276,7 +276,7 @@ int hyc_ens_get_slices(hyc_ens *ens, int32_t basin, int32_t what, int32_t s0, in
                        int32_t where);
 /* Tile shape of the step kernel; hyc_ens_tune picks one.  Mixed form:
  * tx = 56 is the two-column strip kernel (64-column strips streamed by TMA,
- * the default; ty = rows per segment, 32/64/128), tx = 26 the one-column
+ * the default; ty = rows per segment, 32/64/128/256/512), tx = 26 the one-column
  * strip kernel (ty likewise), other shapes tx x ty cell tiles. */
 int hyc_ens_set_tile(hyc_ens *ens, int32_t tx, int32_t ty);
 /*
@@ -286,7 +286,10 @@ int hyc_ens_set_tile(hyc_ens *ens, int32_t tx, int32_t ty);
  */
 int hyc_ens_tune(hyc_ens *ens, int32_t advtyp, double delt1, int32_t *tx, int32_t *ty, double *ms);
 /*
- * Advance every basin nsteps leapfrog steps (advtyp 2 = FCT2; FP64 also 4).
+ * Advance every basin nsteps leapfrog steps.  advtyp: FP64 form 0 (PCM),
+ * 1 (MPDATA), 2 (FCT2), 4 (FCT4); FP32-mixed form 2 (FCT2) with every
+ * kernel and 1 (MPDATA) with the two-column strip kernel (tx = 56).  PCM and
+ * MPDATA read only level t-1 (mod_tsadvc.F90:152, :495).
  * use_graph = 1: the nsteps launches are captured once into a CUDA graph
  * (per nsteps/advtyp/delt1/tile) and replayed.  Asynchronous.
  */
@@ -317,6 +320,12 @@ int hyc_ens_stats(hyc_ens *ens, hyc_stats *out, int32_t reset);
  * on an SM.  hyc_ens_tune tries both. */
 #define HYC_OPT_STRIP_TRACERS 3
 int hyc_ens_set_option(hyc_ens *ens, int32_t option, int32_t value);
+/*
+ * MPDATA offset of one tracer of one basin (default 0).  The reference uses
+ * 256 for temp, 32 for th3d, 1 for q2 and 0 for saln and passive tracers
+ * (mod_tsadvc.F90:1755-1763); FCT ignores it.  Synchronous.
+ */
+int hyc_ens_set_posdef(hyc_ens *ens, int32_t basin, int32_t tracer, double posdef);
 int hyc_ens_get_option(hyc_ens *ens, int32_t option, int32_t *value);
 int hyc_ens_enable_timers(hyc_ens *ens, int32_t on);
 const char *hyc_ens_last_error(const hyc_ens *ens);

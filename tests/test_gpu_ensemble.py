@@ -114,7 +114,7 @@ def test_tune_keeps_state(cuda):
     before = [get_cur(ens, i, m) for i, m in enumerate(members)]
     tx, ty, ms = ens.tune(2, DELT1)
     assert (tx, ty) in [(32, 16), (64, 16), (32, 32), (64, 8), (128, 8), (32, 8), (26, 32), (26, 64), (26, 128),
-                        (56, 32), (56, 64), (56, 128)]
+                        (56, 32), (56, 64), (56, 128), (56, 256), (56, 512)]
     assert ms > 0
     after = [get_cur(ens, i, m) for i, m in enumerate(members)]
     for a, b in zip(before, after):
@@ -273,4 +273,83 @@ def test_put_follows_torch_stream(cuda):
         out = torch.empty_like(x)
         ens.get(0, "cur", out)
         assert torch.equal(out[:, b.J, b.I], x[:, b.J, b.I])
+    ens.close()
+
+def make_ts_members(specs=SPECS[:2], delt1=DELT1):
+    """Members whose tracers are temp (posdef 256 under MPDATA) and saln."""
+    out = []
+    for nx, ny, per, kdm, ntr, seed, cour, _ in specs:
+        b = basin(nx, ny, per, seed)
+        g = oracle_grid(b)
+        c = np_case(b, g, kdm=kdm, ntracr=0, seed=seed, courant=cour, delt1=delt1)
+        trc = np.stack([c["temp"], c["saln"]])  # (2, 2, kdm, ...)
+        out.append(dict(b=b, g=g, c=c, ntr=2, kdm=kdm, trc=trc))
+    return out
+
+
+def oracle_ts_step(m, step, advtyp):
+    c = m["c"]
+    mm, nn = levels(step)
+    # hybrid layers (nhybrd = kdm, advflg = 0): temp and saln are advected (mod_tsadvc.F90:1855, :1969-1981)
+    m["g"].tsadvc(mm, nn, temp=c["temp"], saln=c["saln"], th3d=c["th3d"], uflx=c["uflx"], vflx=c["vflx"],
+                  dp=c["dp"], delt1=DELT1, advtyp=advtyp, nstep=step)
+    return np.stack([c["temp"][nn - 1], c["saln"][nn - 1]])
+
+
+@pytest.mark.parametrize("advtyp", [0, 1])
+def test_fp64_ensemble_pcm_mpdata_bitwise(cuda, advtyp):
+    """FP64 ensemble PCM and MPDATA (temp with posdef 256) equal the oracle's
+    tsadvc bit for bit over three steps, closed and periodic basins."""
+    members = make_ts_members()
+    ens = hycadv.Ensemble([spec_of(m) for m in members], precision="fp64")
+    for i in range(len(members)):
+        ens.set_posdef(i, 0, 256.0)
+    load(ens, members)
+    for step in range(1, 4):
+        ens.step(advtyp, DELT1, 1)
+        for i, m in enumerate(members):
+            want = oracle_ts_step(m, step, advtyp)
+            got = get_cur(ens, i, m)
+            ip = sea_interior(m)
+            assert same(got[..., ip], want[..., ip]), f"basin {i} step {step}"
+            mm, nn = levels(step + 1)
+            ens.put(i, "dp", np.ascontiguousarray(m["c"]["dp"][nn - 1]))
+    ens.close()
+
+
+@pytest.mark.parametrize("prep64", [True, False])
+def test_mixed_mpdata_one_step_error(cuda, prep64):
+    """One FP32-mixed MPDATA step (two-column strip kernel, posdef handled
+    outside the FP32 values) is within 1e-6 of the FP64 oracle relative to
+    each tracer's max |value|, for temp (posdef 256) and saln (posdef 0)."""
+    members = make_ts_members()
+    ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
+    ens.set_prep64(prep64)
+    for i in range(len(members)):
+        ens.set_posdef(i, 0, 256.0)
+    load(ens, members)
+    ens.step(1, DELT1, 1)
+    for i, m in enumerate(members):
+        want = oracle_ts_step(m, 1, 1)
+        got = get_cur(ens, i, m)
+        ip = sea_interior(m)
+        for q in range(2):
+            err = np.abs(got[q][..., ip] - want[q][..., ip]).max() / np.abs(want[q][..., ip]).max()
+            print(f"mpdata prep64={prep64} basin {i} tracer {q}: {err:.2e}")
+            assert err < 1e-6, (i, q, err)
+    ens.close()
+
+
+def test_mixed_mpdata_needs_strip_kernel(cuda):
+    """FP32-mixed MPDATA runs only in the two-column strip kernel; other
+    tiles refuse it, and the tuner picks a strip shape."""
+    members = make_ts_members(SPECS[:1])
+    ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
+    load(ens, members)
+    ens.set_tile(26, 32)
+    with pytest.raises(hycadv.HycError):
+        ens.step(1, DELT1, 1)
+    tx, ty, _ = ens.tune(1, DELT1)
+    assert tx == 56
+    ens.step(1, DELT1, 1)
     ens.close()
