@@ -43,6 +43,25 @@ struct TileArgs {
   int images;
 };
 
+// advem_fct2c (mod_tsadvc.F90:999-1368) over up to kMaxFields (field, layer)
+// pairs, see hyc_fct2c.cu
+struct Fct2cArgs {
+  int ii, jj, nb, ld1, ld2;
+  long long slice;
+  int mode;  // 0: fco/fcn from dp(n), uflx, vflx, onetamas (tsadvc); 1: given (advem)
+  const uint8_t *msk;
+  const double *scal, *scali;
+  const double *uflx, *vflx, *dpn, *oneta;  // mode 0: per layer k (+k*slice); oneta may be null
+  const double *fco, *fcn;                  // mode 1
+  double dt2;
+  int npair;
+  double *work;     // A_N * npair slices
+  uint8_t *lcalc;   // npair slices
+  double *fld[kMaxFields];         // level n of each pair's layer (in: t-1, out: t+1)
+  const double *fldc[kMaxFields];  // level m (t)
+  int k[kMaxFields];               // layer (0-based) of each pair
+};
+
 template <int TX, int TY>
 struct TileGeom {
   static constexpr int RX = TX + 6, RY = TY + 6, N = RX * RY;

@@ -68,6 +68,8 @@ struct hyc_ens {
   int nhead = 0;
   double *d_partial = nullptr;
   int npartial = 0;
+  double *d_stage = nullptr;  // put/get staging (reference layout, FP64), grown on demand
+  size_t stage_bytes = 0;
   // graph cache
   cudaGraphExec_t gexec = nullptr;
   int g_nsteps = 0, g_advtyp = -1, g_rot = -1, g_tx = 0, g_ty = 0;
@@ -139,6 +141,7 @@ void free_all(hyc_ens *e) {
   cudaFree(e->d_items);
   cudaFree(e->d_head);
   cudaFree(e->d_partial);
+  cudaFree(e->d_stage);
   cudaFree(e->d_tmaps);
   cudaFree(e->d_cmaps);
   cudaFree(e->d_err);
@@ -653,8 +656,14 @@ static int move(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns_
   dst = (char *)dst + (size_t)s0 * b.slice * (dfp32 ? 4 : 8);
   const long long rsl = (long long)b.ld1r * b.ld2;
   const size_t bytes = (size_t)rsl * ns * 8;
-  double *stage = nullptr;
-  ECK(cudaMallocAsync(&stage, bytes, e->stream), "staging");
+  if (e->stage_bytes < bytes) {  // the previous put/get synchronised: the old buffer is idle
+    cudaFree(e->d_stage);
+    e->d_stage = nullptr;
+    e->stage_bytes = 0;
+    ECK(cudaMalloc(&e->d_stage, bytes), "staging");
+    e->stage_bytes = bytes;
+  }
+  double *stage = e->d_stage;
   cudaError_t c;
   if (put) {
     ECK(cudaMemcpyAsync(stage, host, bytes, where == HYC_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
@@ -673,7 +682,6 @@ static int move(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns_
                           e->stream);
   }
   if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put/get: %s", cudaGetErrorString(c));
-  ECK(cudaFreeAsync(stage, e->stream), "staging free");
   ECK(cudaStreamSynchronize(e->stream), "put/get sync");
   if (put && (what == HYC_E_OLD || what == HYC_E_CUR)) e->primed = false;
   return HYC_OK;

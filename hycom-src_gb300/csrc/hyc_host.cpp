@@ -41,6 +41,8 @@ struct hyc_ctx {
   Field fields[HYC_NFIELDS];
   double *d_scratch = nullptr;  // advem output slices (fields x layers)
   size_t scratch_elems = 0;
+  unsigned char *d_fct2c = nullptr;  // advem_fct2c work arrays (per (field, layer) pair)
+  size_t fct2c_bytes = 0;
   double *d_tmp = nullptr;      // staging for host-pointer advem/xctilr (8 slices)
   long long *d_keys = nullptr;  // salinity range keys (2*kdm)
   long long *h_keys = nullptr;  // pinned
@@ -109,6 +111,33 @@ hyc::TileShape env_shape(hyc::TileShape def) {
   hyc::TileShape t{0, 0};
   if (sscanf(s, "%dx%d", &t.tx, &t.ty) == 2 && hyc::advect_tile_shape_ok(t)) return t;
   return def;
+}
+
+int ensure_fct2c(hyc_ctx *c, size_t bytes) {
+  if (c->fct2c_bytes >= bytes) return HYC_OK;
+  if (c->d_fct2c) cudaFree(c->d_fct2c);
+  c->d_fct2c = nullptr;
+  c->fct2c_bytes = 0;
+  cudaError_t e = cudaMalloc(&c->d_fct2c, bytes);
+  if (e != cudaSuccess) return fail(c, HYC_ERR_NOMEM, "cannot allocate %zu bytes of fct2c work arrays", bytes);
+  c->fct2c_bytes = bytes;
+  return HYC_OK;
+}
+
+// Pairs per advem_fct2c launch: up to kMaxFields, work arrays within ~4 GB.
+int fct2c_batch(const hyc_ctx *c) {
+  const size_t per = hyc::fct2c_work_bytes(c->slice);
+  size_t n = ((size_t)4 << 30) / (per ? per : 1);
+  if (n < 1) n = 1;
+  if (n > (size_t)hyc::kMaxFields) n = hyc::kMaxFields;
+  return (int)n;
+}
+
+void fct2c_bind(hyc::Fct2cArgs &f, const hyc_ctx *c, int npair) {
+  const size_t sl = (size_t)c->slice;
+  f.npair = npair;
+  f.work = (double *)c->d_fct2c;
+  f.lcalc = c->d_fct2c + (size_t)npair * sl * 13 * sizeof(double);
 }
 
 int ensure_scratch(hyc_ctx *c, size_t elems) {
@@ -372,6 +401,7 @@ int hyc_adv_finalize(hyc_ctx *c) {
     cudaFree(c->d_scp2);
     cudaFree(c->d_scp2i);
     cudaFree(c->d_scratch);
+    cudaFree(c->d_fct2c);
     cudaFree(c->d_tmp);
     cudaFree(c->d_keys);
     cudaFree(c->d_sum);
@@ -470,7 +500,6 @@ int hyc_advem(hyc_ctx *c, int32_t advtyp, double *fld, const double *fldc, const
               int32_t btrmas, int32_t where) {
   if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
   if (!valid_advtyp(advtyp)) return fail(c, HYC_ERR_ADVTYP, "advem called with advtyp = %d", advtyp);
-  if (advtyp == 2 && btrmas) return fail(c, HYC_ERR_UNSUPPORTED, "advem_fct2c (btrmas) not available");
   if (c->nbdy < kMbdy[advtyp]) return fail(c, HYC_ERR_NBDY, "nbdy must be at least %d", kMbdy[advtyp]);
   if (!fld || !u || !v || !fco || !fcn || !scal || !scali || (advtyp >= 2 && !fldc))
     return fail(c, HYC_ERR_ARG, "hyc_advem: null array");
@@ -492,6 +521,41 @@ int hyc_advem(hyc_ctx *c, int32_t advtyp, double *fld, const double *fldc, const
     dfcn = c->d_tmp + 5 * sl;
     dscal = c->d_tmp + 6 * sl;
     dscali = c->d_tmp + 7 * sl;
+  }
+  if (advtyp == 2 && btrmas) {  // advem_fct2c, mod_tsadvc.F90:154-155
+    int rc = ensure_fct2c(c, hyc::fct2c_work_bytes(sl));
+    if (rc) return rc;
+    hyc::Fct2cArgs f;
+    memset(&f, 0, sizeof f);
+    f.ii = c->idm;
+    f.jj = c->jdm;
+    f.nb = c->nbdy;
+    f.ld1 = c->ld1;
+    f.ld2 = c->ld2;
+    f.slice = sl;
+    f.mode = 1;
+    f.msk = c->d_msk;
+    f.scal = dscal;
+    f.scali = dscali;
+    f.uflx = du;
+    f.vflx = dv;
+    f.fco = dfco;
+    f.fcn = dfcn;
+    f.dt2 = dt2;
+    fct2c_bind(f, c, 1);
+    f.fld[0] = dfld;
+    f.fldc[0] = dfldc;
+    f.k[0] = 0;
+    int nl = 0;
+    {
+      Timed t(c, HYC_T_ADVECT);
+      CK(hyc::launch_fct2c(f, c->nreg, &nl, c->stream), "advem_fct2c");
+    }
+    c->stats.launches += nl;
+    if (where == HYC_HOST)
+      CK(cudaMemcpyAsync(fld, c->d_tmp, sl * 8, cudaMemcpyDeviceToHost, c->stream), "advem d2h");
+    CK(cudaStreamSynchronize(c->stream), "advem");
+    return HYC_OK;
   }
   int rc = ensure_scratch(c, (size_t)sl);
   if (rc) return rc;
@@ -543,7 +607,6 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
   if (c->nbdy < kMbdy[at])
     return fail(c, HYC_ERR_NBDY, "nbdy (dimensions.h) must be at least %d for advtyp %d", kMbdy[at], at);
   if (p->isopyc) return fail(c, HYC_ERR_UNSUPPORTED, "isopycnic (nhybrd=0) mode is not supported");
-  if (at == 2 && p->btrmas) return fail(c, HYC_ERR_UNSUPPORTED, "advem_fct2c (btrmas) not available");
   if (p->ntracr < 0 || (p->ntracr > 0 && !p->trcflg)) return fail(c, HYC_ERR_ARG, "ntracr/trcflg");
   const int kk = c->kdm;
   const long long sl = c->slice;
@@ -643,9 +706,52 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
   a.oneta_n = p->btrmas ? F[HYC_F_ONETA].dev + (long long)nn * sl : nullptr;
   a.dt2 = p->delt1;
   a.kdm = kk;
+  if (at == 2 && p->btrmas) {  // advem_fct2c per (field, layer), mod_tsadvc.F90:154-155
+    std::vector<std::pair<int, int>> pairs;  // (layer, field) in the reference's call order
+    for (int k = 0; k < kk; k++)
+      for (int q = 0; q < (int)fl.size(); q++)
+        if (k + 1 >= fl[q].kmin && k + 1 <= fl[q].kmax) pairs.push_back({k, q});
+    const int nb = fct2c_batch(c);
+    if ((rc = ensure_fct2c(c, (size_t)nb * hyc::fct2c_work_bytes(sl)))) return rc;
+    hyc::Fct2cArgs f;
+    memset(&f, 0, sizeof f);
+    f.ii = c->idm;
+    f.jj = c->jdm;
+    f.nb = c->nbdy;
+    f.ld1 = c->ld1;
+    f.ld2 = c->ld2;
+    f.slice = sl;
+    f.mode = 0;
+    f.msk = c->d_msk;
+    f.scal = c->d_scp2;
+    f.scali = c->d_scp2i;
+    f.uflx = F[HYC_F_UFLX].dev;
+    f.vflx = F[HYC_F_VFLX].dev;
+    f.dpn = a.dpn;
+    f.oneta = a.oneta_n;
+    f.dt2 = p->delt1;
+    for (size_t p0 = 0; p0 < pairs.size(); p0 += nb) {
+      const int np = (int)std::min(pairs.size() - p0, (size_t)nb);
+      fct2c_bind(f, c, np);
+      for (int i = 0; i < np; i++) {
+        const int k = pairs[p0 + i].first;
+        const FieldDesc &d = fl[pairs[p0 + i].second];
+        f.k[i] = k;
+        f.fld[i] = d.nbase + (long long)(k + d.k_off) * sl;
+        f.fldc[i] = d.mbase + (long long)(k + d.k_off) * sl;
+      }
+      int nl = 0;
+      {
+        Timed t(c, HYC_T_ADVECT);
+        CK(hyc::launch_fct2c(f, c->nreg, &nl, s), "advem_fct2c");
+      }
+      c->stats.launches += nl;
+    }
+    fl.clear();  // done: no tile launches below
+  }
   const int chunk = hyc::kMaxFields;
   const int nchunk0 = (int)fl.size() < chunk ? (int)fl.size() : chunk;
-  if ((rc = ensure_scratch(c, (size_t)nchunk0 * kk * sl))) return rc;
+  if (!fl.empty() && (rc = ensure_scratch(c, (size_t)nchunk0 * kk * sl))) return rc;
   a.out = c->d_scratch;
   for (size_t f0 = 0; f0 < fl.size(); f0 += chunk) {
     int nf = (int)(fl.size() - f0) < chunk ? (int)(fl.size() - f0) : chunk;

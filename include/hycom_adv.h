@@ -154,7 +154,9 @@ int hyc_tsadvc(hyc_ctx *ctx, int32_t m, int32_t n, const hyc_tsadvc_params *p, d
  * fldc (center level), u, v (mass fluxes), fco, fcn (old/new thickness),
  * posdef, scal, scali (metrics), dt2, btrmas.  All pointers are host
  * (where = HYC_HOST) or device (where = HYC_DEVICE) arrays of ld1*ld2
- * doubles.  The grid and masks are those of ctx.  Synchronous.
+ * doubles.  The grid and masks are those of ctx.  advtyp 2 with btrmas
+ * runs advem_fct2c (mod_tsadvc.F90:999-1368), as hyc_tsadvc does then for
+ * every field.  Synchronous.
  * Replaces: mod_tsadvc.F90:69 (subroutine advem).
  */
 int hyc_advem(hyc_ctx *ctx, int32_t advtyp, double *fld, const double *fldc, const double *u,

@@ -119,6 +119,53 @@ def test_advem_slice_device_pointers(cuda, advtyp):
     assert same(T[0].cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("periodic", [False, True])
+def test_advem_fct2c_slice(cuda, periodic):
+    """advem_fct2c (FCT2 with btrmas, mod_tsadvc.F90:999-1368) on one slice:
+    five sub-cycled donor-cell passes with the halo refreshed between them,
+    at a Courant number that makes cells sub-cycle; bit for bit."""
+    b = basin(77, 45, periodic, seed=131)
+    g = oracle_grid(b)
+    c = np_case(b, g, kdm=1, ntracr=0, seed=131, courant=1.4, delt1=1800.0)
+    ctx = make_ctx(b, g, 1)
+    fld = c["saln"][1, 0].copy()
+    fldc = c["saln"][0, 0].copy()
+    u, v = c["uflx"][0].copy(), c["vflx"][0].copy()
+    for a in (fld, fldc, u, v):
+        g.xctilr(a, 5, 5)
+    dpn = c["dp"][1, 0]
+    fd = np.zeros_like(dpn)
+    fd[:-1, :-1] = ((u[:-1, 1:] - u[:-1, :-1]) + (v[1:, :-1] - v[:-1, :-1])) * 1800.0 * c["scp2i"][:-1, :-1]
+    fco = np.maximum(dpn + fd, 0.0)
+    fcn = np.maximum(dpn, 0.0)
+    ref = fld.copy()
+    g.advem(2, ref, fldc, u, v, fco, fcn, 0.0, c["scp2"], c["scp2i"], 1800.0, btrmas=True)
+    got = fld.copy()
+    ctx.advem(2, got, fldc, u, v, fco, fcn, 0.0, c["scp2"], c["scp2i"], 1800.0, btrmas=True)
+    assert same(got, ref)
+    assert not np.array_equal(got, fld)
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_tsadvc_fct2c_btrmas(cuda, periodic):
+    """tsadvc with btrmas (onetamas != 1 scales the thickness, :1804-1810;
+    every field goes through advem_fct2c) bit for bit over three steps,
+    T, S and a passive tracer."""
+    b = basin(90, 60, periodic, seed=31)
+    g = oracle_grid(b)
+    c = np_case(b, g, kdm=3, ntracr=1, seed=31, courant=1.2, delt1=1800.0)
+    c["delt1"] = 1800.0
+    rng = np.random.default_rng(31)
+    c["oneta"] = 1.0 + 0.05 * rng.standard_normal((2,) + c["dp"].shape[2:])
+    t = torchify(c, cuda)
+    ctx = make_ctx(b, g, 3)
+    bind_all(ctx, t, extra=("oneta",))
+    tf = np.array([0], np.int32)
+    oracle_steps(g, c, range(1, 4), 2, trcflg=tf, btrmas=True, oneta=c["oneta"])
+    gpu_steps(ctx, t, range(1, 4), 2, ntracr=1, trcflg=tf, btrmas=True)
+    compare(c, t)
+
+
 def test_tsadvc_c0_fct2_twenty_steps(cuda):
     """257x193x10 closed basin, T and S, FCT2, dt 1800 s, Courant 0.5, 20 steps."""
     b = basin(257, 193, False, seed=7)
