@@ -530,19 +530,48 @@ def run_ensemble_workload(args, wl, dev):
     RMS error relative to the tracer's max |value|, the one-step change of
     tracer content, and the new level against the inputs' extrema.  Then
     it is timed over K steps replayed from one CUDA graph.  Tile shapes come
-    from the library's autotuner."""
+    from the library's autotuner.
+
+    Under torchrun (N ranks, one GPU each) the 96 basins of c3 are sharded
+    over the ranks (longest-processing-time order, hycadv.shard) and each
+    rank advances its own; c2's single basin is replicated.  Nothing is
+    exchanged in the data path: the timed region is bracketed by barriers,
+    its time is the max over ranks, updates are summed, error metrics are
+    the max over ranks."""
     import torch
 
     import hycadv
+    from hycadv import shard as hshard
+
+    ws, rank, local = dist_setup()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+
+    def reduce(vals, op):
+        if not dist:
+            return vals
+        t = torch.tensor(vals, dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=op)
+        return t.tolist()
 
     if args.workload == "c3":
         members = c3_members(wl)
         if args.layers:
             for m in members:
                 m["kdm"] = args.layers
+        nbasin_all = len(members)
+        if ws > 1:
+            mine = hshard.shard([m["nx"] * m["ny"] * m["kdm"] * m["ntr"] for m in members], ws)[rank]
+            members = [members[i] for i in mine]
         steps = max(args.steps, wl["steps"])
     else:
         members = [dict(nx=wl["nx"], ny=wl["ny"], kdm=args.layers or wl["kdm"], ntr=wl["ntr"], seed=wl["seed"])]
+        nbasin_all = ws
         steps = args.steps
     forms = [f for f in args.ens_forms.split(",") if f]
     if forms[0] != "fp64":
@@ -550,7 +579,8 @@ def run_ensemble_workload(args, wl, dev):
     t_start = time.perf_counter()
     geos = [member_geometry(m, wl) for m in members]
     specs = [g[2] for g in geos]
-    ups = sum(s["idm"] * s["jdm"] * s["kdm"] * s["ntr"] for s in specs)
+    ups_rank = sum(s["idm"] * s["jdm"] * s["kdm"] * s["ntr"] for s in specs)
+    ups = reduce([float(ups_rank)], dist.ReduceOp.SUM if dist else None)[0]
     peak, peak_kind = peak_hbm()
     res, refs = {}, {}
     for form in forms:
@@ -594,7 +624,15 @@ def run_ensemble_workload(args, wl, dev):
                 del new
             del buf
         torch.cuda.empty_cache()
-        names = ["temp", "saln"] + [f"passive{q - 1}" for q in range(2, ntr_max)]
+        names = ["temp", "saln"] + [f"passive{q - 1}" for q in range(2, 6 if args.workload == "c3" else ntr_max)]
+        while len(per_q) < len(names):  # every rank reports the same tracer slots
+            per_q.append({"max_rel": 0.0, "sq": 0.0, "n": 0, "cons": 0.0, "extrema_excess": 0.0})
+        if dist:
+            mx = reduce([v for a in per_q for v in (a["max_rel"], a["cons"], a["extrema_excess"])], dist.ReduceOp.MAX)
+            sm = reduce([v for a in per_q for v in (a["sq"], float(a["n"]))], dist.ReduceOp.SUM)
+            for q, a in enumerate(per_q):
+                a["max_rel"], a["cons"], a["extrema_excess"] = mx[3 * q:3 * q + 3]
+                a["sq"], a["n"] = sm[2 * q], int(sm[2 * q + 1])
         rep = {}
         for q, acc in enumerate(per_q):
             r = {"content_change_one_step": acc["cons"], "new_extrema_rel": acc["extrema_excess"]}
@@ -604,17 +642,23 @@ def run_ensemble_workload(args, wl, dev):
             rep[names[q]] = r
         ens.step(2, wl["delt1"], steps, graph=True)  # capture (and warm up)
         torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
         st = torch.cuda.current_stream(dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with ClockSampler(0) as clk:
+        with ClockSampler(local) as clk:
             e0.record(st)
             ens.step(2, wl["delt1"], steps, graph=True)
             e1.record(st)
             torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1) / steps
+        if dist:
+            dist.barrier()
+        ms = reduce([e0.elapsed_time(e1) / steps], dist.ReduceOp.MAX if dist else None)[0]
         s_t = 8 if prec == "fp64" else 4
         nbytes = sum(s["idm"] * s["jdm"] * s["kdm"] * s["ntr"] * bytes_per_update(s_t, s_t, 8, s["ntr"], s["kdm"])
                      for s in specs)
+        nbytes = reduce([nbytes], dist.ReduceOp.SUM if dist else None)[0]
         ach = nbytes / (ms / 1e3) / 1e9
         res[form] = {"value": ups / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "tile": [tx, ty],
                      "graph_steps": steps, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
@@ -629,12 +673,13 @@ def run_ensemble_workload(args, wl, dev):
     head_form = "mixed-fp32prep" if "mixed-fp32prep" in res else forms[-1]
     head = res[head_form]
     if args.workload == "c3":
-        desc = (f"c3: {len(members)} closed basins, nx 120-1500, ny 90-1100, kdm 22/32/41, 2-6 tracers (T, S, "
-                f"passive), FCT2, max Courant {wl['courant']}, delt1 {wl['delt1']} s, {steps}-step CUDA graph")
+        desc = (f"c3: {nbasin_all} closed basins, nx 120-1500, ny 90-1100, kdm 22/32/41, 2-6 tracers (T, S, "
+                f"passive), FCT2, max Courant {wl['courant']}, delt1 {wl['delt1']} s, {steps}-step CUDA graph"
+                + (f", sharded over {ws} GPUs" if ws > 1 else ""))
     else:
         desc = (f"c2: periodic-x basin {wl['nx']}x{wl['ny']}x{members[0]['kdm']}, T+S+8 passive tracers "
                 f"(log-uniform 1e-6..1e2 with fronts), FCT2, max Courant {wl['courant']}, delt1 {wl['delt1']} s")
-    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": 1, "steps": steps,
+    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": ws, "steps": steps,
             "warmup": 1, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32-mixed" if head_form != "fp64" else "f64",
             "data": "synthetic (seeded generator, HYCOM units/layout)", "impl": f"ensemble-{args.workload}",
@@ -643,7 +688,10 @@ def run_ensemble_workload(args, wl, dev):
             "roofline": {"bound": "hbm", "achieved": head["achieved_GBs"], "peak": peak, "unit": "GB/s",
                          "frac": head["frac_of_measured_hbm"], "traffic": None, "peak_kind": peak_kind},
             "clocks": head["clocks"], "wall_seconds": time.perf_counter() - t_start, "forms": res}
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
     return 0
 
 
@@ -885,7 +933,7 @@ def main():
         hbuild.build()
         if args.workload == "c4":
             return run_c4(args, wl, torch.device("cuda:0"))
-        return run_ensemble_workload(args, wl, torch.device("cuda:0"))
+        return run_ensemble_workload(args, wl, None)
     ws, rank, local = dist_setup()
     dist = None
     if ws > 1:
