@@ -34,6 +34,7 @@ UNITS = {
     "hyc_mixed_col.cu": ["-lineinfo"],
     "hyc_mixed_col2.cu": ["-lineinfo"],
     "hyc_ens_host.cpp": [],
+    "hyc_za.cpp": [],
 }
 
 

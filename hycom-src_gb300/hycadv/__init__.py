@@ -44,7 +44,8 @@ EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "
            "hyc_ens_destroy", "hyc_ens_set_stream", "hyc_ens_put", "hyc_ens_get",
            "hyc_ens_put_slices", "hyc_ens_get_slices", "hyc_ens_set_tile",
            "hyc_ens_tune", "hyc_ens_step", "hyc_ens_content", "hyc_ens_stats", "hyc_ens_enable_timers",
-           "hyc_ens_last_error", "hyc_ens_set_option", "hyc_ens_get_option", "hyc_ens_set_posdef")
+           "hyc_ens_last_error", "hyc_ens_set_option", "hyc_ens_get_option", "hyc_ens_set_posdef",
+           "hyc_za_read", "hyc_za_parse_b", "hyc_za_check")
 ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
 TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4}
@@ -119,6 +120,9 @@ def lib() -> C.CDLL:
         L.hyc_ens_set_option.argtypes = [vp, C.c_int32, C.c_int32]
         L.hyc_ens_get_option.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
         L.hyc_ens_set_posdef.argtypes = [vp, C.c_int32, C.c_int32, C.c_double]
+        L.hyc_za_read.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, ip, vp, C.c_int32, dp, dp]
+        L.hyc_za_parse_b.argtypes = [C.c_char_p, C.c_char_p, ip, ip, dp, dp]
+        L.hyc_za_check.argtypes = [C.c_double] * 4
         L.hyc_ens_last_error.argtypes = [vp]
         L.hyc_ens_last_error.restype = C.c_char_p
         L.hyc_advem_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp,

@@ -332,6 +332,36 @@ int hyc_ens_get_option(hyc_ens *ens, int32_t option, int32_t *value);
 int hyc_ens_enable_timers(hyc_ens *ens, int32_t on);
 const char *hyc_ens_last_error(const hyc_ens *ens);
 
+/* ------------------------------------------------------------------------
+ * HYCOM .a/.b field input, so that fields of a HYCOM run (restart or
+ * archive files) can feed the advection.
+ * ---------------------------------------------------------------------- */
+/*
+ * Record `record` (1-based) of a .a file -- big-endian IEEE real*4 records of
+ * idm*jdm words padded to a multiple of 4096 -- into the interior of h
+ * (reference layout (1-nbdy:idm+nbdy, 1-nbdy:jdm+nbdy), doubles, halo
+ * untouched; where = HYC_HOST or HYC_DEVICE).  With mask (reference layout,
+ * may be NULL) only points with mask != 0 are stored and enter the range,
+ * and 2^100 (data void) there is an error; without a mask every point is
+ * stored and the range leaves 2^100 out.  hmin/hmax (may be NULL) receive
+ * the range.  Synchronous.
+ * Replaces: mod_za_sm.h:700 (subroutine zaiord), :944 (zaiordd).
+ */
+int hyc_za_read(const char *path, int32_t idm, int32_t jdm, int32_t nbdy, int32_t record, const int32_t *mask,
+                double *h, int32_t where, double *hmin, double *hmax);
+/*
+ * One .b line "cfield  : ... = layer level hmin hmax": cfield (9 bytes, may
+ * be NULL) receives the first 8 characters, the rest the four numbers after
+ * '='.  Replaces the parsing in mod_restart.F90:594-603 (restart_in3d).
+ */
+int hyc_za_parse_b(const char *line, char *cfield, int32_t *layer, int32_t *level, double *hmin, double *hmax);
+/*
+ * restart_in3d's consistency test of a field against its .b line
+ * (mod_restart.F90:604-605): both ends within 1e-4 relative, else
+ * HYC_ERR_ARG.
+ */
+int hyc_za_check(double hmin_a, double hmax_a, double hmin_b, double hmax_b);
+
 /* Library build identification, e.g. "hycadv 0.1 sm_103a". */
 const char *hyc_version(void);
 

@@ -345,3 +345,28 @@ def test_error_paths(cuda):
     # a failed call leaves the context usable
     ctx.tsadvc(1, 2, delt1=100.0, advtyp=2)
     torch.cuda.synchronize()
+
+
+def test_za_read_into_device_memory(cuda, tmp_path):
+    """A .a record read straight into a device array (HYC_DEVICE) equals the
+    host read; with a mask the unmasked device points are kept."""
+    import torch
+
+    from hycadv import za
+
+    idm, jdm, nb = 61, 47, 6
+    rng = np.random.default_rng(3)
+    f = rng.normal(5.0, 2.0, (jdm, idm)).astype(np.float32).astype(np.float64)
+    a = str(tmp_path / "d.a")
+    za.write_record_file(a, [f, 2 * f], idm, jdm)
+    host = np.full((jdm + 2 * nb, idm + 2 * nb), -1.0)
+    dev = torch.full(host.shape, -1.0, dtype=torch.float64, device=cuda)
+    assert za.read_record(a, 2, idm, jdm, nb, host) == za.read_record(a, 2, idm, jdm, nb, dev)
+    assert np.array_equal(dev.cpu().numpy(), host)
+    mask = np.zeros(host.shape, np.int32)
+    mask[nb:nb + 10, nb:nb + 20] = 1
+    dev.fill_(-3.0)
+    za.read_record(a, 1, idm, jdm, nb, dev, mask=mask)
+    got = dev.cpu().numpy()
+    assert np.array_equal(got[mask != 0], f[:10, :20].ravel())
+    assert np.all(got[mask == 0] == -3.0)
