@@ -425,14 +425,25 @@ def run_e2e(args, wl, b, spec, case, form, tile, nq, dev, stream, dist):
         if nq:
             ens.set_strip_tracers(nq)
 
+    phases = {"put_ms": 0.0, "step_ms": 0.0, "get_ms": 0.0}
+
     def e2e_step():
+        t0 = time.perf_counter()
         for k in ("old", "cur", "uflx", "vflx", "dp"):
-            ens.put(0, k, host[k])
+            ens.put(0, k, host[k])  # synchronous: the host buffer is free again on return
+        t1 = time.perf_counter()
         ens.step(2, wl["delt1"], 1)
-        ens.get(0, "cur", out)
+        t2 = time.perf_counter()
+        ens.get(0, "cur", out)      # synchronous: waits for the step
+        t3 = time.perf_counter()
+        phases["put_ms"] += (t1 - t0) * 1e3
+        phases["step_ms"] += (t2 - t1) * 1e3
+        phases["get_ms"] += (t3 - t2) * 1e3
 
     e2e_step()
     torch.cuda.synchronize(dev)
+    for k in phases:
+        phases[k] = 0.0
     if dist:
         dist.barrier()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -451,6 +462,7 @@ def run_e2e(args, wl, b, spec, case, form, tile, nq, dev, stream, dist):
     ups_step = wl["nx"] * wl["ny"] * kdm * 2
     return {"value": ws * ups_step * args.e2e_steps / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "steps": args.e2e_steps, "form": form,
+            "host_ms_per_step": {k: v / args.e2e_steps for k, v in phases.items()},
             "note": "per step: hyc_ens_put of T,S (t-1, t), uflx, vflx, dp from pinned host FP64 arrays "
                     "(reference layout), hyc_ens_step, hyc_ens_get of the new T,S level"}
 

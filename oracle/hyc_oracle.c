@@ -70,6 +70,9 @@ typedef struct hyo_grid {
   unsigned char *lcalc;
   /* tsadvc work */
   double *util1, *util2, *uflux, *vflux;
+  /* second-field diffusive fluxes (mod_cb_arrays uflux2/vflux2): 0 on every
+     face a sea cell touches, as geopar.F90:833 leaves them */
+  double *uflux2, *vflux2;
   int nthreads; /* 0 = OpenMP default */
 } hyo_grid;
 
@@ -240,7 +243,7 @@ void hyo_grid_free(hyo_grid *g) {
                   g->fmx,   g->fmn,   g->flx,   g->fly,    g->fldlo,  g->fmxlo,  g->fmnlo, g->fax,
                   g->fay,   g->rp,    g->rm,    g->flxdiv, g->tx1,    g->ty1,    g->fldao, g->fldan,
                   g->uloc,  g->vloc,  g->hloc,  g->dtloc,  g->ucumdt, g->vcumdt, g->flxcum,
-                  g->flycum, g->lcalc, g->util1, g->util2, g->uflux, g->vflux};
+                  g->flycum, g->lcalc, g->util1, g->util2, g->uflux, g->vflux, g->uflux2, g->vflux2};
   for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
   free(g);
 }
@@ -348,6 +351,9 @@ hyo_grid *hyo_grid_create(int idm, int jdm, int nbdy, double *depth, const doubl
     bad |= (*work[k] == NULL);
   }
   g->lcalc = (unsigned char *)calloc(n2, 1);
+  g->uflux2 = (double *)calloc(n2, 8);
+  g->vflux2 = (double *)calloc(n2, 8);
+  bad |= !g->uflux2 || !g->vflux2;
   bad |= (g->lcalc == NULL);
   if (bad) {
     hyo_grid_free(g);
@@ -1322,3 +1328,160 @@ double hyo_xcsum(const hyo_grid *g, const double *a, const int32_t *mask) {
   free(sj);
   return s;
 }
+
+/* ------------------------------------------------------------------ */
+/* Lateral diffusion at the end of tsadvc: mod_tsadvc.F90:2138-2230,   */
+/* tsdff_2x :2262-2350, tsdff_1x :2352-2492, with the 17-term equation */
+/* of state for sigma-2 (stmt_fns.h:174-263, :496-515; EOS_17T with    */
+/* EOS_SIG2, the configuration the reference's relo builds use).       */
+/* ------------------------------------------------------------------ */
+/* stmt_fns.h:183-218 (the coefficients of the 17-term equation of state) */
+static const double c001 = 9.9984085444849347e+02, c002 = 7.3471625860981584e+00, c003 = -5.3211231792841769e-02,
+                    c004 = 3.6492439109814549e-04, c005 = 2.5880571023991390e+00, c006 = 6.7168282786692355e-03,
+                    c007 = 1.9203202055760151e-03, c008 = 1.0000000000000000e+00, c009 = 7.2815210113327091e-03,
+                    c010 = -4.4787265461983921e-05, c011 = 3.3851002965802430e-07, c012 = 1.3651202389758572e-10,
+                    c013 = 1.7632126669040377e-03, c014 = 8.8066583251206474e-06, c015 = 1.8832689434804897e-10,
+                    c016 = 5.7463776745432097e-06, c017 = 1.4716275472242334e-09, c018 = 1.1798263740430364e-02,
+                    c019 = 9.8920219266399117e-08, c020 = 4.6996642771754730e-06, c021 = 2.5862187075154352e-08,
+                    c022 = 3.2921414007960662e-12, c023 = 6.7103246285651894e-06, c024 = 2.4461698007024582e-17,
+                    c025 = 9.1534417604289062e-18;
+
+/* sigma-2 reference pressure in dbar and the pressure-folded coefficients,
+   stmt_fns.h:249-263 (constants folded in double, left to right) */
+static double eos_rpdb(void) { return 2000.e4 * 1.e-4; }
+double hyo_sig(double t, double s) {
+  const double rpdb = eos_rpdb();
+  const double c101 = c001 + (c018 - c021 * rpdb) * rpdb, c103 = c003 + (c019 - c022 * rpdb) * rpdb,
+               c105 = c005 + c020 * rpdb, c108 = c008 + c023 * rpdb, c109 = c009 - c025 * (rpdb * rpdb * rpdb),
+               c111 = c011 - c024 * (rpdb * rpdb);
+  /* stmt_fns.h:497-502 */
+  const double sn = c101 + t * (c002 + t * (c103 + t * c004)) + s * (c105 - t * c006 + s * c007);
+  const double sd = c108 + t * (c109 + t * (c010 + t * (c111 + t * c012))) +
+                    s * (c013 - t * (c014 + t * t * c015) + sqrt(mx2(0.0, s)) * (c016 + t * t * c017));
+  const double sq = 1.0 / sd;
+  return sn * sq - 1000.0;
+}
+/* stmt_fns.h:516: no inverse for the 17-term equation of state */
+static double tofsig17(double r, double s) {
+  (void)r;
+  (void)s;
+  return 99.0;
+}
+
+/* harmonc, mod_tsadvc.F90:1770-1771 */
+static inline double harmonz(double a, double b) { return 2.0 * a * b / mx2((a + b), 2.0 * 1.0e-20); }
+static inline double harmonc(double aa, double bb) { return harmonz(mx2(aa, 0.0), mx2(bb, 0.0)); }
+
+/* tsdff_1x / tsdff_2x on layer slices f1 (and f2), dp(:,:,k,n), onetamas(:,:,n) */
+static void tsdff_nx(hyo_grid *g, double *f1, double *f2, const double *dpk, const double *ota, double temdf2,
+                     double delt1, const double *aspux, const double *aspvy, const double *scuy,
+                     const double *scvx) {
+  const int ii = g->ii, jj = g->jj, ld = g->ld1;
+  const int32_t *ip = g->ip, *iu = g->iu, *iv = g->iv;
+  double *uflux = g->uflux, *vflux = g->vflux, *uflux2 = g->uflux2, *vflux2 = g->vflux2;
+  double *util1 = g->util1, *util2 = g->util2;
+  int margin = 1; /* :2270-2291 */
+#pragma omp parallel for schedule(static) num_threads(nthr(g))
+  for (int j = 1 - margin; j <= jj + margin; j++)
+    for (int i = 1 - margin; i <= ii + margin; i++) {
+      size_t c = P(g, i, j);
+      if (iu[c] != 0) {
+        double factor = temdf2 * aspux[c] * scuy[c] * harmonc(dpk[c - 1] * ota[c - 1], dpk[c] * ota[c]);
+        uflux[c] = factor * (f1[c - 1] - f1[c]);
+        if (f2) uflux2[c] = factor * (f2[c - 1] - f2[c]);
+      }
+      if (iv[c] != 0) {
+        double factor = temdf2 * aspvy[c] * scvx[c] * harmonc(dpk[c - ld] * ota[c - ld], dpk[c] * ota[c]);
+        vflux[c] = factor * (f1[c - ld] - f1[c]);
+        if (f2) vflux2[c] = factor * (f2[c - ld] - f2[c]);
+      }
+    }
+  margin = 0; /* :2329-2343 */
+#pragma omp parallel for schedule(static) num_threads(nthr(g))
+  for (int j = 1 - margin; j <= jj + margin; j++)
+    for (int i = 1 - margin; i <= ii + margin; i++) {
+      size_t c = P(g, i, j);
+      if (ip[c] != 0) {
+        double factor = -delt1 / (g->scp2[c] * mx2(dpk[c] * ota[c], 1.0e-20));
+        util1[c] = ((uflux[c + 1] - uflux[c]) + (vflux[c + ld] - vflux[c])) * factor;
+        f1[c] = f1[c] + util1[c];
+        if (f2) {
+          util2[c] = ((uflux2[c + 1] - uflux2[c]) + (vflux2[c + ld] - vflux2[c])) * factor;
+          f2[c] = f2[c] + util2[c];
+        }
+      }
+    }
+}
+
+/*
+ * The diffusion block of tsadvc(m,n) (temdf2 > 0), run after the advection
+ * (hyo_tsadvc) on the same fields; oneta (ld1,ld2,2) is onetamas(:,:,n) for
+ * diffusion (:1804-1810); aspux, aspvy, scuy, scvx are the grid's arrays.
+ * Layers beyond nhybrd (exactly isopycnal, needing theta) and mxlmy are not
+ * restated.
+ */
+int hyo_tsdff(hyo_grid *g, const hyo_tsparams *p, double temdf2, double temdfc, double thbase, int m, int n,
+              double *temp, double *saln, double *th3d, double *tracer, const double *dp, const double *oneta,
+              const double *aspux, const double *aspvy, const double *scuy, const double *scvx) {
+  const int ii = g->ii, jj = g->jj, kk = p->kdm;
+  const size_t sl = (size_t)g->ld1 * g->ld2;
+  (void)m;
+  if (n < 1 || n > 2 || kk < 1 || !oneta || !aspux || !aspvy || !scuy || !scvx) return HYO_ERR_ARG;
+  if (p->nhybrd < kk || p->mxlmy) return HYO_ERR_ARG;
+  if (!(temdf2 > 0.0)) return HYO_OK; /* :2138 */
+  const int nn = n - 1;
+  for (size_t c = 0; c < sl; c++) { /* :1812-1813, the land values of the diffusive fluxes */
+    g->uflux[c] = 0.0;
+    g->vflux[c] = 0.0;
+  }
+  const int mdf = 2; /* :2139-2152, level n of every diffused field */
+  hyo_xctilr(g, saln + (size_t)nn * kk * sl, kk, mdf, mdf);
+  hyo_xctilr(g, temp + (size_t)nn * kk * sl, kk, mdf, mdf);
+  hyo_xctilr(g, th3d + (size_t)nn * kk * sl, kk, mdf, mdf);
+  for (int ktr = 0; ktr < p->ntracr; ktr++) hyo_xctilr(g, tracer + ((size_t)ktr * 2 * kk + (size_t)nn * kk) * sl, kk, mdf, mdf);
+  const double *ota = oneta + (size_t)nn * sl;
+#define FN(a, k) ((a) + ((size_t)(k) + (size_t)nn * kk) * sl) /* (…,k,n), k 0-based */
+  for (int k = 1; k <= kk; k++) { /* :2153-2198 */
+    const int ldtemp = k <= p->nhybrd && temdfc > 0.0;
+    const int ldth3d = (k <= p->nhybrd && temdfc < 1.0) || (k == 1 && p->isopyc);
+    const double *dpk = dp + ((size_t)(k - 1) + (size_t)nn * kk) * sl;
+    if (ldtemp && ldth3d) {
+      tsdff_nx(g, FN(th3d, k - 1), FN(temp, k - 1), dpk, ota, temdf2, p->delt1, aspux, aspvy, scuy, scvx);
+      tsdff_nx(g, FN(saln, k - 1), NULL, dpk, ota, temdf2, p->delt1, aspux, aspvy, scuy, scvx);
+    } else if (ldtemp) {
+      tsdff_nx(g, FN(temp, k - 1), FN(saln, k - 1), dpk, ota, temdf2, p->delt1, aspux, aspvy, scuy, scvx);
+    } else if (ldth3d) {
+      tsdff_nx(g, FN(th3d, k - 1), FN(saln, k - 1), dpk, ota, temdf2, p->delt1, aspux, aspvy, scuy, scvx);
+    } else {
+      tsdff_nx(g, FN(saln, k - 1), NULL, dpk, ota, temdf2, p->delt1, aspux, aspvy, scuy, scvx);
+    }
+    for (int ktr = 0; ktr < p->ntracr; ktr += 2) {
+      double *t1 = tracer + ((size_t)ktr * 2 * kk + (size_t)nn * kk + (size_t)(k - 1)) * sl;
+      double *t2 = ktr + 1 < p->ntracr ? tracer + ((size_t)(ktr + 1) * 2 * kk + (size_t)nn * kk + (size_t)(k - 1)) * sl
+                                        : NULL;
+      tsdff_nx(g, t1, t2, dpk, ota, temdf2, p->delt1, aspux, aspvy, scuy, scvx);
+    }
+  }
+  for (int j = 1; j <= jj; j++) /* :2199-2229, margin 0 */
+    for (int k = 1; k <= kk; k++) {
+      const int ldtemp = k <= p->nhybrd && temdfc > 0.0;
+      const int ldth3d = (k <= p->nhybrd && temdfc < 1.0) || (k == 1 && p->isopyc);
+      double *tk = FN(temp, k - 1), *sk = FN(saln, k - 1), *hk = FN(th3d, k - 1);
+      for (int i = 1; i <= ii; i++) {
+        size_t c = P(g, i, j);
+        if (g->ip[c] == 0) continue;
+        if (ldtemp && ldth3d) {
+          double th3d_t = hyo_sig(tk[c], sk[c]) - thbase;
+          hk[c] = (1.0 - temdfc) * hk[c] + temdfc * th3d_t;
+          tk[c] = tofsig17(hk[c] + thbase, sk[c]);
+        } else if (ldtemp) {
+          hk[c] = hyo_sig(tk[c], sk[c]) - thbase;
+        } else if (ldth3d) {
+          tk[c] = tofsig17(hk[c] + thbase, sk[c]);
+        }
+      }
+    }
+#undef FN
+  return HYO_OK;
+}
+

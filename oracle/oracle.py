@@ -46,6 +46,9 @@ def lib():
         L.hyo_xctilr.argtypes = [C.c_void_p, dp, C.c_int, C.c_int, C.c_int]
         L.hyo_advem.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp, dp, C.c_double, dp, dp, C.c_double, C.c_int]
         L.hyo_tsadvc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int] + [dp] * 12
+        L.hyo_tsdff.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int] + [dp] * 10
+        L.hyo_sig.restype = C.c_double
+        L.hyo_sig.argtypes = [C.c_double, C.c_double]
         L.hyo_xcsum.restype = C.c_double
         L.hyo_xcsum.argtypes = [C.c_void_p, dp, ip]
         _lib = L
@@ -148,6 +151,27 @@ class Grid:
         if rc != 0:
             raise OracleError(f"tsadvc rc={rc}")
         return xmin, xmax
+
+    def tsdff(self, m: int, n: int, *, temp, saln, th3d, dp, oneta, aspux, aspvy, scuy, scvx, delt1, temdf2,
+              temdfc=1.0, thbase=34.0, tracer=None, advflg=0, nhybrd=None, isopyc=False, mxlmy=False):
+        """The diffusion block of tsadvc(m,n) (mod_tsadvc.F90:2138-2230),
+        in place on level n."""
+        kdm = temp.shape[1]
+        ntr = 0 if tracer is None else tracer.shape[0]
+        tf = np.zeros(max(ntr, 1), np.int32)
+        p = _TsParams(kdm=kdm, advtyp=2, advflg=advflg, btrmas=0, ntracr=ntr,
+                      nhybrd=kdm if nhybrd is None else nhybrd, isopyc=int(isopyc), hybrid=1, mxlmy=int(mxlmy),
+                      nstep=1, diagno=0, delt1=float(delt1), trcflg=_p(tf))
+        rc = lib().hyo_tsdff(self._h, C.byref(p), float(temdf2), float(temdfc), float(thbase), m, n, _p(temp),
+                             _p(saln), _p(th3d), _p(tracer), _p(dp), _p(oneta), _p(aspux), _p(aspvy), _p(scuy),
+                             _p(scvx))
+        if rc != 0:
+            raise OracleError(f"tsdff rc={rc}")
+
+
+def sig(t: float, s: float) -> float:
+    """sigma-2 of the 17-term equation of state (stmt_fns.h:497-505)."""
+    return lib().hyo_sig(float(t), float(s))
 
 
 def max_threads() -> int:
