@@ -339,10 +339,17 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
     return out
 
 
-def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, advtyp=None):
+TEMDF2 = 0.015  # diffusion velocity (m/s) of the diffusion form, a typical blkdat temdf2
+
+
+def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, advtyp=None, diffusion=False):
     """FP64 plain form through the reference-layout C ABI (hyc_tsadvc on
-    resident fields), timed over K steps after W warm-up steps."""
+    resident fields), timed over K steps after W warm-up steps.  With
+    diffusion, every step also runs the diffusion block of tsadvc
+    (hyc_tsdff, temdf2 = TEMDF2) on a uniform grid (aspux = aspvy = 1,
+    scuy = scvx = sqrt(scp2)) with oneta = 1."""
     advtyp = args.advtyp if advtyp is None else advtyp
+    import numpy as np
     import torch
 
     import hycadv
@@ -352,10 +359,19 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
     ctx.set_stream(stream)
     for k in ("temp", "saln", "th3d", "uflx", "vflx", "dp"):
         ctx.bind(k, getattr(case, k))
+    oneta = None
+    if diffusion:
+        oneta = torch.ones((2,) + tuple(case.dp.shape[-2:]), dtype=torch.float64, device=dev)
+        ctx.bind("oneta", oneta)
+        dx = np.sqrt(np.asarray(sc, dtype=np.float64))
+        one = np.ones_like(dx)
+        ctx.set_diffusion_grid(one, one, dx, dx)
 
     def step(s):
         m, n = ((s + 1) % 2) + 1, (s % 2) + 1
         ctx.tsadvc(m, n, delt1=wl["delt1"], advtyp=advtyp, nstep=s)
+        if diffusion:
+            ctx.tsdff(m, n, delt1=wl["delt1"], temdf2=TEMDF2)
 
     for s in range(1, args.warmup + 1):
         step(s)
@@ -388,7 +404,7 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
     bpu = bytes_per_update(8, 8, 8, 2, kdm)
     peak, peak_kind = peak_hbm()
     res = {"value": ws * ups_step * args.steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / args.steps,
-           "scheme": SCHEME_NAMES[advtyp],
+           "scheme": SCHEME_NAMES[advtyp] + (" + Laplacian diffusion" if diffusion else ""),
            "gpu_launches": int(st["launches"]), "clocks": clk.summary(),
            "timers_ms": {k: v for k, v in st.items() if k != "launches"}}
     if adv_calls > 0:
@@ -399,6 +415,21 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
                            "kernel": "advect_tile_kernel", "algorithmic_bytes_per_update": bpu,
                            "avg_launch_ms": adv_ms / adv_calls, "share_of_step": adv_ms / max(st["tsadvc"][0], 1e-9),
                            "traffic": profile_traffic(f"{SCHEME_NAMES[advtyp].lower()}_fp64_{args.workload}")}
+    df_ms, df_calls = st["tsdff"]
+    if df_calls > 0:
+        # diffusion alone: T and S updated per cell and layer; algorithmic
+        # bytes = read T, S, dp and write T, S, th3d (FP64) per cell and layer
+        avg_s = df_ms / df_calls / 1e3
+        bpc = 6 * 8
+        cells = wl["nx"] * wl["ny"] * kdm
+        achieved = cells * bpc / avg_s / 1e9
+        res["tsdff"] = {"value": ups_step / avg_s, "unit": UNIT, "ms_per_call": df_ms / df_calls,
+                        "share_of_step": df_ms / max(ms, 1e-9),
+                        "roofline": {"bound": "fp64-alu (hbm fraction shown)", "achieved": achieved, "peak": peak,
+                                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                                     "kernel": "tsdff_tile_kernel + tsdff_store_kernel",
+                                     "algorithmic_bytes_per_cell_layer": bpc,
+                                     "traffic": profile_traffic(f"tsdff_fp64_{args.workload}")}}
     return res
 
 
@@ -916,7 +947,7 @@ def main():
     ap.add_argument("--form", default="mixed-fp32prep", choices=sorted(ENS_FORMS),
                     help="headline form (ensemble API): FP32-mixed with FP64 thickness prep, with compensated "
                          "FP32 prep, or FP64")
-    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,fp64,mixed,mixed-fp32prep",
+    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-diff,fp64,mixed,mixed-fp32prep",
                     help="forms measured beside the headline (tsadvc[-fct4|-mpdata|-pcm] = FP64 plain through "
                          "hyc_tsadvc, FCT2 unless named)")
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -973,6 +1004,9 @@ def main():
     for f, adv in (("tsadvc-fct4", 4), ("tsadvc-mpdata", 1), ("tsadvc-pcm", 0)):
         if f in others:
             schemes[f] = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, adv)
+    if "tsadvc-diff" in others:
+        schemes["tsadvc-diff"] = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local,
+                                                 2, diffusion=True)
     ens_forms = [f for f in others if f in ENS_FORMS and f != args.form]
     if "fp64" in ens_forms:  # the reference of the error checks runs first
         ens_forms = ["fp64"] + [f for f in ens_forms if f != "fp64"]

@@ -27,6 +27,7 @@ COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
 UNITS = {
     "hyc_fp64.cu": ["-lineinfo", "-fmad=false"],
     "hyc_fct2c.cu": ["-lineinfo", "-fmad=false"],
+    "hyc_tsdff.cu": ["-lineinfo", "-fmad=false"],
     "hyc_host.cpp": [],
     "hyc_noalloc.cu": ["-lineinfo"],
     "hyc_mixed.cu": ["-lineinfo"],

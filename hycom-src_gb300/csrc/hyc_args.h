@@ -62,6 +62,23 @@ struct Fct2cArgs {
   int k[kMaxFields];               // layer (0-based) of each pair
 };
 
+// Lateral diffusion of tsadvc (mod_tsadvc.F90:2138-2230) over up to
+// kMaxFields fields of every layer, see hyc_tsdff.cu
+struct TsdffArgs {
+  int ii, jj, nb, ld1, ld2;
+  long long slice;
+  const uint8_t *msk;
+  const double *scp2, *aspux, *aspvy, *scuy, *scvx;
+  const double *oneta;  // onetamas(:,:,n) = oneta(:,:,n) (mod_tsadvc.F90:1805, :1808)
+  const double *dpn;    // dp(:,:,1,n); layer k at +k*slice
+  double temdf2, delt1, thbase;
+  int kdm, nfld;
+  double *fld[kMaxFields];  // layer 1 of level n of each field; layer k at +k*slice
+  double *out;              // new values: out + (fi*kdm + k)*slice
+  int eos_t, eos_s;         // fields whose new values give th3d (-1: none)
+  double *th3d;             // th3d(:,:,1,n) when eos_t >= 0
+};
+
 template <int TX, int TY>
 struct TileGeom {
   static constexpr int RX = TX + 6, RY = TY + 6, N = RX * RY;

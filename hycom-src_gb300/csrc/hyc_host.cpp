@@ -2,6 +2,7 @@
 // tsadvc/advem/xctilr drivers and the C ABI declared in include/hycom_adv.h.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -38,6 +39,7 @@ struct hyc_ctx {
   bool own_stream = false;
   uint8_t *d_msk = nullptr;
   double *d_scp2 = nullptr, *d_scp2i = nullptr;
+  double *d_diff = nullptr;     // aspux, aspvy, scuy, scvx (4 slices), hyc_set_diffusion_grid
   Field fields[HYC_NFIELDS];
   double *d_scratch = nullptr;  // advem output slices (fields x layers)
   size_t scratch_elems = 0;
@@ -400,6 +402,7 @@ int hyc_adv_finalize(hyc_ctx *c) {
     cudaFree(c->d_msk);
     cudaFree(c->d_scp2);
     cudaFree(c->d_scp2i);
+    cudaFree(c->d_diff);
     cudaFree(c->d_scratch);
     cudaFree(c->d_fct2c);
     cudaFree(c->d_tmp);
@@ -787,6 +790,114 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
       xmin[k] = hyc::key_to_double(c->h_keys[k]);
       xmax[k] = hyc::key_to_double(c->h_keys[kk + k]);
     }
+  }
+  return HYC_OK;
+}
+
+int hyc_set_diffusion_grid(hyc_ctx *c, const double *aspux, const double *aspvy, const double *scuy,
+                           const double *scvx) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (!aspux || !aspvy || !scuy || !scvx) return fail(c, HYC_ERR_ARG, "hyc_set_diffusion_grid: null array");
+  DeviceGuard g(c->device);
+  const size_t sl = (size_t)c->slice;
+  if (!c->d_diff) CK(cudaMalloc(&c->d_diff, 4 * sl * sizeof(double)), "malloc diffusion grid");
+  const double *src[4] = {aspux, aspvy, scuy, scvx};
+  for (int q = 0; q < 4; q++)
+    CK(cudaMemcpyAsync(c->d_diff + q * sl, src[q], sl * 8, cudaMemcpyHostToDevice, c->stream), "diffusion grid");
+  CK(cudaStreamSynchronize(c->stream), "diffusion grid sync");
+  return HYC_OK;
+}
+
+int hyc_tsdff(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, double temdf2, double temdfc,
+              double thbase) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (!p || m < 1 || m > 2 || n < 1 || n > 2) return fail(c, HYC_ERR_ARG, "hyc_tsdff: bad m/n/params");
+  if (!(temdf2 > 0.0)) return HYC_OK;  // mod_tsadvc.F90:2138
+  if (p->isopyc) return fail(c, HYC_ERR_UNSUPPORTED, "isopycnic (nhybrd=0) mode is not supported");
+  if (temdfc != 1.0)
+    return fail(c, HYC_ERR_UNSUPPORTED, "temdfc = %g: only temdfc = 1 (temperature diffusion) is supported", temdfc);
+  const int kk = c->kdm;
+  if (p->nhybrd < kk)
+    return fail(c, HYC_ERR_UNSUPPORTED, "nhybrd = %d < kdm: exactly isopycnal layers are not supported", p->nhybrd);
+  if (p->ntracr < 0) return fail(c, HYC_ERR_ARG, "ntracr");
+  if (!c->d_diff) return fail(c, HYC_ERR_FIELD, "hyc_tsdff: call hyc_set_diffusion_grid first");
+  const long long sl = c->slice;
+  Field *F = c->fields;
+  auto need = [&](int id, int64_t nel, const char *name) -> int {
+    if (!F[id].dev) return fail(c, HYC_ERR_FIELD, "field %s is not bound", name);
+    if (F[id].nelem < nel) return fail(c, HYC_ERR_FIELD, "field %s has %lld elements, needs %lld", name,
+                                       (long long)F[id].nelem, (long long)nel);
+    return HYC_OK;
+  };
+  int rc;
+  if ((rc = need(HYC_F_TEMP, 2LL * kk * sl, "temp")) || (rc = need(HYC_F_SALN, 2LL * kk * sl, "saln")) ||
+      (rc = need(HYC_F_TH3D, 2LL * kk * sl, "th3d")) || (rc = need(HYC_F_DP, 2LL * kk * sl, "dp")) ||
+      (rc = need(HYC_F_ONETA, 2LL * sl, "oneta")))
+    return rc;
+  if (p->ntracr > 0 && (rc = need(HYC_F_TRACER, 2LL * kk * sl * p->ntracr, "tracer"))) return rc;
+  if (p->mxlmy && ((rc = need(HYC_F_Q2, 2LL * (kk + 2) * sl, "q2")) || (rc = need(HYC_F_Q2L, 2LL * (kk + 2) * sl, "q2l"))))
+    return rc;
+  DeviceGuard g(c->device);
+  cudaStream_t s = c->stream;
+  const int nn = n - 1;
+  Timed t_all(c, HYC_T_TSDFF);
+  // level n of every diffused field, halo 2 (:2139-2152)
+  const int mdf = 2;
+  std::vector<std::pair<double *, int>> halos = {{F[HYC_F_SALN].dev + (long long)nn * kk * sl, kk},
+                                                 {F[HYC_F_TEMP].dev + (long long)nn * kk * sl, kk},
+                                                 {F[HYC_F_TH3D].dev + (long long)nn * kk * sl, kk}};
+  if (p->mxlmy) {
+    halos.push_back({F[HYC_F_Q2].dev + (long long)nn * (kk + 2) * sl, kk + 2});
+    halos.push_back({F[HYC_F_Q2L].dev + (long long)nn * (kk + 2) * sl, kk + 2});
+  }
+  for (int t = 0; t < p->ntracr; t++)
+    halos.push_back({F[HYC_F_TRACER].dev + ((long long)t * 2 * kk + (long long)nn * kk) * sl, kk});
+  {
+    Timed t(c, HYC_T_XCTILR);
+    for (auto &h : halos) {
+      CK(hyc::launch_xctilr(h.first, sl, h.second, c->idm, c->jdm, c->nbdy, c->ld1, mdf, mdf, c->nreg, s), "xctilr");
+      c->stats.launches += (h.second + 65534) / 65535;
+    }
+  }
+  // the diffused fields, layer 1 of level n; temp and saln first (they give th3d)
+  std::vector<double *> fl = {F[HYC_F_TEMP].dev + (long long)nn * kk * sl, F[HYC_F_SALN].dev + (long long)nn * kk * sl};
+  if (p->mxlmy) {
+    fl.push_back(F[HYC_F_Q2].dev + ((long long)nn * (kk + 2) + 1) * sl);
+    fl.push_back(F[HYC_F_Q2L].dev + ((long long)nn * (kk + 2) + 1) * sl);
+  }
+  for (int t = 0; t < p->ntracr; t++) fl.push_back(F[HYC_F_TRACER].dev + ((long long)t * 2 * kk + (long long)nn * kk) * sl);
+  const int chunk = hyc::kMaxFields;
+  const int nchunk0 = (int)fl.size() < chunk ? (int)fl.size() : chunk;
+  if ((rc = ensure_scratch(c, (size_t)nchunk0 * kk * sl))) return rc;
+  hyc::TsdffArgs a;
+  memset(&a, 0, sizeof a);
+  a.ii = c->idm;
+  a.jj = c->jdm;
+  a.nb = c->nbdy;
+  a.ld1 = c->ld1;
+  a.ld2 = c->ld2;
+  a.slice = sl;
+  a.msk = c->d_msk;
+  a.scp2 = c->d_scp2;
+  a.aspux = c->d_diff;
+  a.aspvy = c->d_diff + sl;
+  a.scuy = c->d_diff + 2 * sl;
+  a.scvx = c->d_diff + 3 * sl;
+  a.oneta = F[HYC_F_ONETA].dev + (long long)nn * sl;
+  a.dpn = F[HYC_F_DP].dev + (long long)nn * kk * sl;
+  a.temdf2 = temdf2;
+  a.delt1 = p->delt1;
+  a.thbase = thbase;
+  a.kdm = kk;
+  a.out = c->d_scratch;
+  a.th3d = F[HYC_F_TH3D].dev + (long long)nn * kk * sl;
+  for (size_t f0 = 0; f0 < fl.size(); f0 += chunk) {
+    a.nfld = (int)std::min(fl.size() - f0, (size_t)chunk);
+    for (int q = 0; q < a.nfld; q++) a.fld[q] = fl[f0 + q];
+    a.eos_t = f0 == 0 ? 0 : -1;
+    a.eos_s = f0 == 0 ? 1 : -1;
+    CK(hyc::launch_tsdff(a, s), "tsdff");
+    c->stats.launches += 2;
   }
   return HYC_OK;
 }

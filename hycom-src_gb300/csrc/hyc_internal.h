@@ -26,12 +26,17 @@ bool advect_tile_shape_ok(TileShape shape);
 // (field, layer) the launch processed.
 cudaError_t launch_copy_back(const TileArgs &a, int nlayers, cudaStream_t s);
 
-// xctilr on nlev slices (mod_xc_sm.h:1337-1428).
 struct Fct2cArgs;
 // advem_fct2c: work bytes per (field, layer) pair; the stages of one call
 size_t fct2c_work_bytes(long long slice);
 cudaError_t launch_fct2c(const Fct2cArgs &a, int nreg, int *launches, cudaStream_t s);
 
+// Lateral diffusion (tsdff_1x/tsdff_2x and the density update); the two
+// launches of one call
+struct TsdffArgs;
+cudaError_t launch_tsdff(const TsdffArgs &a, cudaStream_t s);
+
+// xctilr on nlev slices (mod_xc_sm.h:1337-1428).
 cudaError_t launch_xctilr(double *a, long long slice, int nlev, int ii, int jj, int nbdy, int ld1, int mh,
                           int nh, int nreg, cudaStream_t s);
 

@@ -45,10 +45,10 @@ EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "
            "hyc_ens_put_slices", "hyc_ens_get_slices", "hyc_ens_set_tile",
            "hyc_ens_tune", "hyc_ens_step", "hyc_ens_content", "hyc_ens_stats", "hyc_ens_enable_timers",
            "hyc_ens_last_error", "hyc_ens_set_option", "hyc_ens_get_option", "hyc_ens_set_posdef",
-           "hyc_za_read", "hyc_za_parse_b", "hyc_za_check")
+           "hyc_za_read", "hyc_za_parse_b", "hyc_za_check", "hyc_set_diffusion_grid", "hyc_tsdff")
 ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
-TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4}
+TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4, "tsdff": 5}
 
 
 class HycError(RuntimeError):
@@ -101,6 +101,9 @@ def lib() -> C.CDLL:
                                 C.c_int32]
         L.hyc_xctilr.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         L.hyc_mass_sum.argtypes = [vp, vp, vp, dp]
+        L.hyc_set_diffusion_grid.argtypes = [vp, dp, dp, dp, dp]
+        L.hyc_tsdff.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(TsadvcParams), C.c_double, C.c_double,
+                                C.c_double]
         L.hyc_enable_timers.argtypes = [vp, C.c_int32]
         L.hyc_get_stats.argtypes = [vp, C.POINTER(Stats), C.c_int32]
         L.hyc_ens_create.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(BasinSpec), C.c_int32, C.c_int32]
@@ -311,6 +314,23 @@ class Context(_StreamFollower):
             return xmin, xmax
         _check(lib().hyc_tsadvc(self._h, m, n, C.byref(p), None, None), self._h)
         return None
+
+    def set_diffusion_grid(self, aspux, aspvy, scuy, scvx):
+        """Grid arrays of the lateral diffusion (host, ld1*ld2 each)."""
+        keep = [_f64(a) for a in (aspux, aspvy, scuy, scvx)]
+        _check(lib().hyc_set_diffusion_grid(self._h, *[k[1] for k in keep]), self._h)
+
+    def tsdff(self, m: int, n: int, *, delt1: float, temdf2: float, temdfc: float = 1.0, thbase: float = 34.0,
+              ntracr: int = 0, nhybrd: int | None = None, isopyc: bool = False, mxlmy: bool = False):
+        """The diffusion block at the end of tsadvc(m,n) on the bound fields
+        (level n in place, th3d from the new temp and saln)."""
+        nh = self.kdm if nhybrd is None else nhybrd
+        tf = np.zeros(max(ntracr, 1), np.int32)
+        p = TsadvcParams(advtyp=2, advflg=0, btrmas=0, ntracr=ntracr, nhybrd=nh, isopyc=int(isopyc),
+                         hybrid=int(nh > 0), mxlmy=int(mxlmy), nstep=1, diagno=0, delt1=float(delt1),
+                         trcflg=tf.ctypes.data_as(C.POINTER(C.c_int32)))
+        self._order(self._bound.values())
+        _check(lib().hyc_tsdff(self._h, m, n, C.byref(p), float(temdf2), float(temdfc), float(thbase)), self._h)
 
     def advem(self, advtyp, fld, fldc, u, v, fco, fcn, posdef, scal, scali, dt2, btrmas=False):
         """advem on one slice; all arrays numpy (host) or all torch CUDA (device)."""

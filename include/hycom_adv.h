@@ -172,6 +172,33 @@ int hyc_advem(hyc_ctx *ctx, int32_t advtyp, double *fld, const double *fldc, con
 int hyc_xctilr(hyc_ctx *ctx, double *a, int32_t nlev, int32_t mh, int32_t nh, int32_t where);
 
 /*
+ * Grid arrays of the lateral diffusion: aspux, aspvy (aspect ratios at u
+ * and v points) and scuy, scvx (grid spacings), mod_cb_arrays.F90 names,
+ * host arrays of ld1*ld2 with valid halos.  Copied to the device and kept.
+ * Replaces the module state tsdff reads (mod_tsadvc.F90:2275-2285).
+ */
+int hyc_set_diffusion_grid(hyc_ctx *ctx, const double *aspux, const double *aspvy, const double *scuy,
+                           const double *scvx);
+
+/*
+ * The diffusion block at the end of tsadvc(m,n) (mod_tsadvc.F90:2138-2230),
+ * to be called right after hyc_tsadvc(m,n) with the same p when temdf2 > 0
+ * (temdf2 <= 0 returns at once, as the reference skips the block):
+ * halo fill of level n (width 2), Laplacian diffusion of temp and saln (and
+ * of every tracer, and of q2/q2l when p->mxlmy) in every layer with the
+ * face factors temdf2*aspux*scuy*harmonc(dp*oneta) (tsdff_1x/tsdff_2x),
+ * then th3d = sig(temp,saln) - thbase at the sea points (17-term equation
+ * of state, sigma-2).  Needs oneta bound (onetamas(:,:,n) = oneta(:,:,n)
+ * for diffusion, :1805) and hyc_set_diffusion_grid.  Supported: temdfc = 1
+ * (what blkdat.F90:1135 requires with the 17-term equation of state) and
+ * nhybrd >= kdm (no exactly isopycnal layers, which need theta); else
+ * HYC_ERR_UNSUPPORTED.  FP64, bit-identical to the oracle.  Asynchronous.
+ * Replaces: mod_tsadvc.F90:2138-2230 with its tsdff_1x/tsdff_2x.
+ */
+int hyc_tsdff(hyc_ctx *ctx, int32_t m, int32_t n, const hyc_tsadvc_params *p, double temdf2, double temdfc,
+              double thbase);
+
+/*
  * Tracer content sum over sea points of the interior,
  *   sum_{i,j} fld(i,j) * (fc(i,j) + onemu) * scp2(i,j),
  * accumulated on the device in FP64 with compensated (two-sum) partials
@@ -193,6 +220,7 @@ int hyc_mass_sum(hyc_ctx *ctx, const double *fld, const double *fc, double *sum)
 #define HYC_T_ADVECT 2 /* fused advection kernels               */
 #define HYC_T_COPY 3   /* copy of updated slices into level n   */
 #define HYC_T_DIAG 4   /* salinity range diagnostic             */
+#define HYC_T_TSDFF 5  /* lateral diffusion (hyc_tsdff)         */
 #define HYC_NTIMERS 8
 
 typedef struct hyc_stats {

@@ -1417,17 +1417,18 @@ static void tsdff_nx(hyo_grid *g, double *f1, double *f2, const double *dpk, con
  * The diffusion block of tsadvc(m,n) (temdf2 > 0), run after the advection
  * (hyo_tsadvc) on the same fields; oneta (ld1,ld2,2) is onetamas(:,:,n) for
  * diffusion (:1804-1810); aspux, aspvy, scuy, scvx are the grid's arrays.
- * Layers beyond nhybrd (exactly isopycnal, needing theta) and mxlmy are not
- * restated.
+ * Layers beyond nhybrd (exactly isopycnal, needing theta) are not restated;
+ * q2, q2l (ld1,ld2,0:kdm+1,2) are read only when mxlmy.
  */
 int hyo_tsdff(hyo_grid *g, const hyo_tsparams *p, double temdf2, double temdfc, double thbase, int m, int n,
-              double *temp, double *saln, double *th3d, double *tracer, const double *dp, const double *oneta,
+              double *temp, double *saln, double *th3d, double *tracer, double *q2, double *q2l, const double *dp,
+              const double *oneta,
               const double *aspux, const double *aspvy, const double *scuy, const double *scvx) {
   const int ii = g->ii, jj = g->jj, kk = p->kdm;
   const size_t sl = (size_t)g->ld1 * g->ld2;
   (void)m;
   if (n < 1 || n > 2 || kk < 1 || !oneta || !aspux || !aspvy || !scuy || !scvx) return HYO_ERR_ARG;
-  if (p->nhybrd < kk || p->mxlmy) return HYO_ERR_ARG;
+  if (p->nhybrd < kk || (p->mxlmy && (!q2 || !q2l))) return HYO_ERR_ARG;
   if (!(temdf2 > 0.0)) return HYO_OK; /* :2138 */
   const int nn = n - 1;
   for (size_t c = 0; c < sl; c++) { /* :1812-1813, the land values of the diffusive fluxes */
@@ -1438,6 +1439,10 @@ int hyo_tsdff(hyo_grid *g, const hyo_tsparams *p, double temdf2, double temdfc, 
   hyo_xctilr(g, saln + (size_t)nn * kk * sl, kk, mdf, mdf);
   hyo_xctilr(g, temp + (size_t)nn * kk * sl, kk, mdf, mdf);
   hyo_xctilr(g, th3d + (size_t)nn * kk * sl, kk, mdf, mdf);
+  if (p->mxlmy) {
+    hyo_xctilr(g, q2 + (size_t)nn * (kk + 2) * sl, kk + 2, mdf, mdf);
+    hyo_xctilr(g, q2l + (size_t)nn * (kk + 2) * sl, kk + 2, mdf, mdf);
+  }
   for (int ktr = 0; ktr < p->ntracr; ktr++) hyo_xctilr(g, tracer + ((size_t)ktr * 2 * kk + (size_t)nn * kk) * sl, kk, mdf, mdf);
   const double *ota = oneta + (size_t)nn * sl;
 #define FN(a, k) ((a) + ((size_t)(k) + (size_t)nn * kk) * sl) /* (…,k,n), k 0-based */
@@ -1455,6 +1460,9 @@ int hyo_tsdff(hyo_grid *g, const hyo_tsparams *p, double temdf2, double temdfc, 
     } else {
       tsdff_nx(g, FN(saln, k - 1), NULL, dpk, ota, temdf2, p->delt1, aspux, aspvy, scuy, scvx);
     }
+    if (p->mxlmy) /* q2(…,k,n), k 1-based in 0:kk+1 */
+      tsdff_nx(g, q2 + ((size_t)k + (size_t)nn * (kk + 2)) * sl, q2l + ((size_t)k + (size_t)nn * (kk + 2)) * sl, dpk,
+               ota, temdf2, p->delt1, aspux, aspvy, scuy, scvx);
     for (int ktr = 0; ktr < p->ntracr; ktr += 2) {
       double *t1 = tracer + ((size_t)ktr * 2 * kk + (size_t)nn * kk + (size_t)(k - 1)) * sl;
       double *t2 = ktr + 1 < p->ntracr ? tracer + ((size_t)(ktr + 1) * 2 * kk + (size_t)nn * kk + (size_t)(k - 1)) * sl
@@ -1485,3 +1493,151 @@ int hyo_tsdff(hyo_grid *g, const hyo_tsparams *p, double temdf2, double temdfc, 
   return HYO_OK;
 }
 
+
+/* ------------------------------------------------------------------ */
+/* Robert-Asselin time filter of the scalar fields, mod_asselin.F90:   */
+/* asselin_save :28-82 (start of the step) and asselin_filter :84-268  */
+/* (end of the step), with the 17-term equation of state for th3d.     */
+/* ------------------------------------------------------------------ */
+/*
+ * Arrays (reference layout), passed in a[HYO_A_N]:
+ *   temp, saln, th3d (ld1,ld2,kdm,2); tracer (ld1,ld2,kdm,2,ntracr);
+ *   q2, q2l (ld1,ld2,0:kdm+1,2); dp, dpo (ld1,ld2,kdm,2);
+ *   oneta, onetao (ld1,ld2,2); pbavg (ld1,ld2,3); pbot (ld1,ld2);
+ *   otemp, osaln, oth3d (ld1,ld2,kdm); otracer (ld1,ld2,kdm,ntracr);
+ *   oq2, oq2l (ld1,ld2,0:kdm+1).
+ * Entries not used by the switches may be NULL.
+ */
+enum {
+  HYO_A_TEMP, HYO_A_SALN, HYO_A_TH3D, HYO_A_TRACER, HYO_A_Q2, HYO_A_Q2L, HYO_A_DP, HYO_A_DPO, HYO_A_ONETA,
+  HYO_A_ONETAO, HYO_A_PBAVG, HYO_A_PBOT, HYO_A_OTEMP, HYO_A_OSALN, HYO_A_OTH3D, HYO_A_OTRACER, HYO_A_OQ2,
+  HYO_A_OQ2L, HYO_A_N
+};
+
+/* asselin_save(m,n): oneta and onetao of both levels from pbavg/pbot at sea
+   points, level n of every scalar into the t-1 copies (all interior points),
+   then the halo of oneta/onetao (:45-80). */
+int hyo_asselin_save(hyo_grid *g, const hyo_tsparams *p, double oneta0, int m, int n, double *const *a) {
+  const int ii = g->ii, jj = g->jj, kk = p->kdm;
+  const size_t sl = (size_t)g->ld1 * g->ld2;
+  if (m < 1 || m > 2 || n < 1 || n > 2 || kk < 1) return HYO_ERR_ARG;
+  if (!a[HYO_A_TEMP] || !a[HYO_A_SALN] || !a[HYO_A_TH3D] || !a[HYO_A_ONETA] || !a[HYO_A_ONETAO] ||
+      !a[HYO_A_PBAVG] || !a[HYO_A_PBOT] || !a[HYO_A_OTEMP] || !a[HYO_A_OSALN] || !a[HYO_A_OTH3D] ||
+      (p->ntracr > 0 && (!a[HYO_A_TRACER] || !a[HYO_A_OTRACER])) ||
+      (p->mxlmy && (!a[HYO_A_Q2] || !a[HYO_A_Q2L] || !a[HYO_A_OQ2] || !a[HYO_A_OQ2L])))
+    return HYO_ERR_ARG;
+  const int mm = m - 1, nn = n - 1;
+  double *oneta = a[HYO_A_ONETA], *onetao = a[HYO_A_ONETAO];
+  const double *pbavg = a[HYO_A_PBAVG], *pbot = a[HYO_A_PBOT];
+#pragma omp parallel for schedule(static) num_threads(nthr(g))
+  for (int j = 1; j <= jj; j++) {
+    for (int i = 1; i <= ii; i++) {
+      size_t c = P(g, i, j);
+      if (g->ip[c] != 0) {
+        oneta[c + nn * sl] = mx2(oneta0, 1.0 + pbavg[c + nn * sl] / pbot[c]);
+        oneta[c + mm * sl] = mx2(oneta0, 1.0 + pbavg[c + mm * sl] / pbot[c]);
+        onetao[c + nn * sl] = oneta[c + nn * sl];
+        onetao[c + mm * sl] = oneta[c + mm * sl];
+      }
+    }
+    for (int k = 0; k < kk; k++)
+      for (int i = 1; i <= ii; i++) {
+        size_t c = P(g, i, j), lk = (size_t)k * sl, ln = ((size_t)k + (size_t)nn * kk) * sl;
+        a[HYO_A_OTEMP][lk + c] = a[HYO_A_TEMP][ln + c];
+        a[HYO_A_OSALN][lk + c] = a[HYO_A_SALN][ln + c];
+        a[HYO_A_OTH3D][lk + c] = a[HYO_A_TH3D][ln + c];
+        for (int t = 0; t < p->ntracr; t++)
+          a[HYO_A_OTRACER][((size_t)t * kk) * sl + lk + c] = a[HYO_A_TRACER][((size_t)t * 2 * kk) * sl + ln + c];
+      }
+    if (p->mxlmy)
+      for (int k = 1; k <= kk; k++)
+        for (int i = 1; i <= ii; i++) {
+          size_t c = P(g, i, j);
+          a[HYO_A_OQ2][(size_t)k * sl + c] = a[HYO_A_Q2][((size_t)k + (size_t)nn * (kk + 2)) * sl + c];
+          a[HYO_A_OQ2L][(size_t)k * sl + c] = a[HYO_A_Q2L][((size_t)k + (size_t)nn * (kk + 2)) * sl + c];
+        }
+  }
+  hyo_xctilr(g, oneta, 2, 6, 6);
+  hyo_xctilr(g, onetao, 2, 6, 6);
+  return HYO_OK;
+}
+
+/* one scalar of asselin_filter, the version that conserves a constant field
+   (:147-155): returns the filtered level-m value */
+static inline double ra_scalar(double fo, double fm, double fn, double dpold, double dpmid, double dpnew,
+                               double ra2fac, double qdpmidn) {
+  const double smin = mn3(fo, fm, fn);
+  const double dpsold = dpold * (fo - smin), dpsmid = dpmid * (fm - smin), dpsnew = dpnew * (fn - smin);
+  const double q = 0.5 * ra2fac * (dpsold + dpsnew - 2.0 * dpsmid);
+  return smin + (dpsmid + q) * qdpmidn;
+}
+
+/* asselin_filter(m,n) for hybrid layers advecting temperature (advflg=0,
+   nhybrd >= kdm: the 17-term equation of state has no tofsig, so the th3d
+   branch and the exactly isopycnal layers are not restated). */
+int hyo_asselin_filter(hyo_grid *g, const hyo_tsparams *p, double ra2fac, double oneta0, double thbase, int m, int n,
+                       double *const *a) {
+  const int ii = g->ii, jj = g->jj, kk = p->kdm;
+  const size_t sl = (size_t)g->ld1 * g->ld2;
+  if (m < 1 || m > 2 || n < 1 || n > 2 || kk < 1) return HYO_ERR_ARG;
+  if (p->advflg != 0 || p->nhybrd < kk || p->isopyc) return HYO_ERR_ARG;
+  if (!a[HYO_A_TEMP] || !a[HYO_A_SALN] || !a[HYO_A_TH3D] || !a[HYO_A_DP] || !a[HYO_A_DPO] || !a[HYO_A_ONETA] ||
+      !a[HYO_A_ONETAO] || !a[HYO_A_PBAVG] || !a[HYO_A_PBOT] || !a[HYO_A_OTEMP] || !a[HYO_A_OSALN] ||
+      (p->ntracr > 0 && (!a[HYO_A_TRACER] || !a[HYO_A_OTRACER])) ||
+      (p->mxlmy && (!a[HYO_A_Q2] || !a[HYO_A_Q2L] || !a[HYO_A_OQ2] || !a[HYO_A_OQ2L])))
+    return HYO_ERR_ARG;
+  const double onezm = 9806.e-20; /* :95 */
+  const int mm = m - 1, nn = n - 1;
+  double *oneta = a[HYO_A_ONETA];
+  const double *onetao = a[HYO_A_ONETAO], *pbavg = a[HYO_A_PBAVG], *pbot = a[HYO_A_PBOT];
+  double *dp = a[HYO_A_DP];
+  const double *dpo = a[HYO_A_DPO];
+#pragma omp parallel for schedule(static) num_threads(nthr(g))
+  for (int j = 1; j <= jj; j++) {
+    for (int i = 1; i <= ii; i++) { /* :112-117 */
+      size_t c = P(g, i, j);
+      if (g->ip[c] != 0) {
+        oneta[c + nn * sl] = mx2(oneta0, 1.0 + pbavg[c + nn * sl] / pbot[c]);
+        oneta[c + mm * sl] = mx2(oneta0, 1.0 + pbavg[c + mm * sl] / pbot[c]);
+      }
+    }
+    for (int k = 0; k < kk; k++)
+      for (int i = 1; i <= ii; i++) {
+        size_t c = P(g, i, j);
+        if (g->ip[c] == 0) continue;
+        const size_t lk = (size_t)k * sl, lm = ((size_t)k + (size_t)mm * kk) * sl,
+                     ln = ((size_t)k + (size_t)nn * kk) * sl;
+        const double dpold = dpo[ln + c] * onetao[c + nn * sl]; /* :128-135 */
+        const double dpmid = dpo[lm + c] * onetao[c + mm * sl];
+        const double dpnew = dp[ln + c] * oneta[c + nn * sl];
+        const double q = 0.5 * ra2fac * (dpold + dpnew - 2.0 * dpmid);
+        const double dpmidn = dpmid + q;
+        dp[lm + c] = dpmidn / oneta[c + mm * sl];
+        if (!(dpmidn > onezm)) continue;
+        const double qdpmidn = 1.0 / dpmidn;
+        double *s = a[HYO_A_SALN], *t = a[HYO_A_TEMP];
+        s[lm + c] = ra_scalar(a[HYO_A_OSALN][lk + c], s[lm + c], s[ln + c], dpold, dpmid, dpnew, ra2fac, qdpmidn);
+        t[lm + c] = ra_scalar(a[HYO_A_OTEMP][lk + c], t[lm + c], t[ln + c], dpold, dpmid, dpnew, ra2fac, qdpmidn);
+        a[HYO_A_TH3D][lm + c] = hyo_sig(t[lm + c], s[lm + c]) - thbase; /* :175-176 */
+        for (int tr = 0; tr < p->ntracr; tr++) { /* :189-221 */
+          double *f = a[HYO_A_TRACER] + (size_t)tr * 2 * kk * sl;
+          const double *fo = a[HYO_A_OTRACER] + (size_t)tr * kk * sl;
+          f[lm + c] = ra_scalar(fo[lk + c], f[lm + c], f[ln + c], dpold, dpmid, dpnew, ra2fac, qdpmidn);
+        }
+        if (p->mxlmy) { /* :222-233, q2(…,k,·) with k 1-based in 0:kk+1 */
+          const size_t qm = ((size_t)(k + 1) + (size_t)mm * (kk + 2)) * sl,
+                       qn = ((size_t)(k + 1) + (size_t)nn * (kk + 2)) * sl, qo = (size_t)(k + 1) * sl;
+          double *q2 = a[HYO_A_Q2], *q2l = a[HYO_A_Q2L];
+          double so = dpold * a[HYO_A_OQ2][qo + c], sm = dpmid * q2[qm + c], sn = dpnew * q2[qn + c];
+          double qq = 0.5 * ra2fac * (so + sn - 2.0 * sm);
+          q2[qm + c] = (sm + qq) * qdpmidn;
+          so = dpold * a[HYO_A_OQ2L][qo + c];
+          sm = dpmid * q2l[qm + c];
+          sn = dpnew * q2l[qn + c];
+          qq = 0.5 * ra2fac * (so + sn - 2.0 * sm);
+          q2l[qm + c] = (sm + qq) * qdpmidn;
+        }
+      }
+  }
+  return HYO_OK;
+}

@@ -46,7 +46,10 @@ def lib():
         L.hyo_xctilr.argtypes = [C.c_void_p, dp, C.c_int, C.c_int, C.c_int]
         L.hyo_advem.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp, dp, C.c_double, dp, dp, C.c_double, C.c_int]
         L.hyo_tsadvc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int] + [dp] * 12
-        L.hyo_tsdff.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int] + [dp] * 10
+        L.hyo_tsdff.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int] + [dp] * 12
+        L.hyo_asselin_save.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_void_p]
+        L.hyo_asselin_filter.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int,
+                                         C.c_int, C.c_void_p]
         L.hyo_sig.restype = C.c_double
         L.hyo_sig.argtypes = [C.c_double, C.c_double]
         L.hyo_xcsum.restype = C.c_double
@@ -152,10 +155,39 @@ class Grid:
             raise OracleError(f"tsadvc rc={rc}")
         return xmin, xmax
 
+    def _assel_params(self, kdm, ntracr, mxlmy, nhybrd=None, advflg=0, isopyc=False):
+        tf = np.zeros(max(ntracr, 1), np.int32)
+        p = _TsParams(kdm=kdm, advtyp=2, advflg=advflg, btrmas=0, ntracr=ntracr,
+                      nhybrd=kdm if nhybrd is None else nhybrd, isopyc=int(isopyc), hybrid=1, mxlmy=int(mxlmy),
+                      nstep=1, diagno=0, delt1=0.0, trcflg=_p(tf))
+        return p, tf
+
+    def asselin_save(self, m: int, n: int, arrays: dict, *, oneta0: float):
+        """asselin_save(m,n) (mod_asselin.F90:28-82) on the arrays named as in
+        ASSELIN_ARRAYS (numpy, reference layout)."""
+        kdm = arrays["temp"].shape[1]
+        ntr = 0 if arrays.get("tracer") is None else arrays["tracer"].shape[0]
+        p, tf = self._assel_params(kdm, ntr, arrays.get("q2") is not None)
+        rc = lib().hyo_asselin_save(self._h, C.byref(p), float(oneta0), m, n, _assel_ptrs(arrays))
+        if rc != 0:
+            raise OracleError(f"asselin_save rc={rc}")
+
+    def asselin_filter(self, m: int, n: int, arrays: dict, *, ra2fac: float, oneta0: float, thbase: float = 34.0,
+                       nhybrd=None, advflg=0):
+        """asselin_filter(m,n) (mod_asselin.F90:84-268), advflg=0 hybrid layers."""
+        kdm = arrays["temp"].shape[1]
+        ntr = 0 if arrays.get("tracer") is None else arrays["tracer"].shape[0]
+        p, tf = self._assel_params(kdm, ntr, arrays.get("q2") is not None, nhybrd, advflg)
+        rc = lib().hyo_asselin_filter(self._h, C.byref(p), float(ra2fac), float(oneta0), float(thbase), m, n,
+                                      _assel_ptrs(arrays))
+        if rc != 0:
+            raise OracleError(f"asselin_filter rc={rc}")
+
     def tsdff(self, m: int, n: int, *, temp, saln, th3d, dp, oneta, aspux, aspvy, scuy, scvx, delt1, temdf2,
-              temdfc=1.0, thbase=34.0, tracer=None, advflg=0, nhybrd=None, isopyc=False, mxlmy=False):
+              temdfc=1.0, thbase=34.0, tracer=None, q2=None, q2l=None, advflg=0, nhybrd=None, isopyc=False):
         """The diffusion block of tsadvc(m,n) (mod_tsadvc.F90:2138-2230),
-        in place on level n."""
+        in place on level n; q2/q2l (2, kdm+2, ld2, ld1) given = mxlmy."""
+        mxlmy = q2 is not None
         kdm = temp.shape[1]
         ntr = 0 if tracer is None else tracer.shape[0]
         tf = np.zeros(max(ntr, 1), np.int32)
@@ -163,10 +195,27 @@ class Grid:
                       nhybrd=kdm if nhybrd is None else nhybrd, isopyc=int(isopyc), hybrid=1, mxlmy=int(mxlmy),
                       nstep=1, diagno=0, delt1=float(delt1), trcflg=_p(tf))
         rc = lib().hyo_tsdff(self._h, C.byref(p), float(temdf2), float(temdfc), float(thbase), m, n, _p(temp),
-                             _p(saln), _p(th3d), _p(tracer), _p(dp), _p(oneta), _p(aspux), _p(aspvy), _p(scuy),
+                             _p(saln), _p(th3d), _p(tracer), _p(q2), _p(q2l), _p(dp), _p(oneta), _p(aspux), _p(aspvy), _p(scuy),
                              _p(scvx))
         if rc != 0:
             raise OracleError(f"tsdff rc={rc}")
+
+
+ASSELIN_ARRAYS = ("temp", "saln", "th3d", "tracer", "q2", "q2l", "dp", "dpo", "oneta", "onetao", "pbavg", "pbot",
+                  "otemp", "osaln", "oth3d", "otracer", "oq2", "oq2l")
+
+
+def _assel_ptrs(arrs: dict):
+    for k, v in arrs.items():
+        if k not in ASSELIN_ARRAYS:
+            raise KeyError(k)
+        if v is not None and not (v.flags["C_CONTIGUOUS"] and v.dtype == np.float64):
+            raise OracleError(f"{k}: need C-contiguous float64")
+    ptrs = (C.c_void_p * len(ASSELIN_ARRAYS))()
+    for i, k in enumerate(ASSELIN_ARRAYS):
+        v = arrs.get(k)
+        ptrs[i] = None if v is None else v.ctypes.data
+    return ptrs
 
 
 def sig(t: float, s: float) -> float:

@@ -50,3 +50,28 @@ def max_rel(a, b, mask=None):
         b = b[..., mask]
     den = max(np.abs(b).max(), 1e-300)
     return float(np.abs(a - b).max() / den)
+
+
+def noise(b, rng, shape):
+    """Gaussian noise, periodic in i on a periodic basin (the halo columns copy
+    the interior ones, as a halo refresh would leave them)."""
+    a = rng.standard_normal(shape)
+    if b.periodic:
+        cols = (np.arange(b.ld1) - b.nbdy) % b.nx + b.nbdy
+        a = a[..., cols]
+    return a
+
+
+def diff_grid(b, seed):
+    """Diffusion metrics aspux, aspvy, scuy, scvx of a 10 km grid, perturbed so
+    every factor matters."""
+    rng = np.random.default_rng(seed)
+    shape = (b.ld2, b.ld1)
+    one = lambda a: np.ascontiguousarray(1.0 + a * noise(b, rng, shape))
+    return dict(aspux=one(0.05), aspvy=one(0.05), scuy=1.0e4 * one(0.02), scvx=1.0e4 * one(0.02))
+
+
+def oneta_field(b, seed):
+    """oneta(ld1,ld2,2) = 1 + pbavg/pbot, a few percent from 1."""
+    rng = np.random.default_rng(seed + 1)
+    return np.ascontiguousarray(1.0 + 0.02 * noise(b, rng, (2, b.ld2, b.ld1)))

@@ -4,34 +4,15 @@ state): known answers and invariants."""
 import numpy as np
 import pytest
 
-from helpers import basin, np_case, oracle_grid
+from helpers import basin, diff_grid, np_case, oneta_field, oracle_grid
 from oracle import oracle as O
-
-
-def noise(b, rng, shape):
-    """Gaussian noise, periodic in i on a periodic basin (the halo columns copy
-    the interior ones, as a halo refresh would leave them)."""
-    a = rng.standard_normal(shape)
-    if b.periodic:
-        cols = (np.arange(b.ld1) - b.nbdy) % b.nx + b.nbdy
-        a = a[..., cols]
-    return a
-
-
-def diff_grid(b, seed):
-    """Diffusion metrics of a 10 km grid, perturbed so every factor matters."""
-    rng = np.random.default_rng(seed)
-    shape = (b.ld2, b.ld1)
-    one = lambda a: np.ascontiguousarray(1.0 + a * noise(b, rng, shape))
-    return dict(aspux=one(0.05), aspvy=one(0.05), scuy=1.0e4 * one(0.02), scvx=1.0e4 * one(0.02))
 
 
 def setup(periodic, seed, kdm=3, ntracr=3):
     b = basin(64, 48, periodic, seed)
     g = oracle_grid(b, threads=1)
     c = np_case(b, g, kdm=kdm, ntracr=ntracr, seed=seed, courant=0.5, delt1=1800.0)
-    rng = np.random.default_rng(seed + 1)
-    c["oneta"] = np.ascontiguousarray(1.0 + 0.02 * noise(b, rng, (2, b.ld2, b.ld1)))
+    c["oneta"] = oneta_field(b, seed)
     return b, g, c, diff_grid(b, seed)
 
 
