@@ -339,15 +339,18 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
     return out
 
 
-TEMDF2 = 0.015  # diffusion velocity (m/s) of the diffusion form, a typical blkdat temdf2
+TEMDF2 = 0.015  # diffusion velocity (m/s) of the full form, a typical blkdat temdf2
+RA2FAC = 0.125  # Robert-Asselin weight of the full form (blkdat ra2fac)
+ONETA0 = 0.1    # minimum 1+eta (blkdat oneta0)
 
 
-def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, advtyp=None, diffusion=False):
+def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, advtyp=None, full=False):
     """FP64 plain form through the reference-layout C ABI (hyc_tsadvc on
-    resident fields), timed over K steps after W warm-up steps.  With
-    diffusion, every step also runs the diffusion block of tsadvc
-    (hyc_tsdff, temdf2 = TEMDF2) on a uniform grid (aspux = aspvy = 1,
-    scuy = scvx = sqrt(scp2)) with oneta = 1."""
+    resident fields), timed over K steps after W warm-up steps.  With full,
+    every step is the tracer part of a HYCOM step: asselin_save, tsadvc, its
+    diffusion block (hyc_tsdff, temdf2 = TEMDF2, on a uniform grid: aspux =
+    aspvy = 1, scuy = scvx = sqrt(scp2)) and asselin_filter (ra2fac =
+    RA2FAC; dpo = the initial dp, pbot = 4e7 Pa, pbavg = 0, so oneta = 1)."""
     advtyp = args.advtyp if advtyp is None else advtyp
     import numpy as np
     import torch
@@ -359,19 +362,29 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
     ctx.set_stream(stream)
     for k in ("temp", "saln", "th3d", "uflx", "vflx", "dp"):
         ctx.bind(k, getattr(case, k))
-    oneta = None
-    if diffusion:
-        oneta = torch.ones((2,) + tuple(case.dp.shape[-2:]), dtype=torch.float64, device=dev)
-        ctx.bind("oneta", oneta)
+    keep = []
+    if full:
+        sh2 = tuple(case.dp.shape[-2:])
+        f64 = dict(dtype=torch.float64, device=dev)
+        extra = {"oneta": torch.ones((2,) + sh2, **f64), "onetao": torch.ones((2,) + sh2, **f64),
+                 "pbavg": torch.zeros((3,) + sh2, **f64), "pbot": torch.full(sh2, 4.0e7, **f64),
+                 "dpo": case.dp.clone(), "otemp": torch.empty_like(case.temp[0]),
+                 "osaln": torch.empty_like(case.saln[0]), "oth3d": torch.empty_like(case.th3d[0])}
+        for k, v in extra.items():
+            ctx.bind(k, v)
+        keep.append(extra)
         dx = np.sqrt(np.asarray(sc, dtype=np.float64))
         one = np.ones_like(dx)
         ctx.set_diffusion_grid(one, one, dx, dx)
 
     def step(s):
         m, n = ((s + 1) % 2) + 1, (s % 2) + 1
+        if full:
+            ctx.asselin_save(m, n, oneta0=ONETA0)
         ctx.tsadvc(m, n, delt1=wl["delt1"], advtyp=advtyp, nstep=s)
-        if diffusion:
+        if full:
             ctx.tsdff(m, n, delt1=wl["delt1"], temdf2=TEMDF2)
+            ctx.asselin_filter(m, n, ra2fac=RA2FAC, oneta0=ONETA0)
 
     for s in range(1, args.warmup + 1):
         step(s)
@@ -404,7 +417,7 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
     bpu = bytes_per_update(8, 8, 8, 2, kdm)
     peak, peak_kind = peak_hbm()
     res = {"value": ws * ups_step * args.steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / args.steps,
-           "scheme": SCHEME_NAMES[advtyp] + (" + Laplacian diffusion" if diffusion else ""),
+           "scheme": SCHEME_NAMES[advtyp] + (" + Laplacian diffusion + Robert-Asselin filter" if full else ""),
            "gpu_launches": int(st["launches"]), "clocks": clk.summary(),
            "timers_ms": {k: v for k, v in st.items() if k != "launches"}}
     if adv_calls > 0:
@@ -430,6 +443,24 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
                                      "kernel": "tsdff_tile_kernel + tsdff_store_kernel",
                                      "algorithmic_bytes_per_cell_layer": bpc,
                                      "traffic": profile_traffic(f"tsdff_fp64_{args.workload}")}}
+    ra_ms, ra_calls = st["asselin"]
+    if ra_calls > 0:
+        # save + filter per step: cell-layer updates of T and S; algorithmic
+        # bytes per cell and layer: save reads T, S, th3d (n) and writes the
+        # three copies; filter reads dpo (2), dp (n, m), the copies of T, S
+        # and T, S at both levels, writes dp, T, S, th3d (m)
+        bpc = 8 * (6 + 13)
+        cells = wl["nx"] * wl["ny"] * kdm
+        avg_s = ra_ms / ra_calls * 2 / 1e3
+        achieved = cells * bpc / avg_s / 1e9
+        res["asselin"] = {"value": ups_step / avg_s, "unit": UNIT, "ms_per_step": ra_ms / ra_calls * 2,
+                          "share_of_step": ra_ms / max(ms, 1e-9),
+                          "roofline": {"bound": "fp64-alu (hbm fraction shown)", "achieved": achieved, "peak": peak,
+                                       "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                                       "kernel": "asselin_save_kernel + asselin_filter_kernel",
+                                       "algorithmic_bytes_per_cell_layer": bpc,
+                                       "traffic": profile_traffic(f"asselin_fp64_{args.workload}")}}
+    del keep
     return res
 
 
@@ -475,6 +506,8 @@ def run_e2e(args, wl, b, spec, case, form, tile, nq, dev, stream, dist):
     torch.cuda.synchronize(dev)
     for k in phases:
         phases[k] = 0.0
+    ens.enable_timers(True)
+    ens.stats(reset=True)
     if dist:
         dist.barrier()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -484,16 +517,22 @@ def run_e2e(args, wl, b, spec, case, form, tile, nq, dev, stream, dist):
     f1.record(stream)
     torch.cuda.synchronize(dev)
     ems = f0.elapsed_time(f1)
+    est = ens.stats(reset=True)
     if dist:
         t = torch.tensor([ems], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ems = float(t.item())
     ens.close()
+    K = args.e2e_steps
+    device_ms = {"host_link_copies": est["copy_ms"] / K, "halo_and_repitch": est["stage_kernels_ms"] / K,
+                 "step": est["step_ms"] / K}
     ws = dist.get_world_size() if dist else 1
     ups_step = wl["nx"] * wl["ny"] * kdm * 2
     return {"value": ws * ups_step * args.e2e_steps / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "steps": args.e2e_steps, "form": form,
             "host_ms_per_step": {k: v / args.e2e_steps for k, v in phases.items()},
+            "device_ms_per_step": device_ms,
+            "host_link_GBs": (h2d + d2h) / max(device_ms["host_link_copies"], 1e-9) / 1e6,
             "note": "per step: hyc_ens_put of T,S (t-1, t), uflx, vflx, dp from pinned host FP64 arrays "
                     "(reference layout), hyc_ens_step, hyc_ens_get of the new T,S level"}
 
@@ -947,9 +986,10 @@ def main():
     ap.add_argument("--form", default="mixed-fp32prep", choices=sorted(ENS_FORMS),
                     help="headline form (ensemble API): FP32-mixed with FP64 thickness prep, with compensated "
                          "FP32 prep, or FP64")
-    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-diff,fp64,mixed,mixed-fp32prep",
+    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-full,fp64,mixed,mixed-fp32prep",
                     help="forms measured beside the headline (tsadvc[-fct4|-mpdata|-pcm] = FP64 plain through "
-                         "hyc_tsadvc, FCT2 unless named)")
+                         "hyc_tsadvc, FCT2 unless named; tsadvc-full = asselin_save + tsadvc + its "
+                         "diffusion + asselin_filter)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--c4-steps", type=int, default=100, help="c4: steps per basin")
     ap.add_argument("--tile", default="", help="mixed forms: fixed tile 'tx,ty,tracers_per_pass' instead of the tuner")
@@ -1004,9 +1044,9 @@ def main():
     for f, adv in (("tsadvc-fct4", 4), ("tsadvc-mpdata", 1), ("tsadvc-pcm", 0)):
         if f in others:
             schemes[f] = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, adv)
-    if "tsadvc-diff" in others:
-        schemes["tsadvc-diff"] = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local,
-                                                 2, diffusion=True)
+    if "tsadvc-full" in others:
+        schemes["tsadvc-full"] = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local,
+                                                 2, full=True)
     ens_forms = [f for f in others if f in ENS_FORMS and f != args.form]
     if "fp64" in ens_forms:  # the reference of the error checks runs first
         ens_forms = ["fp64"] + [f for f in ens_forms if f != "fp64"]

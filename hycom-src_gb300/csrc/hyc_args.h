@@ -79,6 +79,24 @@ struct TsdffArgs {
   double *th3d;             // th3d(:,:,1,n) when eos_t >= 0
 };
 
+// Robert-Asselin filter (mod_asselin.F90), see hyc_asselin.cu; arrays in
+// the reference layout (mod_cb_arrays.F90)
+struct AsselinArgs {
+  int ii, jj, nb, ld1, ld2;
+  long long slice;
+  int kdm, m, n, ntracr, mxlmy;
+  const uint8_t *msk;
+  double oneta0, ra2fac, thbase;
+  double *temp, *saln, *th3d;  // (ld1,ld2,kdm,2)
+  double *tracer;              // (ld1,ld2,kdm,2,ntracr)
+  double *q2, *q2l;            // (ld1,ld2,0:kdm+1,2)
+  double *dp;                  // (ld1,ld2,kdm,2); level m filtered
+  const double *dpo;           // (ld1,ld2,kdm,2)
+  const double *pbavg, *pbot;  // (ld1,ld2,3), (ld1,ld2)
+  double *oneta, *onetao;      // (ld1,ld2,2)
+  double *otemp, *osaln, *oth3d, *otracer, *oq2, *oq2l;  // t-1 copies
+};
+
 template <int TX, int TY>
 struct TileGeom {
   static constexpr int RX = TX + 6, RY = TY + 6, N = RX * RY;

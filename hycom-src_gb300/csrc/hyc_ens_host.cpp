@@ -665,24 +665,48 @@ static int move(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns_
   }
   double *stage = e->d_stage;
   cudaError_t c;
+  // with timers on: events around the host-link copy (slot HYC_T_COPY) and
+  // the halo/repitch kernels (slot HYC_T_XCTILR)
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  if (e->timing)
+    for (auto &x : ev) cudaEventCreate(&x);
+  auto mark = [&](int i) {
+    if (ev[i]) cudaEventRecord(ev[i], e->stream);
+  };
+  mark(0);
   if (put) {
     ECK(cudaMemcpyAsync(stage, host, bytes, where == HYC_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
                         e->stream),
         "put copy");
+    mark(1);
     // tsadvc refreshes these halos before advecting (mod_tsadvc.F90:1829-1836); dp's is taken as given
     if (what != HYC_E_DP) {
       c = hyc::launch_xctilr(stage, rsl, ns, b.idm, b.jdm, b.nbdy, b.ld1r, 5, 5, b.nreg, e->stream);
       if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put halo: %s", cudaGetErrorString(c));
     }
     c = hyc::launch_repitch(stage, 0, b.ld1r, rsl, dst, dfp32, b.ld1, b.slice, b.ld1r, b.ld2, ns, e->stream);
+    mark(2);
   } else {
     c = hyc::launch_repitch(dst, dfp32, b.ld1, b.slice, stage, 0, b.ld1r, rsl, b.ld1r, b.ld2, ns, e->stream);
+    mark(1);
     if (c == cudaSuccess)
       c = cudaMemcpyAsync(host, stage, bytes, where == HYC_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
                           e->stream);
+    mark(2);
   }
   if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put/get: %s", cudaGetErrorString(c));
   ECK(cudaStreamSynchronize(e->stream), "put/get sync");
+  if (ev[0]) {
+    float a = 0.f, z = 0.f;
+    cudaEventElapsedTime(&a, ev[0], ev[1]);
+    cudaEventElapsedTime(&z, ev[1], ev[2]);
+    const float copy = put ? a : z, kern = put ? z : a;
+    e->stats.ms[HYC_T_COPY] += copy;
+    e->stats.calls[HYC_T_COPY] += 1;
+    e->stats.ms[HYC_T_XCTILR] += kern;
+    e->stats.calls[HYC_T_XCTILR] += 1;
+    for (auto &x : ev) cudaEventDestroy(x);
+  }
   if (put && (what == HYC_E_OLD || what == HYC_E_CUR)) e->primed = false;
   return HYC_OK;
 }

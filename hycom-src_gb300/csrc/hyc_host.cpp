@@ -902,6 +902,113 @@ int hyc_tsdff(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, doub
   return HYC_OK;
 }
 
+namespace {
+
+// Bind the arrays of the Robert-Asselin filter; checks what the switches need.
+int asselin_args(hyc_ctx *c, int m, int n, const hyc_tsadvc_params *p, bool filter, hyc::AsselinArgs &a) {
+  if (!p || m < 1 || m > 2 || n < 1 || n > 2) return fail(c, HYC_ERR_ARG, "asselin: bad m/n/params");
+  if (p->ntracr < 0) return fail(c, HYC_ERR_ARG, "ntracr");
+  const int kk = c->kdm;
+  const long long sl = c->slice;
+  Field *F = c->fields;
+  auto need = [&](int id, int64_t nel, const char *name) -> int {
+    if (!F[id].dev) return fail(c, HYC_ERR_FIELD, "field %s is not bound", name);
+    if (F[id].nelem < nel) return fail(c, HYC_ERR_FIELD, "field %s has %lld elements, needs %lld", name,
+                                       (long long)F[id].nelem, (long long)nel);
+    return HYC_OK;
+  };
+  int rc;
+  if ((rc = need(HYC_F_TEMP, 2LL * kk * sl, "temp")) || (rc = need(HYC_F_SALN, 2LL * kk * sl, "saln")) ||
+      (rc = need(HYC_F_TH3D, 2LL * kk * sl, "th3d")) || (rc = need(HYC_F_ONETA, 2LL * sl, "oneta")) ||
+      (rc = need(HYC_F_ONETAO, 2LL * sl, "onetao")) || (rc = need(HYC_F_PBAVG, 3LL * sl, "pbavg")) ||
+      (rc = need(HYC_F_PBOT, sl, "pbot")) || (rc = need(HYC_F_OTEMP, (long long)kk * sl, "otemp")) ||
+      (rc = need(HYC_F_OSALN, (long long)kk * sl, "osaln")))
+    return rc;
+  if (!filter && (rc = need(HYC_F_OTH3D, (long long)kk * sl, "oth3d"))) return rc;
+  if (filter && ((rc = need(HYC_F_DP, 2LL * kk * sl, "dp")) || (rc = need(HYC_F_DPO, 2LL * kk * sl, "dpo"))))
+    return rc;
+  if (p->ntracr > 0 && ((rc = need(HYC_F_TRACER, 2LL * kk * sl * p->ntracr, "tracer")) ||
+                        (rc = need(HYC_F_OTRACER, (long long)kk * sl * p->ntracr, "otracer"))))
+    return rc;
+  if (p->mxlmy && ((rc = need(HYC_F_Q2, 2LL * (kk + 2) * sl, "q2")) || (rc = need(HYC_F_Q2L, 2LL * (kk + 2) * sl, "q2l")) ||
+                   (rc = need(HYC_F_OQ2, (long long)(kk + 2) * sl, "oq2")) ||
+                   (rc = need(HYC_F_OQ2L, (long long)(kk + 2) * sl, "oq2l"))))
+    return rc;
+  memset(&a, 0, sizeof a);
+  a.ii = c->idm;
+  a.jj = c->jdm;
+  a.nb = c->nbdy;
+  a.ld1 = c->ld1;
+  a.ld2 = c->ld2;
+  a.slice = sl;
+  a.kdm = kk;
+  a.m = m;
+  a.n = n;
+  a.ntracr = p->ntracr;
+  a.mxlmy = p->mxlmy ? 1 : 0;
+  a.msk = c->d_msk;
+  a.temp = F[HYC_F_TEMP].dev;
+  a.saln = F[HYC_F_SALN].dev;
+  a.th3d = F[HYC_F_TH3D].dev;
+  a.tracer = F[HYC_F_TRACER].dev;
+  a.q2 = F[HYC_F_Q2].dev;
+  a.q2l = F[HYC_F_Q2L].dev;
+  a.dp = F[HYC_F_DP].dev;
+  a.dpo = F[HYC_F_DPO].dev;
+  a.pbavg = F[HYC_F_PBAVG].dev;
+  a.pbot = F[HYC_F_PBOT].dev;
+  a.oneta = F[HYC_F_ONETA].dev;
+  a.onetao = F[HYC_F_ONETAO].dev;
+  a.otemp = F[HYC_F_OTEMP].dev;
+  a.osaln = F[HYC_F_OSALN].dev;
+  a.oth3d = F[HYC_F_OTH3D].dev;
+  a.otracer = F[HYC_F_OTRACER].dev;
+  a.oq2 = F[HYC_F_OQ2].dev;
+  a.oq2l = F[HYC_F_OQ2L].dev;
+  return HYC_OK;
+}
+
+}  // namespace
+
+int hyc_asselin_save(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, double oneta0) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  hyc::AsselinArgs a;
+  int rc = asselin_args(c, m, n, p, false, a);
+  if (rc) return rc;
+  a.oneta0 = oneta0;
+  DeviceGuard g(c->device);
+  Timed t(c, HYC_T_ASSELIN);
+  CK(hyc::launch_asselin(a, false, c->stream), "asselin_save");
+  CK(hyc::launch_xctilr(a.oneta, c->slice, 2, c->idm, c->jdm, c->nbdy, c->ld1, 6, 6, c->nreg, c->stream),
+     "xctilr oneta");
+  CK(hyc::launch_xctilr(a.onetao, c->slice, 2, c->idm, c->jdm, c->nbdy, c->ld1, 6, 6, c->nreg, c->stream),
+     "xctilr onetao");
+  c->stats.launches += 3;
+  return HYC_OK;
+}
+
+int hyc_asselin_filter(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, double ra2fac, double oneta0,
+                       double thbase) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (p && (p->advflg != 0 || p->isopyc))
+    return fail(c, HYC_ERR_UNSUPPORTED, "asselin_filter: only advflg = 0 hybrid layers (no tofsig in the 17-term "
+                                        "equation of state)");
+  if (p && p->nhybrd < c->kdm)
+    return fail(c, HYC_ERR_UNSUPPORTED, "asselin_filter: nhybrd = %d < kdm: exactly isopycnal layers need theta",
+                p->nhybrd);
+  hyc::AsselinArgs a;
+  int rc = asselin_args(c, m, n, p, true, a);
+  if (rc) return rc;
+  a.oneta0 = oneta0;
+  a.ra2fac = ra2fac;
+  a.thbase = thbase;
+  DeviceGuard g(c->device);
+  Timed t(c, HYC_T_ASSELIN);
+  CK(hyc::launch_asselin(a, true, c->stream), "asselin_filter");
+  c->stats.launches += 1;
+  return HYC_OK;
+}
+
 int hyc_mass_sum(hyc_ctx *c, const double *fld, const double *fc, double *sum) {
   if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
   if (!fld || !fc || !sum) return fail(c, HYC_ERR_ARG, "hyc_mass_sum: null pointer");

@@ -36,6 +36,10 @@ cudaError_t launch_fct2c(const Fct2cArgs &a, int nreg, int *launches, cudaStream
 struct TsdffArgs;
 cudaError_t launch_tsdff(const TsdffArgs &a, cudaStream_t s);
 
+// Robert-Asselin filter: asselin_save (filter false) or asselin_filter
+struct AsselinArgs;
+cudaError_t launch_asselin(const AsselinArgs &a, bool filter, cudaStream_t s);
+
 // xctilr on nlev slices (mod_xc_sm.h:1337-1428).
 cudaError_t launch_xctilr(double *a, long long slice, int nlev, int ii, int jj, int nbdy, int ld1, int mh,
                           int nh, int nreg, cudaStream_t s);

@@ -35,7 +35,8 @@ ERRORS = {-1: "HYC_ERR_ARG", -2: "HYC_ERR_ADVTYP", -3: "HYC_ERR_NBDY", -4: "HYC_
           -6: "HYC_ERR_FIELD", -7: "HYC_ERR_GRID", -8: "HYC_ERR_UNSUPPORTED", -9: "HYC_ERR_NOMEM"}
 HYC_HOST, HYC_DEVICE = 0, 1
 FIELDS = {"temp": 0, "saln": 1, "th3d": 2, "tracer": 3, "uflx": 4, "vflx": 5, "dp": 6, "oneta": 7, "q2": 8,
-          "q2l": 9}
+          "q2l": 9, "dpo": 10, "onetao": 11, "pbavg": 12, "pbot": 13, "otemp": 14, "osaln": 15, "oth3d": 16,
+          "otracer": 17, "oq2": 18, "oq2l": 19}
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "hyc_set_stream", "hyc_bind_field",
@@ -45,10 +46,11 @@ EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "
            "hyc_ens_put_slices", "hyc_ens_get_slices", "hyc_ens_set_tile",
            "hyc_ens_tune", "hyc_ens_step", "hyc_ens_content", "hyc_ens_stats", "hyc_ens_enable_timers",
            "hyc_ens_last_error", "hyc_ens_set_option", "hyc_ens_get_option", "hyc_ens_set_posdef",
-           "hyc_za_read", "hyc_za_parse_b", "hyc_za_check", "hyc_set_diffusion_grid", "hyc_tsdff")
+           "hyc_za_read", "hyc_za_parse_b", "hyc_za_check", "hyc_set_diffusion_grid", "hyc_tsdff",
+           "hyc_asselin_save", "hyc_asselin_filter")
 ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
-TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4, "tsdff": 5}
+TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4, "tsdff": 5, "asselin": 6}
 
 
 class HycError(RuntimeError):
@@ -102,6 +104,9 @@ def lib() -> C.CDLL:
         L.hyc_xctilr.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         L.hyc_mass_sum.argtypes = [vp, vp, vp, dp]
         L.hyc_set_diffusion_grid.argtypes = [vp, dp, dp, dp, dp]
+        L.hyc_asselin_save.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(TsadvcParams), C.c_double]
+        L.hyc_asselin_filter.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(TsadvcParams), C.c_double,
+                                         C.c_double, C.c_double]
         L.hyc_tsdff.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(TsadvcParams), C.c_double, C.c_double,
                                 C.c_double]
         L.hyc_enable_timers.argtypes = [vp, C.c_int32]
@@ -332,6 +337,28 @@ class Context(_StreamFollower):
         self._order(self._bound.values())
         _check(lib().hyc_tsdff(self._h, m, n, C.byref(p), float(temdf2), float(temdfc), float(thbase)), self._h)
 
+    def _params(self, ntracr=0, nhybrd=None, advflg=0, isopyc=False, mxlmy=False, delt1=0.0):
+        nh = self.kdm if nhybrd is None else nhybrd
+        tf = np.zeros(max(ntracr, 1), np.int32)
+        p = TsadvcParams(advtyp=2, advflg=advflg, btrmas=0, ntracr=ntracr, nhybrd=nh, isopyc=int(isopyc),
+                         hybrid=int(nh > 0), mxlmy=int(mxlmy), nstep=1, diagno=0, delt1=float(delt1),
+                         trcflg=tf.ctypes.data_as(C.POINTER(C.c_int32)))
+        return p, tf
+
+    def asselin_save(self, m: int, n: int, *, oneta0: float, ntracr: int = 0, mxlmy: bool = False):
+        """asselin_save(m,n) on the bound fields (start of a step)."""
+        p, tf = self._params(ntracr=ntracr, mxlmy=mxlmy)
+        self._order(self._bound.values())
+        _check(lib().hyc_asselin_save(self._h, m, n, C.byref(p), float(oneta0)), self._h)
+
+    def asselin_filter(self, m: int, n: int, *, ra2fac: float, oneta0: float, thbase: float = 34.0, ntracr: int = 0,
+                       mxlmy: bool = False, nhybrd: int | None = None, advflg: int = 0):
+        """asselin_filter(m,n) on the bound fields (end of a step)."""
+        p, tf = self._params(ntracr=ntracr, nhybrd=nhybrd, advflg=advflg, mxlmy=mxlmy)
+        self._order(self._bound.values())
+        _check(lib().hyc_asselin_filter(self._h, m, n, C.byref(p), float(ra2fac), float(oneta0), float(thbase)),
+               self._h)
+
     def advem(self, advtyp, fld, fldc, u, v, fco, fcn, posdef, scal, scali, dt2, btrmas=False):
         """advem on one slice; all arrays numpy (host) or all torch CUDA (device)."""
         arrs = [fld, fldc, u, v, fco, fcn, scal, scali]
@@ -488,4 +515,5 @@ class Ensemble(_StreamFollower):
     def stats(self, reset: bool = False) -> dict:
         s = Stats()
         self._chk(lib().hyc_ens_stats(self._h, C.byref(s), int(bool(reset))))
-        return {"launches": int(s.launches), "step_ms": float(s.ms[2]), "step_calls": int(s.calls[2])}
+        return {"launches": int(s.launches), "step_ms": float(s.ms[2]), "step_calls": int(s.calls[2]),
+                "copy_ms": float(s.ms[3]), "copy_calls": int(s.calls[3]), "stage_kernels_ms": float(s.ms[1])}

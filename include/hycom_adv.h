@@ -58,7 +58,18 @@ extern "C" {
 #define HYC_F_ONETA 7  /* oneta(ld1,ld2,2), read if btrmas */
 #define HYC_F_Q2 8     /* q2(ld1,ld2,0:kdm+1,2), if mxlmy  */
 #define HYC_F_Q2L 9    /* q2l(ld1,ld2,0:kdm+1,2), if mxlmy */
-#define HYC_NFIELDS 10
+/* Robert-Asselin filter state (mod_cb_arrays.F90), hyc_asselin_* only */
+#define HYC_F_DPO 10     /* dpo(ld1,ld2,kdm,2)                */
+#define HYC_F_ONETAO 11  /* onetao(ld1,ld2,2)                 */
+#define HYC_F_PBAVG 12   /* pbavg(ld1,ld2,3)                  */
+#define HYC_F_PBOT 13    /* pbot(ld1,ld2)                     */
+#define HYC_F_OTEMP 14   /* otemp(ld1,ld2,kdm)                */
+#define HYC_F_OSALN 15   /* osaln(ld1,ld2,kdm)                */
+#define HYC_F_OTH3D 16   /* oth3d(ld1,ld2,kdm)                */
+#define HYC_F_OTRACER 17 /* otracer(ld1,ld2,kdm,ntracr)       */
+#define HYC_F_OQ2 18     /* oq2(ld1,ld2,0:kdm+1), if mxlmy    */
+#define HYC_F_OQ2L 19    /* oq2l(ld1,ld2,0:kdm+1), if mxlmy   */
+#define HYC_NFIELDS 20
 
 typedef struct hyc_ctx hyc_ctx;
 
@@ -199,6 +210,32 @@ int hyc_tsdff(hyc_ctx *ctx, int32_t m, int32_t n, const hyc_tsadvc_params *p, do
               double thbase);
 
 /*
+ * asselin_save(m,n) (mod_asselin.F90:28-82), called at the start of a
+ * step (mod_hycom.F90:2517): oneta and onetao of both levels from
+ * pbavg/pbot at sea points (max with oneta0), level n of temp, saln, th3d,
+ * every tracer (and q2/q2l when p->mxlmy) into otemp, osaln, oth3d,
+ * otracer (oq2, oq2l) at every interior point, then the halo of oneta and
+ * onetao (width 6).  Uses p->ntracr and p->mxlmy.  Asynchronous.
+ * Replaces: mod_asselin.F90:28 (subroutine asselin_save).
+ */
+int hyc_asselin_save(hyc_ctx *ctx, int32_t m, int32_t n, const hyc_tsadvc_params *p, double oneta0);
+
+/*
+ * asselin_filter(m,n) (mod_asselin.F90:84-268), called at the end of a
+ * step (mod_hycom.F90:2645): oneta of both levels from pbavg/pbot, then at
+ * every sea point and layer the Robert-Asselin filter (weight ra2fac) of
+ * the thickness dp(m) and of oneta*dp*scalar for saln, temp, every tracer
+ * (the form that keeps a constant field constant) and q2/q2l, and
+ * th3d(m) = sig(temp(m),saln(m)) - thbase (17-term equation of state).
+ * Supported: advflg = 0 and nhybrd >= kdm (the 17-term equation of state
+ * has no tofsig for th3d-advecting or exactly isopycnal layers); else
+ * HYC_ERR_UNSUPPORTED.  FP64, bit-identical to the oracle.  Asynchronous.
+ * Replaces: mod_asselin.F90:84 (subroutine asselin_filter).
+ */
+int hyc_asselin_filter(hyc_ctx *ctx, int32_t m, int32_t n, const hyc_tsadvc_params *p, double ra2fac,
+                       double oneta0, double thbase);
+
+/*
  * Tracer content sum over sea points of the interior,
  *   sum_{i,j} fld(i,j) * (fc(i,j) + onemu) * scp2(i,j),
  * accumulated on the device in FP64 with compensated (two-sum) partials
@@ -221,6 +258,7 @@ int hyc_mass_sum(hyc_ctx *ctx, const double *fld, const double *fc, double *sum)
 #define HYC_T_COPY 3   /* copy of updated slices into level n   */
 #define HYC_T_DIAG 4   /* salinity range diagnostic             */
 #define HYC_T_TSDFF 5  /* lateral diffusion (hyc_tsdff)         */
+#define HYC_T_ASSELIN 6 /* Robert-Asselin save and filter      */
 #define HYC_NTIMERS 8
 
 typedef struct hyc_stats {
