@@ -68,15 +68,33 @@ struct hyc_ens {
   int nhead = 0;
   double *d_partial = nullptr;
   int npartial = 0;
-  double *d_stage = nullptr;  // put/get staging (reference layout, FP64), grown on demand
-  size_t stage_bytes = 0;
+  // put staging (reference layout, FP64), two buffers used in turn: a put's
+  // host-to-device copy runs on in_stream while the previous put's halo and
+  // repitch kernels (and the step) run on the ensemble's stream
+  double *d_stage[2] = {nullptr, nullptr};
+  size_t stage_bytes[2] = {0, 0};
+  int stage_next = 0;
+  bool stage_used[2] = {false, false};
+  cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr}, ev_entry = nullptr;
+  cudaStream_t in_stream = nullptr;
+  // get staging; hyc_ens_get_async copies it out on copy_stream so the
+  // device-to-host transfer overlaps later puts (the link is full duplex)
+  double *d_gstage = nullptr;
+  size_t gstage_bytes = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_staged = nullptr, ev_gdone = nullptr;
+  bool get_pending = false;
   // graph cache
   cudaGraphExec_t gexec = nullptr;
   int g_nsteps = 0, g_advtyp = -1, g_rot = -1, g_tx = 0, g_ty = 0;
   double g_dt = 0.0;
   // timers
   bool timing = false;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+  struct Span {
+    int slot;
+    cudaEvent_t a, z;
+  };
+  std::vector<Span> pending;  // timed spans, folded into stats by hyc_ens_stats
   hyc_stats stats{};
   std::string err;
 };
@@ -141,14 +159,26 @@ void free_all(hyc_ens *e) {
   cudaFree(e->d_items);
   cudaFree(e->d_head);
   cudaFree(e->d_partial);
-  cudaFree(e->d_stage);
+  if (e->in_stream) cudaStreamSynchronize(e->in_stream);
+  if (e->copy_stream) cudaStreamSynchronize(e->copy_stream);
+  for (int q = 0; q < 2; q++) {
+    cudaFree(e->d_stage[q]);
+    if (e->ev_copied[q]) cudaEventDestroy(e->ev_copied[q]);
+    if (e->ev_used[q]) cudaEventDestroy(e->ev_used[q]);
+  }
+  if (e->ev_entry) cudaEventDestroy(e->ev_entry);
+  cudaFree(e->d_gstage);
+  if (e->ev_staged) cudaEventDestroy(e->ev_staged);
+  if (e->ev_gdone) cudaEventDestroy(e->ev_gdone);
+  if (e->copy_stream) cudaStreamDestroy(e->copy_stream);
+  if (e->in_stream) cudaStreamDestroy(e->in_stream);
   cudaFree(e->d_tmaps);
   cudaFree(e->d_cmaps);
   cudaFree(e->d_err);
   if (e->gexec) cudaGraphExecDestroy(e->gexec);
   for (auto &p : e->pending) {
-    cudaEventDestroy(p.first);
-    cudaEventDestroy(p.second);
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.z);
   }
 }
 
@@ -627,8 +657,49 @@ int hyc_ens_set_stream(hyc_ens *e, void *stream) {
   return HYC_OK;
 }
 
+// Open a timed span on stream st (timers on): returns the start event.
+static cudaEvent_t span_open(hyc_ens *e, cudaStream_t st) {
+  if (!e->timing) return nullptr;
+  cudaEvent_t a = nullptr;
+  cudaEventCreate(&a);
+  cudaEventRecord(a, st);
+  return a;
+}
+static void span_close(hyc_ens *e, cudaEvent_t a, int slot, cudaStream_t st) {
+  if (!a) return;
+  cudaEvent_t z = nullptr;
+  cudaEventCreate(&z);
+  cudaEventRecord(z, st);
+  e->pending.push_back({slot, a, z});
+}
+
+static int grow(hyc_ens *e, double **buf, size_t *have, size_t bytes, const char *what) {
+  if (*have >= bytes) return HYC_OK;
+  cudaFree(*buf);
+  *buf = nullptr;
+  *have = 0;
+  ECK(cudaMalloc(buf, bytes), what);
+  *have = bytes;
+  return HYC_OK;
+}
+
+static int ensure_io(hyc_ens *e) {
+  if (e->in_stream) return HYC_OK;
+  ECK(cudaStreamCreateWithFlags(&e->in_stream, cudaStreamNonBlocking), "input stream");
+  ECK(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking), "copy stream");
+  for (int q = 0; q < 2; q++) {
+    ECK(cudaEventCreateWithFlags(&e->ev_copied[q], cudaEventDisableTiming), "event");
+    ECK(cudaEventCreateWithFlags(&e->ev_used[q], cudaEventDisableTiming), "event");
+  }
+  ECK(cudaEventCreateWithFlags(&e->ev_entry, cudaEventDisableTiming), "event");
+  ECK(cudaEventCreateWithFlags(&e->ev_staged, cudaEventDisableTiming), "event");
+  ECK(cudaEventCreateWithFlags(&e->ev_gdone, cudaEventDisableTiming), "event");
+  return HYC_OK;
+}
+
+// Host-link copies with timers on: slot HYC_T_COPY; halo/repitch kernels: HYC_T_XCTILR.
 static int move(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns_req, void *host, int32_t where,
-                bool put) {
+                bool put, bool async_get = false) {
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   if (basin < 0 || basin >= (int)e->b.size() || what < HYC_E_OLD || what > HYC_E_DP || !host ||
       (where != HYC_HOST && where != HYC_DEVICE) || (!put && what > HYC_E_CUR && what != HYC_E_DP))
@@ -656,58 +727,72 @@ static int move(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns_
   dst = (char *)dst + (size_t)s0 * b.slice * (dfp32 ? 4 : 8);
   const long long rsl = (long long)b.ld1r * b.ld2;
   const size_t bytes = (size_t)rsl * ns * 8;
-  if (e->stage_bytes < bytes) {  // the previous put/get synchronised: the old buffer is idle
-    cudaFree(e->d_stage);
-    e->d_stage = nullptr;
-    e->stage_bytes = 0;
-    ECK(cudaMalloc(&e->d_stage, bytes), "staging");
-    e->stage_bytes = bytes;
-  }
-  double *stage = e->d_stage;
+  int rc;
+  if ((rc = ensure_io(e))) return rc;
+  const cudaMemcpyKind kin = where == HYC_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  const cudaMemcpyKind kout = where == HYC_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   cudaError_t c;
-  // with timers on: events around the host-link copy (slot HYC_T_COPY) and
-  // the halo/repitch kernels (slot HYC_T_XCTILR)
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-  if (e->timing)
-    for (auto &x : ev) cudaEventCreate(&x);
-  auto mark = [&](int i) {
-    if (ev[i]) cudaEventRecord(ev[i], e->stream);
-  };
-  mark(0);
   if (put) {
-    ECK(cudaMemcpyAsync(stage, host, bytes, where == HYC_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
-                        e->stream),
-        "put copy");
-    mark(1);
+    const int q = e->stage_next;
+    e->stage_next ^= 1;
+    if (e->stage_bytes[q] < bytes) {  // nothing may still use the old buffer
+      ECK(cudaStreamSynchronize(e->stream), "put sync");
+      ECK(cudaStreamSynchronize(e->in_stream), "put sync");
+      e->stage_used[q] = false;
+      if ((rc = grow(e, &e->d_stage[q], &e->stage_bytes[q], bytes, "staging"))) return rc;
+    }
+    double *stage = e->d_stage[q];
+    // the copy waits for the last kernels that read this buffer; a device
+    // source may still be written by work queued on the ensemble's stream
+    if (e->stage_used[q]) ECK(cudaStreamWaitEvent(e->in_stream, e->ev_used[q], 0), "wait staging");
+    if (where == HYC_DEVICE) {
+      ECK(cudaEventRecord(e->ev_entry, e->stream), "event");
+      ECK(cudaStreamWaitEvent(e->in_stream, e->ev_entry, 0), "wait source");
+    }
+    cudaEvent_t t0 = span_open(e, e->in_stream);
+    ECK(cudaMemcpyAsync(stage, host, bytes, kin, e->in_stream), "put copy");
+    span_close(e, t0, HYC_T_COPY, e->in_stream);
+    ECK(cudaEventRecord(e->ev_copied[q], e->in_stream), "event");
+    ECK(cudaStreamWaitEvent(e->stream, e->ev_copied[q], 0), "wait copy");
+    cudaEvent_t t1 = span_open(e, e->stream);
     // tsadvc refreshes these halos before advecting (mod_tsadvc.F90:1829-1836); dp's is taken as given
     if (what != HYC_E_DP) {
       c = hyc::launch_xctilr(stage, rsl, ns, b.idm, b.jdm, b.nbdy, b.ld1r, 5, 5, b.nreg, e->stream);
       if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put halo: %s", cudaGetErrorString(c));
     }
     c = hyc::launch_repitch(stage, 0, b.ld1r, rsl, dst, dfp32, b.ld1, b.slice, b.ld1r, b.ld2, ns, e->stream);
-    mark(2);
-  } else {
-    c = hyc::launch_repitch(dst, dfp32, b.ld1, b.slice, stage, 0, b.ld1r, rsl, b.ld1r, b.ld2, ns, e->stream);
-    mark(1);
-    if (c == cudaSuccess)
-      c = cudaMemcpyAsync(host, stage, bytes, where == HYC_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
-                          e->stream);
-    mark(2);
+    if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put: %s", cudaGetErrorString(c));
+    span_close(e, t1, HYC_T_XCTILR, e->stream);
+    ECK(cudaEventRecord(e->ev_used[q], e->stream), "event");
+    e->stage_used[q] = true;
+    // the caller's buffer is free once its copy is done; the kernels go on
+    ECK(cudaEventSynchronize(e->ev_copied[q]), "put copy sync");
+    if (what == HYC_E_OLD || what == HYC_E_CUR) e->primed = false;
+    return HYC_OK;
   }
-  if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put/get: %s", cudaGetErrorString(c));
-  ECK(cudaStreamSynchronize(e->stream), "put/get sync");
-  if (ev[0]) {
-    float a = 0.f, z = 0.f;
-    cudaEventElapsedTime(&a, ev[0], ev[1]);
-    cudaEventElapsedTime(&z, ev[1], ev[2]);
-    const float copy = put ? a : z, kern = put ? z : a;
-    e->stats.ms[HYC_T_COPY] += copy;
-    e->stats.calls[HYC_T_COPY] += 1;
-    e->stats.ms[HYC_T_XCTILR] += kern;
-    e->stats.calls[HYC_T_XCTILR] += 1;
-    for (auto &x : ev) cudaEventDestroy(x);
+  // get: repitch into the get staging on the ensemble's stream (after any
+  // copy-out still reading it), then copy out
+  if (e->gstage_bytes < bytes) {
+    ECK(cudaStreamSynchronize(e->copy_stream), "copy stream sync");
+    e->get_pending = false;
+    if ((rc = grow(e, &e->d_gstage, &e->gstage_bytes, bytes, "get staging"))) return rc;
   }
-  if (put && (what == HYC_E_OLD || what == HYC_E_CUR)) e->primed = false;
+  if (e->get_pending) ECK(cudaStreamWaitEvent(e->stream, e->ev_gdone, 0), "wait copy-out");
+  cudaEvent_t t1 = span_open(e, e->stream);
+  c = hyc::launch_repitch(dst, dfp32, b.ld1, b.slice, e->d_gstage, 0, b.ld1r, rsl, b.ld1r, b.ld2, ns, e->stream);
+  if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "get: %s", cudaGetErrorString(c));
+  span_close(e, t1, HYC_T_XCTILR, e->stream);
+  ECK(cudaEventRecord(e->ev_staged, e->stream), "event");
+  ECK(cudaStreamWaitEvent(e->copy_stream, e->ev_staged, 0), "wait staged");
+  cudaEvent_t t0 = span_open(e, e->copy_stream);
+  ECK(cudaMemcpyAsync(host, e->d_gstage, bytes, kout, e->copy_stream), "get copy");
+  span_close(e, t0, HYC_T_COPY, e->copy_stream);
+  ECK(cudaEventRecord(e->ev_gdone, e->copy_stream), "event");
+  e->get_pending = true;
+  if (!async_get) {
+    ECK(cudaEventSynchronize(e->ev_gdone), "get sync");
+    e->get_pending = false;
+  }
   return HYC_OK;
 }
 
@@ -717,6 +802,18 @@ int hyc_ens_put(hyc_ens *e, int32_t basin, int32_t what, const double *src, int3
 
 int hyc_ens_get(hyc_ens *e, int32_t basin, int32_t what, double *dst, int32_t where) {
   return move(e, basin, what, 0, -1, dst, where, false);
+}
+
+int hyc_ens_get_async(hyc_ens *e, int32_t basin, int32_t what, double *dst, int32_t where) {
+  return move(e, basin, what, 0, -1, dst, where, false, true);
+}
+
+int hyc_ens_wait(hyc_ens *e) {
+  if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
+  Dev g(e->device);
+  if (e->copy_stream) ECK(cudaStreamSynchronize(e->copy_stream), "copy-out sync");
+  e->get_pending = false;
+  return HYC_OK;
 }
 
 int hyc_ens_put_slices(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns, const double *src,
@@ -822,14 +919,16 @@ int hyc_ens_stats(hyc_ens *e, hyc_stats *out, int32_t reset) {
   int flag = 0;
   ECK(cudaMemcpy(&flag, e->d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
   if (flag) return efail(e, HYC_ERR_CUDA, "a step kernel gave up waiting for its TMA loads");
+  if (e->in_stream) ECK(cudaStreamSynchronize(e->in_stream), "stats sync");
+  if (e->copy_stream) ECK(cudaStreamSynchronize(e->copy_stream), "stats sync");
   for (auto &p : e->pending) {
     float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, p.first, p.second) == cudaSuccess) {
-      e->stats.ms[HYC_T_ADVECT] += ms;
-      e->stats.calls[HYC_T_ADVECT] += 1;
+    if (cudaEventElapsedTime(&ms, p.a, p.z) == cudaSuccess) {
+      e->stats.ms[p.slot] += ms;
+      e->stats.calls[p.slot] += 1;
     }
-    cudaEventDestroy(p.first);
-    cudaEventDestroy(p.second);
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.z);
   }
   e->pending.clear();
   *out = e->stats;
@@ -900,7 +999,7 @@ int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32
   }
   if (e->timing) {
     cudaEventRecord(z, e->stream);
-    e->pending.push_back({a, z});
+    e->pending.push_back({HYC_T_ADVECT, a, z});
   }
   return HYC_OK;
 }

@@ -210,7 +210,9 @@ double key_to_double(long long k) {
 __global__ void saln_range_kernel(const double *saln_n, const double *dp_n, const uint8_t *msk, long long slice,
                                   int ii, int jj, int nb, int ld1, long long *keys, int kdm) {
   const int k = blockIdx.y;
-  const double onemm = 9806.0 * 0.001;  // onem*0.001 Pa, mod_cb_arrays.F90:846-848
+  // onemm = onem*0.001 with onem = g/svref = 9.806/(1/1000) folded in double
+  // (9805.999999999998 Pa), mod_cb_arrays.F90:843-851
+  const double onemm = (9.806 / (1.0 / 1000.0)) * 0.001;
   const double *s = saln_n + (long long)k * slice, *d = dp_n + (long long)k * slice;
   long long kmn = LLONG_MAX, kmx = LLONG_MIN;
   const long long n = (long long)ii * jj;

@@ -47,7 +47,7 @@ EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "
            "hyc_ens_tune", "hyc_ens_step", "hyc_ens_content", "hyc_ens_stats", "hyc_ens_enable_timers",
            "hyc_ens_last_error", "hyc_ens_set_option", "hyc_ens_get_option", "hyc_ens_set_posdef",
            "hyc_za_read", "hyc_za_parse_b", "hyc_za_check", "hyc_set_diffusion_grid", "hyc_tsdff",
-           "hyc_asselin_save", "hyc_asselin_filter")
+           "hyc_asselin_save", "hyc_asselin_filter", "hyc_ens_get_async", "hyc_ens_wait")
 ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
 TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4, "tsdff": 5, "asselin": 6}
@@ -116,6 +116,8 @@ def lib() -> C.CDLL:
         L.hyc_ens_set_stream.argtypes = [vp, vp]
         L.hyc_ens_put.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int32]
         L.hyc_ens_get.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int32]
+        L.hyc_ens_get_async.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int32]
+        L.hyc_ens_wait.argtypes = [vp]
         L.hyc_ens_put_slices.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
         L.hyc_ens_get_slices.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
         L.hyc_ens_set_tile.argtypes = [vp, C.c_int32, C.c_int32]
@@ -467,6 +469,17 @@ class Ensemble(_StreamFollower):
         else:
             self._chk(lib().hyc_ens_get_slices(self._h, b, ENS_WHAT[what], s0, ns, p, where))
         return out
+
+    def get_async(self, b: int, what: str, out):
+        """hyc_ens_get_async: the copy into out overlaps later work; call
+        wait() before reading out."""
+        p, where = _ptr(out)
+        self._order((out,))
+        self._chk(lib().hyc_ens_get_async(self._h, b, ENS_WHAT[what], p, where))
+        return out
+
+    def wait(self):
+        self._chk(lib().hyc_ens_wait(self._h))
 
     def set_tile(self, tx: int, ty: int):
         self._chk(lib().hyc_ens_set_tile(self._h, tx, ty))

@@ -336,6 +336,16 @@ int hyc_ens_set_stream(hyc_ens *ens, void *stream);
 /* src/dst: ld1*ld2*(slices) doubles in the reference layout (pitch idm+2*nbdy) */
 int hyc_ens_put(hyc_ens *ens, int32_t basin, int32_t what, const double *src, int32_t where);
 int hyc_ens_get(hyc_ens *ens, int32_t basin, int32_t what, double *dst, int32_t where);
+/*
+ * As hyc_ens_get, but returns once the values are staged on the device:
+ * the copy into dst runs on a copy stream of the ensemble and overlaps the
+ * puts and steps queued after it (host<->device links are full duplex).
+ * dst must stay valid and is not to be read until hyc_ens_wait returns.
+ * A later get_async waits for the previous one's copy-out on the device.
+ */
+int hyc_ens_get_async(hyc_ens *ens, int32_t basin, int32_t what, double *dst, int32_t where);
+/* Wait for every hyc_ens_get_async copy-out issued so far. */
+int hyc_ens_wait(hyc_ens *ens);
 /* The same for the slices [s0, s0+ns) only (tracer-major for HYC_E_OLD/CUR:
  * slice q*kdm+k), so a caller can move one tracer at a time. */
 int hyc_ens_put_slices(hyc_ens *ens, int32_t basin, int32_t what, int32_t s0, int32_t ns, const double *src,

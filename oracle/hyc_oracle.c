@@ -82,6 +82,9 @@ typedef struct hyo_grid {
 #define SI(g, i, l) ((size_t)((i) + (g)->nbdy - 1) + (size_t)((l)-1) * (size_t)(g)->ld1)
 
 static const double ONEMU = 9806.e-12; /* mod_tsadvc.F90:236,519,671,1396 */
+/* onem = g/svref with g = 9.806, svref = 1/1000 (mod_cb_arrays.F90:843-846),
+   folded in double: 9805.999999999998, not 9806 */
+#define ONEM (9.806 / (1.0 / 1000.0))
 static const double EPSIL = 1.e-10;    /* mod_tsadvc.F90:1027 */
 
 static inline double mx2(double a, double b) { return a > b ? a : b; }
@@ -1282,7 +1285,7 @@ int hyo_tsadvc(hyo_grid *g, const hyo_tsparams *p, int m, int n, double *temp, d
     }
     if (rc != HYO_OK) return HYO_ERR_ADVTYP;
     if (diag && xmin && xmax) { /* :2065-2084 */
-      const double onemm = 9806.0 * 0.001; /* onem*0.001, mod_cb_arrays.F90 */
+      const double onemm = ONEM * 0.001; /* onemm, mod_cb_arrays.F90:851 */
       double smin = 999., smax = -999.;
       const double *sk = F3(saln, k - 1, nn), *dk = F3(dp, k - 1, nn);
       for (int j = 1; j <= jj; j++) {
@@ -1640,4 +1643,433 @@ int hyo_asselin_filter(hyo_grid *g, const hyo_tsparams *p, double ra2fac, double
       }
   }
   return HYO_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* Continuity equation, cnuity.F90:14-1419 (flux-corrected transport   */
+/* of the layer thicknesses): loop 76 (low-order fluxes, FCT limiter,  */
+/* antidiffusive fluxes), the negative-thickness check, loop 77 and    */
+/* the bottom-pressure restoring (not btrmas), biharmonic (loop 13) or */
+/* Laplacian (loop 113) interface-depth diffusion, the cumulative      */
+/* fluxes, the btrmas restoring and the Robert-Asselin filter of dp.   */
+/* Not restated: open boundaries (iuopn/ivopn), STOKES drift, isopyc   */
+/* (dpmixl), the Kraus-Turner mixed-layer base advection (mxlkta) and  */
+/* the float vertical velocity (synflt).                               */
+/* ------------------------------------------------------------------ */
+typedef struct hyo_cnparams {
+  int kdm, nstep, btrmas;
+  int thkdf4, thkdf2; /* nonzero: that thickness diffusion runs, with the coefficients thkdfu/thkdfv
+                         (the reference's thkdf4u/thkdf4v, which hold thkdf2's in the Laplacian case) */
+  double delt1, ra2fac;
+} hyo_cnparams;
+
+enum {
+  HYO_C_DP, HYO_C_DPO, HYO_C_DPU, HYO_C_DPV, HYO_C_U, HYO_C_V, HYO_C_UBAVG, HYO_C_VBAVG, HYO_C_PBOT, HYO_C_DEPTHU,
+  HYO_C_DEPTHV, HYO_C_ONETA, HYO_C_SCUY, HYO_C_SCVX, HYO_C_THKDFU, HYO_C_THKDFV, HYO_C_P, HYO_C_UFLX, HYO_C_VFLX,
+  HYO_C_UFLXAV, HYO_C_VFLXAV, HYO_C_DPAV, HYO_C_ONETACNT, HYO_C_N
+};
+#define HYO_ERR_NEGDP (-9)
+
+/* ipim1x etc. (bigrid.F90:343-368): W (E, S, N) if sea, else the opposite
+   neighbour if sea, else the point itself */
+static inline int nbx(const hyo_grid *g, int i, int j, int di, int dj) {
+  if (g->ip[P(g, i + di, j + dj)] != 0) return 1;
+  if (g->ip[P(g, i - di, j - dj)] != 0) return -1;
+  return 0;
+}
+
+int hyo_cnuity(hyo_grid *g, const hyo_cnparams *p, int m, int n, double *const *a, double *dpkmin_out) {
+  const int ii = g->ii, jj = g->jj, kk = p->kdm, ld = g->ld1;
+  const size_t sl = (size_t)g->ld1 * g->ld2;
+  if (m < 1 || m > 2 || n < 1 || n > 2 || kk < 1 || g->nbdy < 6) return HYO_ERR_ARG;
+  for (int q = 0; q < HYO_C_N; q++)
+    if (!a[q] && q != HYO_C_UFLXAV && q != HYO_C_VFLXAV && q != HYO_C_DPAV && q != HYO_C_ONETA &&
+        q != HYO_C_ONETACNT && q != HYO_C_THKDFU && q != HYO_C_THKDFV)
+      return HYO_ERR_ARG;
+  if (p->btrmas && (!a[HYO_C_ONETA] || !a[HYO_C_ONETACNT])) return HYO_ERR_ARG;
+  if ((p->thkdf4 || p->thkdf2) && (!a[HYO_C_THKDFU] || !a[HYO_C_THKDFV])) return HYO_ERR_ARG;
+  const int mm = m - 1, nn = n - 1;
+  const int32_t *ip = g->ip, *iu = g->iu, *iv = g->iv;
+  const double *scp2 = g->scp2, *scp2i = g->scp2i;
+  double *dp = a[HYO_C_DP], *dpo = a[HYO_C_DPO], *pp = a[HYO_C_P], *uflx = a[HYO_C_UFLX], *vflx = a[HYO_C_VFLX];
+  const double *dpu = a[HYO_C_DPU], *dpv = a[HYO_C_DPV], *u = a[HYO_C_U], *v = a[HYO_C_V];
+  const double *ubavg = a[HYO_C_UBAVG], *vbavg = a[HYO_C_VBAVG], *pbot = a[HYO_C_PBOT];
+  const double *depthu = a[HYO_C_DEPTHU], *depthv = a[HYO_C_DEPTHV], *scuy = a[HYO_C_SCUY], *scvx = a[HYO_C_SCVX];
+  const double onem = ONEM, onecm = ONEM * 0.01, epsil = 1.0e-11, dpfatal = -10.0, epsil_cnuity = 1.e-14;
+  double *uflux = g->uflux, *vflux = g->vflux, *uflux2 = g->uflux2, *vflux2 = g->vflux2;
+  double *w = (double *)calloc(sl * 12, sizeof(double));
+  if (!w) return HYO_ERR_ARG;
+  double *utotm = w, *vtotm = w + sl, *utotn = w + 2 * sl, *vtotn = w + 3 * sl, *util1 = w + 4 * sl,
+         *util2 = w + 5 * sl, *util3 = w + 6 * sl, *pold = w + 7 * sl, *oneta_u = w + 8 * sl,
+         *oneta_v = w + 9 * sl, *om = w + 10 * sl; /* onetamas(:,:,1:2) */
+#define DPK(k, t) (dp + ((size_t)(k) + (size_t)(t) * kk) * sl) /* k 0-based */
+#define PK(k) (pp + (size_t)(k) * sl)                          /* p(:,:,k+1), k 0-based */
+  double *dpkmin = (double *)malloc(sizeof(double) * 2 * kk);
+  /* uflux/vflux hold 0 on faces that are not sea faces when cnuity runs:
+     geopar zeroes them next to the sea (geopar.F90:826-836), tsadvc zeroes
+     the whole array every step (mod_tsadvc.F90:1812-1813), and momtum,
+     cnuity and tsdff write sea faces only */
+  for (size_t c = 0; c < sl; c++) {
+    if (iu[c] == 0) uflux[c] = 0.0;
+    if (iv[c] == 0) vflux[c] = 0.0;
+  }
+  int mbdy = 6;
+  /* halos (:100-107); dpmixl is not restated */
+  hyo_xctilr(g, dp, 2 * kk, 6, 6);
+  hyo_xctilr(g, (double *)dpu + (size_t)mm * kk * sl, kk, 6, 6);
+  hyo_xctilr(g, (double *)dpv + (size_t)mm * kk * sl, kk, 6, 6);
+  hyo_xctilr(g, (double *)u + (size_t)mm * kk * sl, kk, 6, 6);
+  hyo_xctilr(g, (double *)v + (size_t)mm * kk * sl, kk, 6, 6);
+  hyo_xctilr(g, (double *)ubavg + (size_t)mm * sl, 1, 6, 6);
+  hyo_xctilr(g, (double *)vbavg + (size_t)mm * sl, 1, 6, 6);
+  int margin = mbdy; /* :112-157 */
+  for (int j = 1 - margin; j <= jj + margin; j++)
+    for (int i = 1 - margin; i <= ii + margin; i++) {
+      size_t c = P(g, i, j);
+      if (p->btrmas) {
+        const double *oneta = a[HYO_C_ONETA];
+        om[c] = oneta[c];
+        om[c + sl] = oneta[c + sl];
+        if (iu[c] != 0) {
+          if (pbot[c] == pbot[c - 1]) oneta_u[c] = 0.5 * (om[c + mm * sl] + om[c - 1 + mm * sl]);
+          else if (pbot[c] == depthu[c]) oneta_u[c] = om[c + mm * sl];
+          else oneta_u[c] = om[c - 1 + mm * sl];
+        }
+        if (iv[c] != 0) {
+          if (pbot[c] == pbot[c - ld]) oneta_v[c] = 0.5 * (om[c + mm * sl] + om[c - ld + mm * sl]);
+          else if (pbot[c] == depthv[c]) oneta_v[c] = om[c + mm * sl];
+          else oneta_v[c] = om[c - ld + mm * sl];
+        }
+      } else {
+        om[c] = 1.0;
+        om[c + sl] = 1.0;
+        oneta_u[c] = 1.0;
+        oneta_v[c] = 1.0;
+      }
+      utotn[c] = 0.0;
+      vtotn[c] = 0.0;
+      util3[c] = 0.0;
+      for (int k = 0; k < kk; k++) dpo[((size_t)k + (size_t)nn * kk) * sl + c] = DPK(k, nn)[c]; /* t-1 */
+    }
+  const double *omn = om + (size_t)nn * sl;
+  for (int k = 0; k < kk; k++) { /* loop 76 */
+    double *dk = DPK(k, nn);
+    const double *uk = u + ((size_t)k + (size_t)mm * kk) * sl, *vk = v + ((size_t)k + (size_t)mm * kk) * sl;
+    const double *dpuk = dpu + ((size_t)k + (size_t)mm * kk) * sl, *dpvk = dpv + ((size_t)k + (size_t)mm * kk) * sl;
+    double *uflxk = uflx + (size_t)k * sl, *vflxk = vflx + (size_t)k * sl;
+    margin = mbdy - 1; /* :240-285 (open-boundary loops :160-234 do nothing without iuopn/ivopn) */
+    for (int j = 1 - margin; j <= jj + margin; j++) {
+      for (int i = 1 - margin; i <= ii + margin; i++) {
+        size_t c = P(g, i, j);
+        if (iu[c] == 0) continue;
+        utotm[c] = (uk[c] + ubavg[c + mm * sl]) * scuy[c];
+        double q;
+        if (utotm[c] >= 0.) q = mn2(dk[c - 1], mx2(0., depthu[c] - util3[c - 1])) * omn[c - 1];
+        else q = mn2(dk[c], mx2(0., depthu[c] - util3[c])) * omn[c];
+        uflux[c] = utotm[c] * q;
+        uflux2[c] = utotm[c] * dpuk[c] * oneta_u[c] - uflux[c];
+        uflxk[c] = uflux[c];
+      }
+      for (int i = 1 - margin; i <= ii + margin; i++) {
+        size_t c = P(g, i, j);
+        if (iv[c] == 0) continue;
+        vtotm[c] = (vk[c] + vbavg[c + mm * sl]) * scvx[c];
+        double q;
+        if (vtotm[c] >= 0.) q = mn2(dk[c - ld], mx2(0., depthv[c] - util3[c - ld])) * omn[c - ld];
+        else q = mn2(dk[c], mx2(0., depthv[c] - util3[c])) * omn[c];
+        vflux[c] = vtotm[c] * q;
+        vflux2[c] = vtotm[c] * dpvk[c] * oneta_v[c] - vflux[c];
+        vflxk[c] = vflux[c];
+      }
+    }
+    margin = mbdy - 2; /* loop 19, :294-315 */
+    double dmin = 999.;
+    for (int j = 1 - margin; j <= jj + margin; j++) {
+      double dpmin = 999.;
+      for (int i = 1 - margin; i <= ii + margin; i++) {
+        size_t c = P(g, i, j);
+        if (ip[c] == 0) continue;
+        util3[c] = util3[c] + dk[c];
+        dk[c] = dk[c] * omn[c] - ((uflux[c + 1] - uflux[c]) + (vflux[c + ld] - vflux[c])) * p->delt1 * scp2i[c];
+        dpo[((size_t)k + (size_t)mm * kk) * sl + c] = dk[c];
+        dpmin = mn2(dpmin, dk[c]);
+      }
+      if (j >= 1 && j <= jj) dmin = mn2(dmin, dpmin);
+    }
+    dpkmin[k] = dmin;
+    margin = mbdy - 2; /* :400-430 */
+    for (int j = 1 - margin; j <= jj + margin; j++)
+      for (int i = 1 - margin; i <= ii + margin; i++) {
+        size_t c = P(g, i, j);
+        if (ip[c] == 0) continue;
+        const size_t ca = P(g, g->ipim1[c], j), cb = P(g, g->ipip1[c], j), cja = P(g, i, g->ipjm1[c]),
+                     cjb = P(g, i, g->ipjp1[c]);
+        double u1 = mx5(dk[c], dk[ca], dk[cb], dk[cja], dk[cjb]);
+        double u2 = mx2(0., mn2(mn2(mn2(mn2(dk[c], dk[ca]), dk[cb]), dk[cja]), dk[cjb]));
+        util1[c] = (u1 - dk[c]) / ((((mx2(0., uflux2[c]) - mn2(0., uflux2[c + 1])) +
+                                     (mx2(0., vflux2[c]) - mn2(0., vflux2[c + ld]))) + epsil) *
+                                   p->delt1 * scp2i[c]);
+        util2[c] = (u2 - dk[c]) / ((((mn2(0., uflux2[c]) - mx2(0., uflux2[c + 1])) +
+                                     (mn2(0., vflux2[c]) - mx2(0., vflux2[c + ld]))) - epsil) *
+                                   p->delt1 * scp2i[c]);
+      }
+    margin = mbdy - 3; /* :442-472 */
+    for (int j = 1 - margin; j <= jj + margin; j++) {
+      for (int i = 1 - margin; i <= ii + margin; i++) {
+        size_t c = P(g, i, j);
+        if (iu[c] == 0) continue;
+        double clip = uflux2[c] >= 0. ? mn2(mn2(1., util1[c]), util2[c - 1]) : mn2(mn2(1., util2[c]), util1[c - 1]);
+        utotn[c] = utotn[c] + uflux2[c] * (1. - clip);
+        uflux[c] = uflux2[c] * clip;
+        uflxk[c] = uflxk[c] + uflux[c];
+      }
+      for (int i = 1 - margin; i <= ii + margin; i++) {
+        size_t c = P(g, i, j);
+        if (iv[c] == 0) continue;
+        double clip =
+            vflux2[c] >= 0. ? mn2(mn2(1., util1[c]), util2[c - ld]) : mn2(mn2(1., util2[c]), util1[c - ld]);
+        vtotn[c] = vtotn[c] + vflux2[c] * (1. - clip);
+        vflux[c] = vflux2[c] * clip;
+        vflxk[c] = vflxk[c] + vflux[c];
+      }
+    }
+    margin = mbdy - 4; /* loop 15, :480-498 */
+    dmin = 999.;
+    for (int j = 1 - margin; j <= jj + margin; j++) {
+      double dpmin = 999.;
+      for (int i = 1 - margin; i <= ii + margin; i++) {
+        size_t c = P(g, i, j);
+        if (ip[c] == 0) continue;
+        dk[c] = dk[c] - ((uflux[c + 1] - uflux[c]) + (vflux[c + ld] - vflux[c])) * p->delt1 * scp2i[c];
+        PK(k + 1)[c] = PK(k)[c] + dk[c];
+        dpmin = mn2(dpmin, dk[c]);
+      }
+      if (j >= 1 && j <= jj) dmin = mn2(dmin, dpmin);
+    }
+    dpkmin[k + kk] = dmin;
+  }
+  int rc = HYO_OK;
+  if (p->nstep % 3 == 0) { /* :520-580: only the fatal part changes the run */
+    double mn = dpkmin[kk];
+    for (int k = kk + 1; k < 2 * kk; k++) mn = mn2(mn, dpkmin[k]);
+    if (mn < dpfatal * onem) rc = HYO_ERR_NEGDP;
+  }
+  if (dpkmin_out) memcpy(dpkmin_out, dpkmin, sizeof(double) * 2 * kk);
+  if (rc == HYO_OK && !p->btrmas) {
+    for (int k = 0; k < kk; k++) { /* loop 77 */
+      double *dk = DPK(k, nn), *uflxk = uflx + (size_t)k * sl, *vflxk = vflx + (size_t)k * sl;
+      margin = mbdy - 5;
+      for (int j = 1 - margin; j <= jj + margin; j++) {
+        for (int i = 1 - margin; i <= ii + margin; i++) {
+          size_t c = P(g, i, j);
+          if (iu[c] == 0) continue;
+          double q = utotn[c] >= 0. ? dk[c - 1] / PK(kk)[c - 1] : dk[c] / PK(kk)[c];
+          uflux[c] = utotn[c] * q;
+          uflxk[c] = uflxk[c] + uflux[c];
+        }
+        for (int i = 1 - margin; i <= ii + margin; i++) {
+          size_t c = P(g, i, j);
+          if (iv[c] == 0) continue;
+          double q = vtotn[c] >= 0. ? dk[c - ld] / PK(kk)[c - ld] : dk[c] / PK(kk)[c];
+          vflux[c] = vtotn[c] * q;
+          vflxk[c] = vflxk[c] + vflux[c];
+        }
+      }
+      margin = mbdy - 6;
+      for (int j = 1 - margin; j <= jj + margin; j++)
+        for (int i = 1 - margin; i <= ii + margin; i++) {
+          size_t c = P(g, i, j);
+          if (ip[c] == 0) continue;
+          dk[c] = dk[c] - ((uflux[c + 1] - uflux[c]) + (vflux[c + ld] - vflux[c])) * p->delt1 * scp2i[c];
+          PK(k + 1)[c] = PK(k)[c] + dk[c];
+        }
+    }
+    margin = mbdy - 6; /* bottom-pressure restoring, :709-735 */
+    for (int j = 1 - margin; j <= jj + margin; j++)
+      for (int i = 1 - margin; i <= ii + margin; i++) {
+        size_t c = P(g, i, j);
+        if (ip[c] == 0) continue;
+        double q = pbot[c] / PK(kk)[c];
+        for (int k = 0; k < kk; k++) {
+          DPK(k, nn)[c] = DPK(k, nn)[c] * q;
+          PK(k + 1)[c] = PK(k)[c] + DPK(k, nn)[c];
+        }
+      }
+  }
+  if (rc == HYO_OK && (p->thkdf4 || p->thkdf2)) { /* loops 13 (biharmonic) and 113 (Laplacian) */
+    const double *thu = a[HYO_C_THKDFU], *thv = a[HYO_C_THKDFV];
+    for (int pass = 0; pass < 2; pass++) {
+      const int bih = pass == 0;
+      if (bih ? !p->thkdf4 : !p->thkdf2) continue;
+      hyo_xctilr(g, dp + (size_t)nn * kk * sl, kk, 6, 6);
+      hyo_xctilr(g, pp + sl, kk, 6, 6);
+      const double dtinv = 1. / p->delt1;
+      const int iflip = p->nstep % 2;
+      margin = mbdy;
+      for (int j = 1 - margin; j <= jj + margin; j++)
+        for (int i = 1 - margin; i <= ii + margin; i++) {
+          size_t c = P(g, i, j);
+          if (iu[c] != 0) uflux[c] = 0.;
+          if (iv[c] != 0) vflux[c] = 0.;
+          if (ip[c] != 0) {
+            if (!bih) vflux[c] = 0.; /* :1005 */
+            pold[c] = iflip == 1 ? PK(kk)[c] : 0.;
+          }
+        }
+      const int k0 = bih ? (iflip ? kk : 2) : 2, k1 = bih ? (iflip ? 2 : kk) : kk, dk_ = bih ? (iflip ? -1 : 1) : 1;
+      for (int k = k0;; k += dk_) { /* k 1-based; p(:,:,k) = PK(k-1) */
+        const double *pk = PK(k - 1), *ptop = PK(kk);
+        const double *dk = DPK(k - 1, nn), *dkm = DPK(k - 2, nn);
+        if (bih) {
+          margin = mbdy - 1; /* :790-830 */
+          for (int j = 1 - margin; j <= jj + margin; j++)
+            for (int i = 1 - margin; i <= ii + margin; i++) {
+              size_t c = P(g, i, j);
+              if (ip[c] == 0) continue;
+              if (mn2(dk[c], dkm[c]) < onecm) {
+                util1[c] = 0.0;
+                util2[c] = 0.0;
+              } else {
+                const size_t ca = c + nbx(g, i, j, -1, 0) * -1, cb = c + nbx(g, i, j, 1, 0),
+                             cja = c + (size_t)(nbx(g, i, j, 0, -1) * -ld), cjb = c + (size_t)(nbx(g, i, j, 0, 1) * ld);
+                util1[c] = pk[c] - .5 * (pk[ca] + pk[cb]);
+                util2[c] = pk[c] - .5 * (pk[cja] + pk[cjb]);
+                if (util1[c] > 0.0) {
+                  if (mn2(dk[ca], dk[cb]) < onecm) util1[c] = 0.0;
+                } else {
+                  if (mn2(dkm[ca], dkm[cb]) < onecm) util1[c] = 0.0;
+                }
+                if (util2[c] > 0.0) {
+                  if (mn2(dk[cja], dk[cjb]) < onecm) util2[c] = 0.0;
+                } else {
+                  if (mn2(dkm[cja], dkm[cjb]) < onecm) util2[c] = 0.0;
+                }
+              }
+            }
+        }
+        margin = mbdy - 2; /* :838-900 and :1030-1060 */
+        double *uk1 = uflx + (size_t)(k - 2) * sl, *uk = uflx + (size_t)(k - 1) * sl;
+        double *vk1 = vflx + (size_t)(k - 2) * sl, *vk = vflx + (size_t)(k - 1) * sl;
+        for (int j = 1 - margin; j <= jj + margin; j++) {
+          for (int i = 1 - margin; i <= ii + margin; i++) {
+            size_t c = P(g, i, j);
+            if (iu[c] == 0) continue;
+            double flxhi = .25 * (ptop[c] - pk[c]) * scp2[c];
+            double flxlo = -.25 * (ptop[c - 1] - pk[c - 1]) * scp2[c - 1];
+            if (bih) {
+              if (iflip == 0) {
+                flxhi = mn2(flxhi, uflux[c] + .25 * (pk[c - 1] - pold[c - 1]) * scp2[c - 1]);
+                flxlo = mx2(flxlo, uflux[c] - .25 * (pk[c] - pold[c]) * scp2[c]);
+              } else {
+                flxhi = mn2(flxhi, uflux[c] + .25 * (pold[c] - pk[c]) * scp2[c]);
+                flxlo = mx2(flxlo, uflux[c] - .25 * (pold[c - 1] - pk[c - 1]) * scp2[c - 1]);
+              }
+              const double thkdfu = p->delt1 * thu[c];
+              uflux[c] = mn2(flxhi, mx2(flxlo, thkdfu * (util1[c - 1] - util1[c])));
+            } else {
+              const double thkdfu = p->delt1 * thu[c];
+              uflux[c] = mn2(flxhi, mx2(flxlo, thkdfu * (pk[c - 1] - pk[c])));
+            }
+            uk1[c] = uk1[c] + uflux[c] * dtinv;
+            uk[c] = uk[c] - uflux[c] * dtinv;
+          }
+          for (int i = 1 - margin; i <= ii + margin; i++) {
+            size_t c = P(g, i, j);
+            if (iv[c] == 0) continue;
+            double flxhi = .25 * (ptop[c] - pk[c]) * scp2[c];
+            double flxlo = -.25 * (ptop[c - ld] - pk[c - ld]) * scp2[c - ld];
+            if (bih) {
+              if (iflip == 0) {
+                flxhi = mn2(flxhi, vflux[c] + .25 * (pk[c - ld] - pold[c - ld]) * scp2[c - ld]);
+                flxlo = mx2(flxlo, vflux[c] - .25 * (pk[c] - pold[c]) * scp2[c]);
+              } else {
+                flxhi = mn2(flxhi, vflux[c] + .25 * (pold[c] - pk[c]) * scp2[c]);
+                flxlo = mx2(flxlo, vflux[c] - .25 * (pold[c - ld] - pk[c - ld]) * scp2[c - ld]);
+              }
+              const double thkdfv = p->delt1 * thv[c];
+              vflux[c] = mn2(flxhi, mx2(flxlo, thkdfv * (util2[c - ld] - util2[c])));
+            } else {
+              const double thkdfv = p->delt1 * thv[c];
+              vflux[c] = mn2(flxhi, mx2(flxlo, thkdfv * (pk[c - ld] - pk[c])));
+            }
+            vk1[c] = vk1[c] + vflux[c] * dtinv;
+            vk[c] = vk[c] - vflux[c] * dtinv;
+          }
+        }
+        margin = mbdy - 2; /* :905-920 */
+        double *pkw = PK(k - 1);
+        for (int j = 1 - margin; j <= jj + margin; j++)
+          for (int i = 1 - margin; i <= ii + margin; i++) {
+            size_t c = P(g, i, j);
+            if (ip[c] == 0) continue;
+            pold[c] = pkw[c];
+            pkw[c] = pkw[c] - ((uflux[c + 1] - uflux[c]) + (vflux[c + ld] - vflux[c])) * scp2i[c];
+          }
+        if (k == k1) break;
+      }
+      margin = mbdy - 2; /* :925-950 */
+      for (int j = 1 - margin; j <= jj + margin; j++)
+        for (int k = 0; k < kk; k++)
+          for (int i = 1 - margin; i <= ii + margin; i++) {
+            size_t c = P(g, i, j);
+            if (ip[c] == 0) continue;
+            if (PK(k + 1)[c] < PK(k)[c]) PK(k + 1)[c] = PK(k)[c];
+            DPK(k, nn)[c] = PK(k + 1)[c] - PK(k)[c];
+          }
+    }
+  }
+  if (rc == HYO_OK) {
+    if (a[HYO_C_UFLXAV] && a[HYO_C_VFLXAV] && a[HYO_C_DPAV]) /* cumulative fluxes, :1326-1348 */
+      for (int j = 1; j <= jj; j++)
+        for (int k = 0; k < kk; k++)
+          for (int i = 1; i <= ii; i++) {
+            size_t c = P(g, i, j), ck = (size_t)k * sl + c;
+            if (iu[c] != 0) a[HYO_C_UFLXAV][ck] = a[HYO_C_UFLXAV][ck] + uflx[ck];
+            if (iv[c] != 0) a[HYO_C_VFLXAV][ck] = a[HYO_C_VFLXAV][ck] + vflx[ck];
+            if (ip[c] != 0) a[HYO_C_DPAV][ck] = a[HYO_C_DPAV][ck] + DPK(k, nn)[c];
+          }
+    if (p->btrmas) { /* :1350-1385 */
+      double *onetacnt = a[HYO_C_ONETACNT];
+      margin = 1;
+      for (int j = 1 - margin; j <= jj + margin; j++)
+        for (int i = 1 - margin; i <= ii + margin; i++) {
+          size_t c = P(g, i, j);
+          if (ip[c] == 0) continue;
+          onetacnt[c] = PK(kk)[c] / pbot[c];
+          if (onetacnt[c] > epsil_cnuity) {
+            const double q = 1.0 / onetacnt[c];
+            for (int k = 0; k < kk; k++) {
+              DPK(k, nn)[c] = DPK(k, nn)[c] * q;
+              PK(k + 1)[c] = PK(k)[c] + DPK(k, nn)[c];
+            }
+          } else {
+            DPK(0, nn)[c] = pbot[c];
+            PK(1)[c] = PK(0)[c] + DPK(0, nn)[c];
+            for (int k = 1; k < kk; k++) {
+              DPK(k, nn)[c] = 0.0;
+              PK(k + 1)[c] = PK(k)[c] + DPK(k, nn)[c];
+            }
+          }
+        }
+    }
+    hyo_xctilr(g, dp + (size_t)nn * kk * sl, kk, 6, 6); /* Robert-Asselin filter of dp, :1387-1410 */
+    margin = mbdy;
+    for (int j = 1 - margin; j <= jj + margin; j++)
+      for (int i = 1 - margin; i <= ii + margin; i++) {
+        size_t c = P(g, i, j);
+        if (ip[c] == 0) continue;
+        for (int k = 0; k < kk; k++) {
+          const double dpold = dpo[((size_t)k + (size_t)nn * kk) * sl + c], dpmid = DPK(k, mm)[c],
+                       dpnew = DPK(k, nn)[c];
+          const double q = 0.5 * p->ra2fac * (dpold + dpnew - 2.0 * dpmid);
+          dpo[((size_t)k + (size_t)mm * kk) * sl + c] = DPK(k, mm)[c];
+          DPK(k, mm)[c] = dpmid + q;
+        }
+      }
+  }
+#undef DPK
+#undef PK
+  free(dpkmin);
+  free(w);
+  return rc;
 }

@@ -50,6 +50,7 @@ def lib():
         L.hyo_asselin_save.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_void_p]
         L.hyo_asselin_filter.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int,
                                          C.c_int, C.c_void_p]
+        L.hyo_cnuity.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, dp]
         L.hyo_sig.restype = C.c_double
         L.hyo_sig.argtypes = [C.c_double, C.c_double]
         L.hyo_xcsum.restype = C.c_double
@@ -183,6 +184,33 @@ class Grid:
         if rc != 0:
             raise OracleError(f"asselin_filter rc={rc}")
 
+    def cnuity(self, m: int, n: int, arrays: dict, *, delt1: float, nstep: int = 1, btrmas: bool = False,
+               thkdf4: bool = False, thkdf2: bool = False, ra2fac: float = 0.125):
+        """cnuity(m,n) (cnuity.F90) on the arrays named as in CNUITY_ARRAYS
+        (numpy, reference layout; inputs' halos are refreshed in place).
+        Returns dpkmin (2*kdm: after the low-order and the antidiffusive
+        update of each layer); raises OracleError(-9) on a fatal negative
+        thickness (checked when nstep % 3 == 0)."""
+        kdm = arrays["dp"].shape[1]
+        for k, v in arrays.items():
+            if k not in CNUITY_ARRAYS:
+                raise KeyError(k)
+            if v is not None and not (v.flags["C_CONTIGUOUS"] and v.dtype == np.float64):
+                raise OracleError(f"{k}: need C-contiguous float64")
+        ptrs = (C.c_void_p * len(CNUITY_ARRAYS))()
+        for i, k in enumerate(CNUITY_ARRAYS):
+            v = arrays.get(k)
+            ptrs[i] = None if v is None else v.ctypes.data
+        p = _CnParams(kdm=kdm, nstep=nstep, btrmas=int(btrmas), thkdf4=int(thkdf4), thkdf2=int(thkdf2),
+                      delt1=float(delt1), ra2fac=float(ra2fac))
+        dpkmin = np.zeros(2 * kdm)
+        rc = lib().hyo_cnuity(self._h, C.byref(p), m, n, ptrs, _p(dpkmin))
+        if rc != 0:
+            err = OracleError(f"cnuity rc={rc}")
+            err.code = rc
+            raise err
+        return dpkmin
+
     def tsdff(self, m: int, n: int, *, temp, saln, th3d, dp, oneta, aspux, aspvy, scuy, scvx, delt1, temdf2,
               temdfc=1.0, thbase=34.0, tracer=None, q2=None, q2l=None, advflg=0, nhybrd=None, isopyc=False):
         """The diffusion block of tsadvc(m,n) (mod_tsadvc.F90:2138-2230),
@@ -216,6 +244,16 @@ def _assel_ptrs(arrs: dict):
         v = arrs.get(k)
         ptrs[i] = None if v is None else v.ctypes.data
     return ptrs
+
+
+CNUITY_ARRAYS = ("dp", "dpo", "dpu", "dpv", "u", "v", "ubavg", "vbavg", "pbot", "depthu", "depthv", "oneta", "scuy",
+                 "scvx", "thkdfu", "thkdfv", "p", "uflx", "vflx", "uflxav", "vflxav", "dpav", "onetacnt")
+ERR_NEGDP = -9
+
+
+class _CnParams(C.Structure):
+    _fields_ = [("kdm", C.c_int), ("nstep", C.c_int), ("btrmas", C.c_int), ("thkdf4", C.c_int), ("thkdf2", C.c_int),
+                ("delt1", C.c_double), ("ra2fac", C.c_double)]
 
 
 def sig(t: float, s: float) -> float:

@@ -75,3 +75,58 @@ def oneta_field(b, seed):
     """oneta(ld1,ld2,2) = 1 + pbavg/pbot, a few percent from 1."""
     rng = np.random.default_rng(seed + 1)
     return np.ascontiguousarray(1.0 + 0.02 * noise(b, rng, (2, b.ld2, b.ld1)))
+
+
+def cnuity_case(b, g, kdm=3, seed=81, delt1=1800.0, umax=0.5, btrmas=False, thkdf=False):
+    """Inputs of cnuity(m,n) in the reference layout (numpy): thicknesses of
+    both levels, u-/v-point thicknesses and velocities of level m, barotropic
+    velocities, the bottom pressure and u/v-point depths, the interface
+    pressures p(:,:,1:kdm+1) and the metrics.  Velocities reach umax m/s, so
+    the Courant number is umax*delt1/1e4."""
+    rng = np.random.default_rng(seed)
+    sh = (b.ld2, b.ld1)
+    ip = g.masks["ip"] != 0
+    onem = 9.806 / (1.0 / 1000.0)
+
+    def smooth(amp, shape):
+        return amp * noise(b, rng, shape)
+
+    dp = np.zeros((2, kdm) + sh)
+    for k in range(kdm):
+        dp[0, k] = (20.0 + 5.0 * k) * onem * (1.0 + 0.2 * np.tanh(smooth(1.0, sh)))
+    dp[1] = dp[0] * (1.0 + 0.01 * np.tanh(smooth(1.0, (kdm,) + sh)))
+    dp *= ip
+    pbot = dp[0].sum(axis=0)
+    c = {"dp": np.ascontiguousarray(dp)}
+    c["dpo"] = np.zeros((2, kdm) + sh)
+    dpu = np.zeros((2, kdm) + sh)
+    dpv = np.zeros((2, kdm) + sh)
+    dpu[..., 1:] = 0.5 * (dp[..., 1:] + dp[..., :-1])
+    dpv[..., 1:, :] = 0.5 * (dp[..., 1:, :] + dp[..., :-1, :])
+    c["dpu"], c["dpv"] = dpu * (g.masks["iu"] != 0), dpv * (g.masks["iv"] != 0)
+    c["u"] = np.ascontiguousarray(smooth(umax * 0.6, (2, kdm) + sh) * (g.masks["iu"] != 0))
+    c["v"] = np.ascontiguousarray(smooth(umax * 0.6, (2, kdm) + sh) * (g.masks["iv"] != 0))
+    c["ubavg"] = np.ascontiguousarray(smooth(umax * 0.3, (3,) + sh) * (g.masks["iu"] != 0))
+    c["vbavg"] = np.ascontiguousarray(smooth(umax * 0.3, (3,) + sh) * (g.masks["iv"] != 0))
+    c["pbot"] = np.ascontiguousarray(pbot)
+    du = np.zeros(sh)
+    dv = np.zeros(sh)
+    du[:, 1:] = np.minimum(pbot[:, 1:], pbot[:, :-1])
+    dv[1:, :] = np.minimum(pbot[1:, :], pbot[:-1, :])
+    c["depthu"], c["depthv"] = du, dv
+    c["oneta"] = np.ascontiguousarray(1.0 + 0.01 * noise(b, rng, (2,) + sh)) if btrmas else None
+    c["scuy"] = np.full(sh, 1.0e4)
+    c["scvx"] = np.full(sh, 1.0e4)
+    if thkdf:
+        c["thkdfu"] = np.full(sh, 0.02 * 1.0e4 ** 3 / 1.0e8 * 0.05)
+        c["thkdfv"] = np.full(sh, 0.02 * 1.0e4 ** 3 / 1.0e8 * 0.05)
+    p = np.zeros((kdm + 1,) + sh)
+    p[1:] = np.cumsum(dp[0], axis=0)
+    c["p"] = p
+    c["uflx"] = np.zeros((kdm,) + sh)
+    c["vflx"] = np.zeros((kdm,) + sh)
+    c["uflxav"] = np.zeros((kdm,) + sh)
+    c["vflxav"] = np.zeros((kdm,) + sh)
+    c["dpav"] = np.zeros((kdm,) + sh)
+    c["onetacnt"] = np.zeros(sh) if btrmas else None
+    return {k: (None if v is None else np.ascontiguousarray(v)) for k, v in c.items()}

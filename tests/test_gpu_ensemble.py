@@ -353,3 +353,36 @@ def test_mixed_mpdata_needs_strip_kernel(cuda):
     assert tx == 56
     ens.step(1, DELT1, 1)
     ens.close()
+
+
+def test_get_async_overlaps_and_equals_get(cuda):
+    """hyc_ens_get_async: after wait() the host buffers hold what a synchronous
+    get returns, for outputs of consecutive steps whose copies overlap the
+    next step's puts; pinned host memory and device destinations."""
+    import torch
+
+    members = make_members(SPECS[:2])
+    ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
+    load(ens, members)
+    outs, want = [], []
+    for s in range(3):
+        ens.step(2, DELT1, 1)
+        for i, m in enumerate(members):
+            shape = (m["ntr"] * m["kdm"], m["b"].ld2, m["b"].ld1)
+            pinned = torch.zeros(shape, dtype=torch.float64).pin_memory()
+            dev = torch.zeros(shape, dtype=torch.float64, device=cuda)
+            ens.get_async(i, "cur", pinned)
+            ens.get_async(i, "cur", dev)
+            ref = np.zeros(shape)
+            ens.get(i, "cur", ref)
+            outs.append((pinned, dev))
+            want.append(ref)
+        for i, m in enumerate(members):  # re-put the inputs while the copies run
+            c = m["c"]
+            ens.put(i, "uflx", np.ascontiguousarray(c["uflx"]))
+    ens.wait()
+    torch.cuda.synchronize()
+    for (pinned, dev), ref in zip(outs, want):
+        assert np.array_equal(pinned.numpy(), ref)
+        assert np.array_equal(dev.cpu().numpy(), ref)
+    ens.close()
