@@ -464,6 +464,107 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
     return res
 
 
+THKDF4 = 0.02  # biharmonic interface-diffusion velocity (m/s), a typical blkdat thkdf4
+
+
+def run_cnuity(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local):
+    """cnuity (hyc_cnuity, FP64) on the workload's basin, resident fields,
+    K steps after W warm-up steps: the layer thicknesses of the tsadvc case,
+    velocities u = uflx/(dpu*scuy) (so the Courant number is the case's),
+    ubavg = vbavg = 0, pbot = the column, biharmonic interface diffusion
+    thkdf4*dx^3, not btrmas, ra2fac = RA2FAC."""
+    import numpy as np
+    import torch
+
+    import hycadv
+
+    kdm = wl["kdm"]
+    ctx = hycadv.Context.from_masks(masks, sc, si, kdm=kdm, nreg=nreg, nbdy=b.nbdy, device=local)
+    ctx.set_stream(stream)
+    f64 = dict(dtype=torch.float64, device=dev)
+    iu = torch.from_numpy(np.asarray(masks["iu"]) != 0).to(dev)
+    iv = torch.from_numpy(np.asarray(masks["iv"]) != 0).to(dev)
+    dx = float(np.sqrt(np.asarray(sc, dtype=np.float64)).max())
+    dp = case.dp
+    f = {"dp": dp, "dpo": torch.zeros_like(dp)}
+    dpu = torch.zeros_like(dp)
+    dpv = torch.zeros_like(dp)
+    dpu[..., 1:] = 0.5 * (dp[..., 1:] + dp[..., :-1])
+    dpv[..., 1:, :] = 0.5 * (dp[..., 1:, :] + dp[..., :-1, :])
+    dpu *= iu
+    dpv *= iv
+    f["dpu"], f["dpv"] = dpu, dpv
+    u = torch.zeros_like(dp)
+    v = torch.zeros_like(dp)
+    for t in range(2):
+        u[t] = torch.where(iu, case.uflx / (dpu[0].clamp(min=1.0) * dx), 0.0)
+        v[t] = torch.where(iv, case.vflx / (dpv[0].clamp(min=1.0) * dx), 0.0)
+    f["u"], f["v"] = u, v
+    sh = tuple(dp.shape[-2:])
+    f["ubavg"] = torch.zeros((3,) + sh, **f64)
+    f["vbavg"] = torch.zeros((3,) + sh, **f64)
+    pbot = dp[0].sum(dim=0)
+    f["pbot"] = pbot
+    p = torch.zeros((kdm + 1,) + sh, **f64)
+    p[1:] = torch.cumsum(dp[0], dim=0)
+    f["p"] = p
+    f["uflx"] = torch.zeros((kdm,) + sh, **f64)
+    f["vflx"] = torch.zeros((kdm,) + sh, **f64)
+    for k, t in f.items():
+        ctx.bind(k, t)
+    pb = pbot.cpu().numpy()
+    du = np.zeros_like(pb)
+    dv = np.zeros_like(pb)
+    du[:, 1:] = np.minimum(pb[:, 1:], pb[:, :-1])
+    dv[1:, :] = np.minimum(pb[1:, :], pb[:-1, :])
+    dxa = np.sqrt(np.asarray(sc, dtype=np.float64))
+    th = THKDF4 * dxa ** 3
+    ctx.set_cnuity_grid(dxa, dxa, du, dv, th, th)
+    del iu, iv
+
+    def step(s):
+        m, n = ((s + 1) % 2) + 1, (s % 2) + 1
+        ctx.cnuity(m, n, delt1=wl["delt1"], nstep=s, thkdf=4, ra2fac=RA2FAC)
+
+    for s in range(1, args.warmup + 1):
+        step(s)
+    torch.cuda.synchronize(dev)
+    ctx.enable_timers(True)
+    ctx.stats(reset=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for s in range(args.warmup + 1, args.warmup + args.steps + 1):
+            step(s)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    st = ctx.stats(reset=True)
+    ctx.close()
+    del f
+    torch.cuda.empty_cache()
+    ws = dist.get_world_size() if dist else 1
+    cells = wl["nx"] * wl["ny"] * kdm
+    # algorithmic bytes per cell and layer: read dp(n), dp(m), u, v, dpu, dpv;
+    # write dp(n), dp(m), dpo(n), dpo(m), uflx, vflx, p (FP64)
+    bpc = 13 * 8
+    peak, peak_kind = peak_hbm()
+    achieved = cells * bpc / (ms / args.steps / 1e3) / 1e9
+    return {"value": ws * cells * args.steps / (ms / 1e3), "unit": "cell·layer updates/s",
+            "ms_per_step": ms / args.steps, "gpu_launches": int(st["launches"]), "clocks": clk.summary(),
+            "config": "FCT continuity + barotropic restoration + bottom restoring + biharmonic interface "
+                      "diffusion + RA of dp, FP64, bit-identical to the oracle",
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "kernel": "cnuity sweeps (cn_*)",
+                         "algorithmic_bytes_per_cell_layer": bpc,
+                         "traffic": profile_traffic(f"cnuity_fp64_{args.workload}")}}
+
+
 def run_e2e(args, wl, b, spec, case, form, tile, nq, dev, stream, dist):
     """The headline form end to end through the C ABI with host buffers: per
     step hyc_ens_put of T and S (levels t-1 and t), uflx, vflx and dp from
@@ -993,11 +1094,11 @@ def main():
     ap.add_argument("--form", default="mixed-fp32prep", choices=sorted(ENS_FORMS),
                     help="headline form (ensemble API): FP32-mixed with FP64 thickness prep, with compensated "
                          "FP32 prep, or FP64")
-    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-full,fp64,mixed,mixed-fp32prep",
+    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-full,cnuity,fp64,mixed,mixed-fp32prep",
                     help="forms measured beside the headline (tsadvc[-fct4|-mpdata|-pcm] = FP64 plain through "
                          "hyc_tsadvc, FCT2 unless named; tsadvc-full = asselin_save + tsadvc + its "
-                         "diffusion + asselin_filter)")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+                         "diffusion + asselin_filter; cnuity = the continuity equation)")
+    ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--c4-steps", type=int, default=100, help="c4: steps per basin")
     ap.add_argument("--tile", default="", help="mixed forms: fixed tile 'tx,ty,tracers_per_pass' instead of the tuner")
     ap.add_argument("--ref-layers", type=int, default=4, help="layers in the CPU sample")
@@ -1054,6 +1155,8 @@ def main():
     if "tsadvc-full" in others:
         schemes["tsadvc-full"] = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local,
                                                  2, full=True)
+    if "cnuity" in others:
+        schemes["cnuity"] = run_cnuity(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local)
     ens_forms = [f for f in others if f in ENS_FORMS and f != args.form]
     if "fp64" in ens_forms:  # the reference of the error checks runs first
         ens_forms = ["fp64"] + [f for f in ens_forms if f != "fp64"]

@@ -29,6 +29,7 @@ UNITS = {
     "hyc_fct2c.cu": ["-lineinfo", "-fmad=false"],
     "hyc_tsdff.cu": ["-lineinfo", "-fmad=false"],
     "hyc_asselin.cu": ["-lineinfo", "-fmad=false"],
+    "hyc_cnuity.cu": ["-lineinfo", "-fmad=false"],
     "hyc_host.cpp": [],
     "hyc_noalloc.cu": ["-lineinfo"],
     "hyc_mixed.cu": ["-lineinfo"],

@@ -97,6 +97,26 @@ struct AsselinArgs {
   double *otemp, *osaln, *oth3d, *otracer, *oq2, *oq2l;  // t-1 copies
 };
 
+// Continuity equation (cnuity.F90), see hyc_cnuity.cu; arrays in the
+// reference layout (mod_cb_arrays.F90)
+struct CnuityArgs {
+  int ii, jj, nb, ld1, ld2, nreg;
+  long long slice;
+  int kdm, m, n, nstep, btrmas, thk;  // thk: 0 none, 4 biharmonic, 2 Laplacian interface diffusion
+  const uint8_t *msk;
+  const double *scp2, *scp2i, *scuy, *scvx, *depthu, *depthv, *thkdfu, *thkdfv, *pbot, *oneta;
+  const double *u, *v, *dpu, *dpv;  // (ld1,ld2,kdm,2)
+  const double *ubavg, *vbavg;      // (ld1,ld2,3)
+  double *dp, *dpo;                 // (ld1,ld2,kdm,2)
+  double *p;                        // (ld1,ld2,kdm+1)
+  double *uflx, *vflx;              // (ld1,ld2,kdm)
+  double *uflxav, *vflxav, *dpav;   // (ld1,ld2,kdm) or null
+  double *onetacnt;                 // (ld1,ld2), btrmas
+  double delt1, ra2fac;
+  double *w;                        // work slices
+  long long *keys;                  // 2*kdm dpkmin keys, or null
+};
+
 template <int TX, int TY>
 struct TileGeom {
   static constexpr int RX = TX + 6, RY = TY + 6, N = RX * RY;

@@ -40,6 +40,10 @@ struct hyc_ctx {
   uint8_t *d_msk = nullptr;
   double *d_scp2 = nullptr, *d_scp2i = nullptr;
   double *d_diff = nullptr;     // aspux, aspvy, scuy, scvx (4 slices), hyc_set_diffusion_grid
+  double *d_cngrid = nullptr;   // scuy, scvx, depthu, depthv, thkdfu, thkdfv (6 slices), hyc_set_cnuity_grid
+  bool cn_thkdf = false;        // thkdfu/thkdfv were given
+  double *d_cnw = nullptr;      // cnuity work slices
+  long long *d_cnkeys = nullptr;  // cnuity dpkmin keys (2*kdm)
   Field fields[HYC_NFIELDS];
   double *d_scratch = nullptr;  // advem output slices (fields x layers)
   size_t scratch_elems = 0;
@@ -403,6 +407,9 @@ int hyc_adv_finalize(hyc_ctx *c) {
     cudaFree(c->d_scp2);
     cudaFree(c->d_scp2i);
     cudaFree(c->d_diff);
+    cudaFree(c->d_cngrid);
+    cudaFree(c->d_cnw);
+    cudaFree(c->d_cnkeys);
     cudaFree(c->d_scratch);
     cudaFree(c->d_fct2c);
     cudaFree(c->d_tmp);
@@ -1006,6 +1013,155 @@ int hyc_asselin_filter(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params
   Timed t(c, HYC_T_ASSELIN);
   CK(hyc::launch_asselin(a, true, c->stream), "asselin_filter");
   c->stats.launches += 1;
+  return HYC_OK;
+}
+
+int hyc_set_cnuity_grid(hyc_ctx *c, const double *scuy, const double *scvx, const double *depthu, const double *depthv,
+                        const double *thkdfu, const double *thkdfv) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (!scuy || !scvx || !depthu || !depthv || (!thkdfu != !thkdfv))
+    return fail(c, HYC_ERR_ARG, "hyc_set_cnuity_grid: null array");
+  DeviceGuard g(c->device);
+  const size_t sl = (size_t)c->slice;
+  if (!c->d_cngrid) CK(cudaMalloc(&c->d_cngrid, 6 * sl * sizeof(double)), "malloc cnuity grid");
+  const double *src[6] = {scuy, scvx, depthu, depthv, thkdfu, thkdfv};
+  for (int q = 0; q < 6; q++)
+    if (src[q])
+      CK(cudaMemcpyAsync(c->d_cngrid + q * sl, src[q], sl * 8, cudaMemcpyHostToDevice, c->stream), "cnuity grid");
+  CK(cudaStreamSynchronize(c->stream), "cnuity grid sync");
+  c->cn_thkdf = thkdfu != nullptr;
+  return HYC_OK;
+}
+
+int hyc_cnuity(hyc_ctx *c, int32_t m, int32_t n, const hyc_cnuity_params *p, double *dpkmin) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  if (!p || m < 1 || m > 2 || n < 1 || n > 2) return fail(c, HYC_ERR_ARG, "hyc_cnuity: bad m/n/params");
+  if (p->isopyc) return fail(c, HYC_ERR_UNSUPPORTED, "isopycnic (nhybrd=0) mode is not supported");
+  if (p->thkdf != 0 && p->thkdf != 2 && p->thkdf != 4) return fail(c, HYC_ERR_ARG, "thkdf must be 0, 2 or 4");
+  if (c->nbdy < 6) return fail(c, HYC_ERR_NBDY, "cnuity needs nbdy >= 6 (its halo is 6 wide)");
+  if (!c->d_cngrid) return fail(c, HYC_ERR_FIELD, "hyc_cnuity: call hyc_set_cnuity_grid first");
+  if (p->thkdf && !c->cn_thkdf) return fail(c, HYC_ERR_FIELD, "hyc_cnuity: interface diffusion without thkdfu/thkdfv");
+  const int kk = c->kdm;
+  const long long sl = c->slice;
+  Field *F = c->fields;
+  auto need = [&](int id, int64_t nel, const char *name) -> int {
+    if (!F[id].dev) return fail(c, HYC_ERR_FIELD, "field %s is not bound", name);
+    if (F[id].nelem < nel) return fail(c, HYC_ERR_FIELD, "field %s has %lld elements, needs %lld", name,
+                                       (long long)F[id].nelem, (long long)nel);
+    return HYC_OK;
+  };
+  int rc;
+  if ((rc = need(HYC_F_DP, 2LL * kk * sl, "dp")) || (rc = need(HYC_F_DPO, 2LL * kk * sl, "dpo")) ||
+      (rc = need(HYC_F_U, 2LL * kk * sl, "u")) || (rc = need(HYC_F_V, 2LL * kk * sl, "v")) ||
+      (rc = need(HYC_F_DPU, 2LL * kk * sl, "dpu")) || (rc = need(HYC_F_DPV, 2LL * kk * sl, "dpv")) ||
+      (rc = need(HYC_F_UBAVG, 3LL * sl, "ubavg")) || (rc = need(HYC_F_VBAVG, 3LL * sl, "vbavg")) ||
+      (rc = need(HYC_F_PBOT, sl, "pbot")) || (rc = need(HYC_F_P, (long long)(kk + 1) * sl, "p")) ||
+      (rc = need(HYC_F_UFLX, (long long)kk * sl, "uflx")) || (rc = need(HYC_F_VFLX, (long long)kk * sl, "vflx")))
+    return rc;
+  if (p->btrmas && ((rc = need(HYC_F_ONETA, 2LL * sl, "oneta")) || (rc = need(HYC_F_ONETACNT, sl, "onetacnt"))))
+    return rc;
+  const bool cumul = F[HYC_F_UFLXAV].dev && F[HYC_F_VFLXAV].dev && F[HYC_F_DPAV].dev;
+  if (cumul && ((rc = need(HYC_F_UFLXAV, (long long)kk * sl, "uflxav")) ||
+                (rc = need(HYC_F_VFLXAV, (long long)kk * sl, "vflxav")) ||
+                (rc = need(HYC_F_DPAV, (long long)kk * sl, "dpav"))))
+    return rc;
+  DeviceGuard g(c->device);
+  cudaStream_t s = c->stream;
+  const size_t nw = hyc::cnuity_work_slices();
+  if (!c->d_cnw) {
+    CK(cudaMalloc(&c->d_cnw, nw * sl * sizeof(double)), "malloc cnuity work");
+    CK(cudaMemsetAsync(c->d_cnw, 0, nw * sl * sizeof(double), s), "cnuity work");
+  }
+  const bool want_keys = dpkmin || p->nstep % 3 == 0;
+  if (want_keys) {
+    if (!c->d_cnkeys) CK(cudaMalloc(&c->d_cnkeys, 2 * kk * sizeof(long long)), "malloc keys");
+    std::vector<long long> k0(2 * kk, hyc::double_to_key(999.));  // dpmin = 999. (:296, :482)
+    CK(cudaMemcpyAsync(c->d_cnkeys, k0.data(), k0.size() * sizeof(long long), cudaMemcpyHostToDevice, s), "keys");
+  }
+  Timed t_all(c, HYC_T_CNUITY);
+  const int mm = m - 1;
+  // halos, cnuity.F90:100-107 (dpmixl is not carried)
+  struct H {
+    double *a;
+    int nlev;
+  } halos[] = {{F[HYC_F_DP].dev, 2 * kk},
+               {F[HYC_F_DPU].dev + (long long)mm * kk * sl, kk},
+               {F[HYC_F_DPV].dev + (long long)mm * kk * sl, kk},
+               {F[HYC_F_U].dev + (long long)mm * kk * sl, kk},
+               {F[HYC_F_V].dev + (long long)mm * kk * sl, kk},
+               {F[HYC_F_UBAVG].dev + (long long)mm * sl, 1},
+               {F[HYC_F_VBAVG].dev + (long long)mm * sl, 1}};
+  for (auto &h : halos) {
+    CK(hyc::launch_xctilr(h.a, sl, h.nlev, c->idm, c->jdm, c->nbdy, c->ld1, 6, 6, c->nreg, s), "xctilr");
+    c->stats.launches += 1;
+  }
+  hyc::CnuityArgs a;
+  memset(&a, 0, sizeof a);
+  a.ii = c->idm;
+  a.jj = c->jdm;
+  a.nb = c->nbdy;
+  a.ld1 = c->ld1;
+  a.ld2 = c->ld2;
+  a.nreg = c->nreg;
+  a.slice = sl;
+  a.kdm = kk;
+  a.m = m;
+  a.n = n;
+  a.nstep = p->nstep;
+  a.btrmas = p->btrmas ? 1 : 0;
+  a.thk = p->thkdf;
+  a.msk = c->d_msk;
+  a.scp2 = c->d_scp2;
+  a.scp2i = c->d_scp2i;
+  a.scuy = c->d_cngrid;
+  a.scvx = c->d_cngrid + sl;
+  a.depthu = c->d_cngrid + 2 * sl;
+  a.depthv = c->d_cngrid + 3 * sl;
+  a.thkdfu = c->d_cngrid + 4 * sl;
+  a.thkdfv = c->d_cngrid + 5 * sl;
+  a.pbot = F[HYC_F_PBOT].dev;
+  a.oneta = F[HYC_F_ONETA].dev;
+  a.u = F[HYC_F_U].dev;
+  a.v = F[HYC_F_V].dev;
+  a.dpu = F[HYC_F_DPU].dev;
+  a.dpv = F[HYC_F_DPV].dev;
+  a.ubavg = F[HYC_F_UBAVG].dev;
+  a.vbavg = F[HYC_F_VBAVG].dev;
+  a.dp = F[HYC_F_DP].dev;
+  a.dpo = F[HYC_F_DPO].dev;
+  a.p = F[HYC_F_P].dev;
+  a.uflx = F[HYC_F_UFLX].dev;
+  a.vflx = F[HYC_F_VFLX].dev;
+  if (cumul) {
+    a.uflxav = F[HYC_F_UFLXAV].dev;
+    a.vflxav = F[HYC_F_VFLXAV].dev;
+    a.dpav = F[HYC_F_DPAV].dev;
+  }
+  a.onetacnt = F[HYC_F_ONETACNT].dev;
+  a.delt1 = p->delt1;
+  a.ra2fac = p->ra2fac;
+  a.w = c->d_cnw;
+  a.keys = want_keys ? c->d_cnkeys : nullptr;
+  int nl = 0;
+  CK(hyc::launch_cnuity_layers(a, &nl, s), "cnuity loop 76");
+  std::vector<long long> keys(want_keys ? 2 * kk : 0);
+  if (want_keys) {
+    CK(cudaMemcpyAsync(keys.data(), c->d_cnkeys, keys.size() * sizeof(long long), cudaMemcpyDeviceToHost, s), "keys");
+    CK(cudaStreamSynchronize(s), "keys sync");
+    if (dpkmin)
+      for (int k = 0; k < 2 * kk; k++) dpkmin[k] = hyc::key_to_double(keys[k]);
+  }
+  if (p->nstep % 3 == 0) {  // cnuity.F90:574-580
+    const double onem = 9.806 / (1.0 / 1000.0), dpfatal = -10.0;
+    double mn = hyc::key_to_double(keys[kk]);
+    for (int k = kk + 1; k < 2 * kk; k++) mn = std::min(mn, hyc::key_to_double(keys[k]));
+    if (mn < dpfatal * onem) {
+      c->stats.launches += nl;
+      return fail(c, HYC_ERR_NEGDP, "cnuity: neg. dp (m) < %g (minimum %g m)", dpfatal, mn / onem);
+    }
+  }
+  CK(hyc::launch_cnuity_rest(a, &nl, s), "cnuity");
+  c->stats.launches += nl;
   return HYC_OK;
 }
 

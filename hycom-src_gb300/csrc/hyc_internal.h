@@ -40,6 +40,12 @@ cudaError_t launch_tsdff(const TsdffArgs &a, cudaStream_t s);
 struct AsselinArgs;
 cudaError_t launch_asselin(const AsselinArgs &a, bool filter, cudaStream_t s);
 
+// Continuity equation: work slices, loop 76 (all layers), then the rest
+struct CnuityArgs;
+size_t cnuity_work_slices();
+cudaError_t launch_cnuity_layers(const CnuityArgs &a, int *launches, cudaStream_t s);
+cudaError_t launch_cnuity_rest(const CnuityArgs &a, int *launches, cudaStream_t s);
+
 // xctilr on nlev slices (mod_xc_sm.h:1337-1428).
 cudaError_t launch_xctilr(double *a, long long slice, int nlev, int ii, int jj, int nbdy, int ld1, int mh,
                           int nh, int nreg, cudaStream_t s);

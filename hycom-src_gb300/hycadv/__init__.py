@@ -32,11 +32,13 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libhycadv.so")
 
 HYC_OK = 0
 ERRORS = {-1: "HYC_ERR_ARG", -2: "HYC_ERR_ADVTYP", -3: "HYC_ERR_NBDY", -4: "HYC_ERR_MASK", -5: "HYC_ERR_CUDA",
-          -6: "HYC_ERR_FIELD", -7: "HYC_ERR_GRID", -8: "HYC_ERR_UNSUPPORTED", -9: "HYC_ERR_NOMEM"}
+          -6: "HYC_ERR_FIELD", -7: "HYC_ERR_GRID", -8: "HYC_ERR_UNSUPPORTED", -9: "HYC_ERR_NOMEM",
+          -10: "HYC_ERR_NEGDP"}
 HYC_HOST, HYC_DEVICE = 0, 1
 FIELDS = {"temp": 0, "saln": 1, "th3d": 2, "tracer": 3, "uflx": 4, "vflx": 5, "dp": 6, "oneta": 7, "q2": 8,
           "q2l": 9, "dpo": 10, "onetao": 11, "pbavg": 12, "pbot": 13, "otemp": 14, "osaln": 15, "oth3d": 16,
-          "otracer": 17, "oq2": 18, "oq2l": 19}
+          "otracer": 17, "oq2": 18, "oq2l": 19, "u": 20, "v": 21, "dpu": 22, "dpv": 23, "ubavg": 24, "vbavg": 25,
+          "p": 26, "uflxav": 27, "vflxav": 28, "dpav": 29, "onetacnt": 30}
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "hyc_set_stream", "hyc_bind_field",
@@ -47,10 +49,11 @@ EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "
            "hyc_ens_tune", "hyc_ens_step", "hyc_ens_content", "hyc_ens_stats", "hyc_ens_enable_timers",
            "hyc_ens_last_error", "hyc_ens_set_option", "hyc_ens_get_option", "hyc_ens_set_posdef",
            "hyc_za_read", "hyc_za_parse_b", "hyc_za_check", "hyc_set_diffusion_grid", "hyc_tsdff",
-           "hyc_asselin_save", "hyc_asselin_filter", "hyc_ens_get_async", "hyc_ens_wait")
+           "hyc_asselin_save", "hyc_asselin_filter", "hyc_ens_get_async", "hyc_ens_wait",
+           "hyc_set_cnuity_grid", "hyc_cnuity")
 ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
-TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4, "tsdff": 5, "asselin": 6}
+TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4, "tsdff": 5, "asselin": 6, "cnuity": 7}
 
 
 class HycError(RuntimeError):
@@ -68,6 +71,11 @@ class BasinSpec(C.Structure):
                 ("nreg", C.c_int32), ("ntr", C.c_int32), ("ip", C.POINTER(C.c_int32)),
                 ("iu", C.POINTER(C.c_int32)), ("iv", C.POINTER(C.c_int32)), ("scp2", C.POINTER(C.c_double)),
                 ("scp2i", C.POINTER(C.c_double))]
+
+
+class CnuityParams(C.Structure):
+    _fields_ = [("nstep", C.c_int32), ("btrmas", C.c_int32), ("thkdf", C.c_int32), ("isopyc", C.c_int32),
+                ("delt1", C.c_double), ("ra2fac", C.c_double)]
 
 
 class TsadvcParams(C.Structure):
@@ -104,6 +112,8 @@ def lib() -> C.CDLL:
         L.hyc_xctilr.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         L.hyc_mass_sum.argtypes = [vp, vp, vp, dp]
         L.hyc_set_diffusion_grid.argtypes = [vp, dp, dp, dp, dp]
+        L.hyc_set_cnuity_grid.argtypes = [vp, dp, dp, dp, dp, dp, dp]
+        L.hyc_cnuity.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(CnuityParams), dp]
         L.hyc_asselin_save.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(TsadvcParams), C.c_double]
         L.hyc_asselin_filter.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(TsadvcParams), C.c_double,
                                          C.c_double, C.c_double]
@@ -346,6 +356,23 @@ class Context(_StreamFollower):
                          hybrid=int(nh > 0), mxlmy=int(mxlmy), nstep=1, diagno=0, delt1=float(delt1),
                          trcflg=tf.ctypes.data_as(C.POINTER(C.c_int32)))
         return p, tf
+
+    def set_cnuity_grid(self, scuy, scvx, depthu, depthv, thkdfu=None, thkdfv=None):
+        """Grid arrays of cnuity (host, ld1*ld2 each; thkdf* may be None)."""
+        keep = [_f64(a) for a in (scuy, scvx, depthu, depthv)]
+        th = [(None, None) if a is None else _f64(a) for a in (thkdfu, thkdfv)]
+        _check(lib().hyc_set_cnuity_grid(self._h, *[k[1] for k in keep], th[0][1], th[1][1]), self._h)
+
+    def cnuity(self, m: int, n: int, *, delt1: float, nstep: int = 1, btrmas: bool = False, thkdf: int = 0,
+               ra2fac: float = 0.125, want_dpkmin: bool = False):
+        """cnuity(m,n) on the bound fields.  Returns dpkmin (2*kdm) when asked."""
+        p = CnuityParams(nstep=nstep, btrmas=int(btrmas), thkdf=int(thkdf), isopyc=0, delt1=float(delt1),
+                         ra2fac=float(ra2fac))
+        out = np.zeros(2 * self.kdm) if want_dpkmin else None
+        self._order(self._bound.values())
+        _check(lib().hyc_cnuity(self._h, m, n, C.byref(p), None if out is None else
+                                out.ctypes.data_as(C.POINTER(C.c_double))), self._h)
+        return out
 
     def asselin_save(self, m: int, n: int, *, oneta0: float, ntracr: int = 0, mxlmy: bool = False):
         """asselin_save(m,n) on the bound fields (start of a step)."""

@@ -42,6 +42,7 @@ extern "C" {
 #define HYC_ERR_GRID -7        /* bigrid: 1-point sea, arctic row, ms overflow */
 #define HYC_ERR_UNSUPPORTED -8 /* option outside this library's scope */
 #define HYC_ERR_NOMEM -9       /* device allocation failed */
+#define HYC_ERR_NEGDP -10      /* cnuity: a layer thinner than dpfatal, cnuity.F90:574-580 */
 
 /* where a pointer lives */
 #define HYC_HOST 0
@@ -69,7 +70,19 @@ extern "C" {
 #define HYC_F_OTRACER 17 /* otracer(ld1,ld2,kdm,ntracr)       */
 #define HYC_F_OQ2 18     /* oq2(ld1,ld2,0:kdm+1), if mxlmy    */
 #define HYC_F_OQ2L 19    /* oq2l(ld1,ld2,0:kdm+1), if mxlmy   */
-#define HYC_NFIELDS 20
+/* continuity equation (mod_cb_arrays.F90), hyc_cnuity only */
+#define HYC_F_U 20        /* u(ld1,ld2,kdm,2)                  */
+#define HYC_F_V 21        /* v(ld1,ld2,kdm,2)                  */
+#define HYC_F_DPU 22      /* dpu(ld1,ld2,kdm,2)                */
+#define HYC_F_DPV 23      /* dpv(ld1,ld2,kdm,2)                */
+#define HYC_F_UBAVG 24    /* ubavg(ld1,ld2,3)                  */
+#define HYC_F_VBAVG 25    /* vbavg(ld1,ld2,3)                  */
+#define HYC_F_P 26        /* p(ld1,ld2,kdm+1)                  */
+#define HYC_F_UFLXAV 27   /* uflxav(ld1,ld2,kdm), optional     */
+#define HYC_F_VFLXAV 28   /* vflxav(ld1,ld2,kdm), optional     */
+#define HYC_F_DPAV 29     /* dpav(ld1,ld2,kdm), optional       */
+#define HYC_F_ONETACNT 30 /* onetacnt(ld1,ld2), if btrmas      */
+#define HYC_NFIELDS 31
 
 typedef struct hyc_ctx hyc_ctx;
 
@@ -235,6 +248,52 @@ int hyc_asselin_save(hyc_ctx *ctx, int32_t m, int32_t n, const hyc_tsadvc_params
 int hyc_asselin_filter(hyc_ctx *ctx, int32_t m, int32_t n, const hyc_tsadvc_params *p, double ra2fac,
                        double oneta0, double thbase);
 
+/* Run-time switches of cnuity (blkdat.F90 names). */
+typedef struct hyc_cnuity_params {
+  int32_t nstep;   /* model step: the fatal negative-thickness check runs when
+                      mod(nstep,3)==0 (cnuity.F90:520); the biharmonic
+                      diffusion alternates its direction with mod(nstep,2) */
+  int32_t btrmas;  /* barotropic mass flag                                  */
+  int32_t thkdf;   /* interface-depth diffusion: 0 none, 4 biharmonic
+                      (thkdf4 != 0), 2 Laplacian (thkdf2 != 0)              */
+  int32_t isopyc;  /* isopycnic mode: unsupported, must be 0               */
+  double delt1;    /* leapfrog time step                                    */
+  double ra2fac;   /* Robert-Asselin weight                                 */
+} hyc_cnuity_params;
+
+/*
+ * Grid arrays of cnuity (mod_cb_arrays.F90 names, host arrays of ld1*ld2
+ * with valid halos): scuy, scvx, depthu, depthv (u/v-point depths in
+ * pressure units) and thkdfu, thkdfv (the reference's thkdf4u/thkdf4v:
+ * the interface-diffusion coefficients, biharmonic or Laplacian; NULL when
+ * no interface diffusion runs).  Copied to the device and kept.
+ */
+int hyc_set_cnuity_grid(hyc_ctx *ctx, const double *scuy, const double *scvx, const double *depthu,
+                        const double *depthv, const double *thkdfu, const double *thkdfv);
+
+/*
+ * cnuity(m,n) (cnuity.F90:14-1419), the continuity equation on the bound
+ * fields: halo fill of dp, dpu, dpv, u, v, ubavg, vbavg (width 6); per
+ * layer the flux-corrected transport of dp(:,:,k,n) with low-order
+ * fluxes, the Zalesak limiter and the clipped antidiffusive fluxes
+ * (loop 76), the mass fluxes into uflx/vflx and the interface pressures p;
+ * without btrmas the barotropic restoration (loop 77) and the
+ * bottom-pressure restoring; the interface-depth diffusion p->thkdf; the
+ * cumulative uflxav/vflxav/dpav when all three are bound; with btrmas the
+ * restoring to dp' (onetacnt); then the Robert-Asselin filter of dp(m) and
+ * dpo.  Needs nbdy >= 6, hyc_set_cnuity_grid, and fields dp, dpo, u, v,
+ * dpu, dpv, ubavg, vbavg, pbot, p, uflx, vflx (oneta and onetacnt with
+ * btrmas).  dpkmin (host, 2*kdm, may be NULL) receives the minimum
+ * thickness of each layer after the low-order and after the antidiffusive
+ * update.  A layer thinner than dpfatal = -10 m (checked when
+ * mod(nstep,3)==0) stops the reference; here it returns HYC_ERR_NEGDP
+ * before the rest of the step.  Not supported: open boundaries (the
+ * masks have none), STOKES drift, isopyc, the Kraus-Turner mixed-layer
+ * base (mxlkta), floats.  FP64, bit-identical to the oracle.
+ * Replaces: cnuity.F90:14 (subroutine cnuity), call site mod_hycom.F90:2520.
+ */
+int hyc_cnuity(hyc_ctx *ctx, int32_t m, int32_t n, const hyc_cnuity_params *p, double *dpkmin);
+
 /*
  * Tracer content sum over sea points of the interior,
  *   sum_{i,j} fld(i,j) * (fc(i,j) + onemu) * scp2(i,j),
@@ -259,6 +318,7 @@ int hyc_mass_sum(hyc_ctx *ctx, const double *fld, const double *fc, double *sum)
 #define HYC_T_DIAG 4   /* salinity range diagnostic             */
 #define HYC_T_TSDFF 5  /* lateral diffusion (hyc_tsdff)         */
 #define HYC_T_ASSELIN 6 /* Robert-Asselin save and filter      */
+#define HYC_T_CNUITY 7  /* continuity equation (hyc_cnuity)    */
 #define HYC_NTIMERS 8
 
 typedef struct hyc_stats {

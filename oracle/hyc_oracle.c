@@ -1730,12 +1730,14 @@ int hyo_cnuity(hyo_grid *g, const hyo_cnparams *p, int m, int n, double *const *
         const double *oneta = a[HYO_C_ONETA];
         om[c] = oneta[c];
         om[c + sl] = oneta[c + sl];
-        if (iu[c] != 0) {
+        /* the outermost halo column/row has no west/south neighbour (the
+           reference reads outside the array there); those factors are never read */
+        if (iu[c] != 0 && i > 1 - g->nbdy) {
           if (pbot[c] == pbot[c - 1]) oneta_u[c] = 0.5 * (om[c + mm * sl] + om[c - 1 + mm * sl]);
           else if (pbot[c] == depthu[c]) oneta_u[c] = om[c + mm * sl];
           else oneta_u[c] = om[c - 1 + mm * sl];
         }
-        if (iv[c] != 0) {
+        if (iv[c] != 0 && j > 1 - g->nbdy) {
           if (pbot[c] == pbot[c - ld]) oneta_v[c] = 0.5 * (om[c + mm * sl] + om[c - ld + mm * sl]);
           else if (pbot[c] == depthv[c]) oneta_v[c] = om[c + mm * sl];
           else oneta_v[c] = om[c - ld + mm * sl];
