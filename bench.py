@@ -360,15 +360,19 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
     kdm = wl["kdm"]
     ctx = hycadv.Context.from_masks(masks, sc, si, kdm=kdm, nreg=nreg, nbdy=b.nbdy, device=local)
     ctx.set_stream(stream)
-    for k in ("temp", "saln", "th3d", "uflx", "vflx", "dp"):
+    for k in ("temp", "saln", "th3d", "uflx", "vflx"):
         ctx.bind(k, getattr(case, k))
-    keep = []
+    # the Robert-Asselin filter rewrites dp(m): the full form works on a copy
+    # so that dp stays consistent with uflx/vflx for the forms after it
+    dpb = case.dp.clone() if full else case.dp
+    ctx.bind("dp", dpb)
+    keep = [dpb]
     if full:
         sh2 = tuple(case.dp.shape[-2:])
         f64 = dict(dtype=torch.float64, device=dev)
         extra = {"oneta": torch.ones((2,) + sh2, **f64), "onetao": torch.ones((2,) + sh2, **f64),
                  "pbavg": torch.zeros((3,) + sh2, **f64), "pbot": torch.full(sh2, 4.0e7, **f64),
-                 "dpo": case.dp.clone(), "otemp": torch.empty_like(case.temp[0]),
+                 "dpo": dpb.clone(), "otemp": torch.empty_like(case.temp[0]),
                  "osaln": torch.empty_like(case.saln[0]), "oth3d": torch.empty_like(case.th3d[0])}
         for k, v in extra.items():
             ctx.bind(k, v)
@@ -485,7 +489,7 @@ def run_cnuity(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local)
     iu = torch.from_numpy(np.asarray(masks["iu"]) != 0).to(dev)
     iv = torch.from_numpy(np.asarray(masks["iv"]) != 0).to(dev)
     dx = float(np.sqrt(np.asarray(sc, dtype=np.float64)).max())
-    dp = case.dp
+    dp = case.dp.clone()  # cnuity rewrites dp; the other forms keep the case's
     f = {"dp": dp, "dpo": torch.zeros_like(dp)}
     dpu = torch.zeros_like(dp)
     dpv = torch.zeros_like(dp)
