@@ -325,8 +325,8 @@ int hyc_adv_init(hyc_ctx **out, int32_t idm, int32_t jdm, int32_t kdm, int32_t n
   *out = nullptr;
   if (idm < 1 || jdm < 1 || kdm < 1 || nbdy < 3 || !ip || !iu || !iv || !scp2 || !scp2i)
     return fail(nullptr, HYC_ERR_ARG, "hyc_adv_init: bad sizes or null arrays (need nbdy >= 3)");
-  if (!(nreg == 0 || nreg == 1 || nreg == 3 || nreg == 4))
-    return fail(nullptr, HYC_ERR_ARG, "hyc_adv_init: nreg %d unsupported (0, 1, 3 or 4)", nreg);
+  if (!(nreg == 0 || nreg == 1 || nreg == 3 || nreg == 4 || nreg == HYC_NREG_EXTERNAL))
+    return fail(nullptr, HYC_ERR_ARG, "hyc_adv_init: nreg %d unsupported (0, 1, 3, 4 or HYC_NREG_EXTERNAL)", nreg);
   hyc_ctx *c = new hyc_ctx;
   c->idm = idm;
   c->jdm = jdm;
@@ -533,6 +533,8 @@ int hyc_advem(hyc_ctx *c, int32_t advtyp, double *fld, const double *fldc, const
     dscali = c->d_tmp + 7 * sl;
   }
   if (advtyp == 2 && btrmas) {  // advem_fct2c, mod_tsadvc.F90:154-155
+    if (c->nreg < 0)
+      return fail(c, HYC_ERR_UNSUPPORTED, "advem_fct2c refreshes halos in mid-scheme: not with external halos");
     int rc = ensure_fct2c(c, hyc::fct2c_work_bytes(sl));
     if (rc) return rc;
     hyc::Fct2cArgs f;
@@ -640,6 +642,8 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
   if (p->mxlmy && ((rc = need(HYC_F_Q2, 2LL * (kk + 2) * sl, "q2")) || (rc = need(HYC_F_Q2L, 2LL * (kk + 2) * sl, "q2l"))))
     return rc;
   if (p->btrmas && (rc = need(HYC_F_ONETA, 2LL * sl, "oneta"))) return rc;
+  if (p->btrmas && at == 2 && c->nreg < 0)
+    return fail(c, HYC_ERR_UNSUPPORTED, "advem_fct2c refreshes halos in mid-scheme: not with external halos");
   DeviceGuard g(c->device);
   cudaStream_t s = c->stream;
   const int mm = m - 1, nn = n - 1;
@@ -1041,6 +1045,8 @@ int hyc_cnuity(hyc_ctx *c, int32_t m, int32_t n, const hyc_cnuity_params *p, dou
   if (c->nbdy < 6) return fail(c, HYC_ERR_NBDY, "cnuity needs nbdy >= 6 (its halo is 6 wide)");
   if (!c->d_cngrid) return fail(c, HYC_ERR_FIELD, "hyc_cnuity: call hyc_set_cnuity_grid first");
   if (p->thkdf && !c->cn_thkdf) return fail(c, HYC_ERR_FIELD, "hyc_cnuity: interface diffusion without thkdfu/thkdfv");
+  if (p->thkdf && c->nreg < 0)
+    return fail(c, HYC_ERR_UNSUPPORTED, "the interface diffusion refreshes halos in mid-step: not with external halos");
   const int kk = c->kdm;
   const long long sl = c->slice;
   Field *F = c->fields;

@@ -35,6 +35,7 @@ ERRORS = {-1: "HYC_ERR_ARG", -2: "HYC_ERR_ADVTYP", -3: "HYC_ERR_NBDY", -4: "HYC_
           -6: "HYC_ERR_FIELD", -7: "HYC_ERR_GRID", -8: "HYC_ERR_UNSUPPORTED", -9: "HYC_ERR_NOMEM",
           -10: "HYC_ERR_NEGDP"}
 HYC_HOST, HYC_DEVICE = 0, 1
+NREG_EXTERNAL = -1  # HYC_NREG_EXTERNAL: one block of a decomposed basin (hycadv.decomp)
 FIELDS = {"temp": 0, "saln": 1, "th3d": 2, "tracer": 3, "uflx": 4, "vflx": 5, "dp": 6, "oneta": 7, "q2": 8,
           "q2l": 9, "dpo": 10, "onetao": 11, "pbavg": 12, "pbot": 13, "otemp": 14, "osaln": 15, "oth3d": 16,
           "otracer": 17, "oq2": 18, "oq2l": 19, "u": 20, "v": 21, "dpu": 22, "dpv": 23, "ubavg": 24, "vbavg": 25,

@@ -44,6 +44,11 @@ extern "C" {
 #define HYC_ERR_NOMEM -9       /* device allocation failed */
 #define HYC_ERR_NEGDP -10      /* cnuity: a layer thinner than dpfatal, cnuity.F90:574-580 */
 
+/* nreg of a context that is one block of a basin split over ranks: its
+   halos are filled by the caller's exchange with the neighbouring blocks
+   (hycadv.decomp), and xctilr leaves them alone */
+#define HYC_NREG_EXTERNAL -1
+
 /* where a pointer lives */
 #define HYC_HOST 0
 #define HYC_DEVICE 1
@@ -118,7 +123,11 @@ int hyc_bigrid(int32_t idm, int32_t jdm, int32_t nbdy, double *depth, int32_t *i
 
 /*
  * Create a context bound to one GPU: grid sizes, nreg (mod_xc: 0 closed,
- * 1 periodic-x/closed-y, 3 periodic in both), masks ip/iu/iv and the grid
+ * 1 periodic-x/closed-y, 3 periodic in both; HYC_NREG_EXTERNAL for one
+ * block of a decomposed basin, whose halos the caller exchanges before
+ * hyc_tsadvc / hyc_tsdff / hyc_cnuity; the routines that refresh halos in
+ * mid-step, advem_fct2c (btrmas) and cnuity's interface diffusion, return
+ * HYC_ERR_UNSUPPORTED there), masks ip/iu/iv and the grid
  * metrics scp2/scp2i (all host arrays of ld1*ld2).  The masks and metrics
  * are copied to the device and stay resident.  Replaces the module state
  * that tsadvc reads through `use mod_dimensions, mod_cb_arrays`

@@ -130,6 +130,7 @@ int hyo_max_threads(void) {
 /* a points at a(1-nbdy,1-nbdy,1); nlev slices of ld1*ld2 each.        */
 /* ------------------------------------------------------------------ */
 void hyo_xctilr(const hyo_grid *g, double *a, int nlev, int mh, int nh) {
+  if (g->nreg < 0) return; /* a tile of a decomposed basin: its halo is exchanged by the caller */
   const int ii = g->ii, jj = g->jj, nbdy = g->nbdy;
   const size_t sl = (size_t)g->ld1 * g->ld2;
   const double vland = 0.0; /* mod_xc_sm.h:841 */
@@ -251,6 +252,71 @@ void hyo_grid_free(hyo_grid *g) {
   free(g);
 }
 
+/* arrays of a grid of g->ld1 x g->ld2 points; the work arrays start as NaN */
+static int grid_alloc(hyo_grid *g) {
+  const size_t n2 = (size_t)g->ld1 * g->ld2;
+  g->ip = (int32_t *)calloc(n2, 4);
+  g->iu = (int32_t *)calloc(n2, 4);
+  g->iv = (int32_t *)calloc(n2, 4);
+  g->iq = (int32_t *)calloc(n2, 4);
+  g->ipim1 = (int32_t *)calloc(n2, 4);
+  g->ipip1 = (int32_t *)calloc(n2, 4);
+  g->ipjm1 = (int32_t *)calloc(n2, 4);
+  g->ipjp1 = (int32_t *)calloc(n2, 4);
+  g->ifp = (int32_t *)calloc((size_t)g->ld2 * g->ms, 4);
+  g->ilp = (int32_t *)calloc((size_t)g->ld2 * g->ms, 4);
+  g->isp = (int32_t *)calloc((size_t)g->ld2, 4);
+  g->jfp = (int32_t *)calloc((size_t)g->ld1 * g->ms, 4);
+  g->jlp = (int32_t *)calloc((size_t)g->ld1 * g->ms, 4);
+  g->jsp = (int32_t *)calloc((size_t)g->ld1, 4);
+  g->scp2 = (double *)malloc(n2 * 8);
+  g->scp2i = (double *)malloc(n2 * 8);
+  double **work[] = {&g->fmx,   &g->fmn,   &g->flx,    &g->fly,    &g->fldlo,  &g->fmxlo,  &g->fmnlo,
+                     &g->fax,   &g->fay,   &g->rp,     &g->rm,     &g->flxdiv, &g->tx1,    &g->ty1,
+                     &g->fldao, &g->fldan, &g->uloc,   &g->vloc,   &g->hloc,   &g->dtloc,  &g->ucumdt,
+                     &g->vcumdt, &g->flxcum, &g->flycum, &g->util1, &g->util2, &g->uflux, &g->vflux};
+  int bad = !g->ip || !g->iu || !g->iv || !g->iq || !g->ipim1 || !g->ipip1 || !g->ipjm1 || !g->ipjp1 ||
+            !g->ifp || !g->ilp || !g->isp || !g->jfp || !g->jlp || !g->jsp || !g->scp2 || !g->scp2i;
+  for (size_t k = 0; k < sizeof(work) / sizeof(work[0]); k++) {
+    *work[k] = nan_array(n2);
+    bad |= (*work[k] == NULL);
+  }
+  g->lcalc = (unsigned char *)calloc(n2, 1);
+  g->uflux2 = (double *)calloc(n2, 8);
+  g->vflux2 = (double *)calloc(n2, 8);
+  bad |= !g->uflux2 || !g->vflux2 || !g->lcalc;
+  if (bad) {
+    hyo_grid_free(g);
+    return HYO_ERR_MEM;
+  }
+  return HYO_OK;
+}
+
+/* sea-only neighbour indices (bigrid.F90:316-333; outer ring = self) and
+   the sea sections (indxi/indxj) from ip */
+static int grid_finish(hyo_grid *g) {
+  const int ii = g->ii, jj = g->jj, nbdy = g->nbdy;
+  for (int j = 1 - nbdy; j <= jj + nbdy; j++)
+    for (int i = 1 - nbdy; i <= ii + nbdy; i++) {
+      size_t c = P(g, i, j);
+      g->ipim1[c] = i;
+      g->ipip1[c] = i;
+      g->ipjm1[c] = j;
+      g->ipjp1[c] = j;
+    }
+  for (int j = 2 - nbdy; j <= jj + nbdy - 1; j++)
+    for (int i = 2 - nbdy; i <= ii + nbdy - 1; i++) {
+      size_t c = P(g, i, j);
+      g->ipim1[c] = g->ip[P(g, i - 1, j)] != 0 ? i - 1 : i;
+      g->ipip1[c] = g->ip[P(g, i + 1, j)] != 0 ? i + 1 : i;
+      g->ipjm1[c] = g->ip[P(g, i, j - 1)] != 0 ? j - 1 : j;
+      g->ipjp1[c] = g->ip[P(g, i, j + 1)] != 0 ? j + 1 : j;
+    }
+  if (indxi(g, g->ip, g->ifp, g->ilp, g->isp) != HYO_OK || indxj(g, g->ip, g->jfp, g->jlp, g->jsp) != HYO_OK)
+    return HYO_ERR_GRID;
+  return HYO_OK;
+}
+
 /*
  * bigrid: bigrid.F90:1-415 for a single tile (i0=j0=0, ii=itdm, jj=jtdm),
  * mapflg != 4 (no f-plane).  depth is (ld1*ld2) with halo; it is modified
@@ -327,45 +393,12 @@ hyo_grid *hyo_grid_create(int idm, int jdm, int nbdy, double *depth, const doubl
     free(g);
     return NULL;
   }
-  g->ip = (int32_t *)calloc(n2, 4);
-  g->iu = (int32_t *)calloc(n2, 4);
-  g->iv = (int32_t *)calloc(n2, 4);
-  g->iq = (int32_t *)calloc(n2, 4);
-  g->ipim1 = (int32_t *)calloc(n2, 4);
-  g->ipip1 = (int32_t *)calloc(n2, 4);
-  g->ipjm1 = (int32_t *)calloc(n2, 4);
-  g->ipjp1 = (int32_t *)calloc(n2, 4);
-  g->ifp = (int32_t *)calloc((size_t)g->ld2 * g->ms, 4);
-  g->ilp = (int32_t *)calloc((size_t)g->ld2 * g->ms, 4);
-  g->isp = (int32_t *)calloc((size_t)g->ld2, 4);
-  g->jfp = (int32_t *)calloc((size_t)g->ld1 * g->ms, 4);
-  g->jlp = (int32_t *)calloc((size_t)g->ld1 * g->ms, 4);
-  g->jsp = (int32_t *)calloc((size_t)g->ld1, 4);
-  g->scp2 = (double *)malloc(n2 * 8);
-  g->scp2i = (double *)malloc(n2 * 8);
-  double **work[] = {&g->fmx,   &g->fmn,   &g->flx,    &g->fly,    &g->fldlo,  &g->fmxlo,  &g->fmnlo,
-                     &g->fax,   &g->fay,   &g->rp,     &g->rm,     &g->flxdiv, &g->tx1,    &g->ty1,
-                     &g->fldao, &g->fldan, &g->uloc,   &g->vloc,   &g->hloc,   &g->dtloc,  &g->ucumdt,
-                     &g->vcumdt, &g->flxcum, &g->flycum, &g->util1, &g->util2, &g->uflux, &g->vflux};
-  int bad = !g->ip || !g->iu || !g->iv || !g->iq || !g->ipim1 || !g->ipip1 || !g->ipjm1 || !g->ipjp1 ||
-            !g->ifp || !g->ilp || !g->isp || !g->jfp || !g->jlp || !g->jsp || !g->scp2 || !g->scp2i;
-  for (size_t k = 0; k < sizeof(work) / sizeof(work[0]); k++) {
-    *work[k] = nan_array(n2);
-    bad |= (*work[k] == NULL);
-  }
-  g->lcalc = (unsigned char *)calloc(n2, 1);
-  g->uflux2 = (double *)calloc(n2, 8);
-  g->vflux2 = (double *)calloc(n2, 8);
-  bad |= !g->uflux2 || !g->vflux2;
-  bad |= (g->lcalc == NULL);
-  if (bad) {
-    hyo_grid_free(g);
+  if (grid_alloc(g) != HYO_OK) {
     *err = HYO_ERR_MEM;
     return NULL;
   }
   memcpy(g->scp2, scp2, n2 * 8);
   memcpy(g->scp2i, scp2i, n2 * 8);
-
   /* masks: bigrid.F90:193-290 */
   for (int j = 1 - nbdy; j <= jj + nbdy; j++)
     for (int i = 1 - nbdy; i <= ii + nbdy; i++)
@@ -423,24 +456,50 @@ hyo_grid *hyo_grid_create(int idm, int jdm, int nbdy, double *depth, const doubl
     for (int j = 1 - nbdy; j <= jj + nbdy; j++)
       for (int i = ii + 1; i <= ii + nbdy; i++) g->iq[P(g, i, j)] = g->iu[P(g, i, j)] = g->iv[P(g, i, j)] = 0;
   }
-  /* sea-only neighbour indices: bigrid.F90:316-333; outer ring = self */
-  for (int j = 1 - nbdy; j <= jj + nbdy; j++)
-    for (int i = 1 - nbdy; i <= ii + nbdy; i++) {
-      size_t c = P(g, i, j);
-      g->ipim1[c] = i;
-      g->ipip1[c] = i;
-      g->ipjm1[c] = j;
-      g->ipjp1[c] = j;
-    }
-  for (int j = 2 - nbdy; j <= jj + nbdy - 1; j++)
-    for (int i = 2 - nbdy; i <= ii + nbdy - 1; i++) {
-      size_t c = P(g, i, j);
-      g->ipim1[c] = g->ip[P(g, i - 1, j)] != 0 ? i - 1 : i;
-      g->ipip1[c] = g->ip[P(g, i + 1, j)] != 0 ? i + 1 : i;
-      g->ipjm1[c] = g->ip[P(g, i, j - 1)] != 0 ? j - 1 : j;
-      g->ipjp1[c] = g->ip[P(g, i, j + 1)] != 0 ? j + 1 : j;
-    }
-  if (indxi(g, g->ip, g->ifp, g->ilp, g->isp) != HYO_OK || indxj(g, g->ip, g->jfp, g->jlp, g->jsp) != HYO_OK) {
+  if (grid_finish(g) != HYO_OK) {
+    hyo_grid_free(g);
+    *err = HYO_ERR_GRID;
+    return NULL;
+  }
+  return g;
+}
+
+/*
+ * A grid with given masks: one tile of a decomposed basin (its window of
+ * the basin's ip/iu/iv with halo, ld1*ld2 each).  nreg < 0: the tile's
+ * halos are exchanged by the caller, xctilr leaves them alone.
+ */
+hyo_grid *hyo_grid_from_masks(int idm, int jdm, int nbdy, int nreg, const int32_t *ip, const int32_t *iu,
+                              const int32_t *iv, const double *scp2, const double *scp2i, int *err) {
+  *err = HYO_OK;
+  if (idm < 1 || jdm < 1 || nbdy < 1 || !ip || !iu || !iv || !scp2 || !scp2i) {
+    *err = HYO_ERR_ARG;
+    return NULL;
+  }
+  hyo_grid *g = (hyo_grid *)calloc(1, sizeof(hyo_grid));
+  if (!g) {
+    *err = HYO_ERR_MEM;
+    return NULL;
+  }
+  g->ii = idm;
+  g->jj = jdm;
+  g->nbdy = nbdy;
+  g->ld1 = idm + 2 * nbdy;
+  g->ld2 = jdm + 2 * nbdy;
+  g->ms = 99;
+  g->nreg = nreg;
+  g->lperiod = nreg == 1 || nreg == 3;
+  const size_t n2 = (size_t)g->ld1 * g->ld2;
+  if (grid_alloc(g) != HYO_OK) {
+    *err = HYO_ERR_MEM;
+    return NULL;
+  }
+  memcpy(g->scp2, scp2, n2 * 8);
+  memcpy(g->scp2i, scp2i, n2 * 8);
+  memcpy(g->ip, ip, n2 * 4);
+  memcpy(g->iu, iu, n2 * 4);
+  memcpy(g->iv, iv, n2 * 4);
+  if (grid_finish(g) != HYO_OK) {
     hyo_grid_free(g);
     *err = HYO_ERR_GRID;
     return NULL;

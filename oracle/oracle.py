@@ -37,6 +37,8 @@ def lib():
         ip = C.POINTER(C.c_int32)
         L.hyo_grid_create.restype = C.c_void_p
         L.hyo_grid_create.argtypes = [C.c_int, C.c_int, C.c_int, dp, dp, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.hyo_grid_from_masks.restype = C.c_void_p
+        L.hyo_grid_from_masks.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, ip, ip, ip, dp, dp, C.POINTER(C.c_int)]
         L.hyo_grid_free.argtypes = [C.c_void_p]
         L.hyo_grid_nreg.argtypes = [C.c_void_p]
         L.hyo_grid_masks.argtypes = [C.c_void_p] + [ip] * 7
@@ -115,6 +117,35 @@ class Grid:
         if h is not None and _lib is not None:
             _lib.hyo_grid_free(h)
             self._h = None
+
+    @classmethod
+    def from_masks(cls, ip, iu, iv, scp2, scp2i, nbdy: int = 6, nreg: int = -1, threads: int = 0):
+        """A tile of a decomposed basin: its window (with halo) of the basin's
+        masks and metrics.  nreg < 0: halos come from the caller's exchange."""
+        L = lib()
+        self = cls.__new__(cls)
+        self.nbdy = nbdy
+        self.ld2, self.ld1 = ip.shape
+        self.idm = self.ld1 - 2 * nbdy
+        self.jdm = self.ld2 - 2 * nbdy
+        self.depth = None
+        keep = [np.ascontiguousarray(a, np.int32) for a in (ip, iu, iv)]
+        self.scp2 = np.ascontiguousarray(scp2, np.float64)
+        self.scp2i = np.ascontiguousarray(scp2i, np.float64)
+        err = C.c_int(0)
+        h = L.hyo_grid_from_masks(self.idm, self.jdm, nbdy, nreg, *[_p(k) for k in keep], _p(self.scp2),
+                                  _p(self.scp2i), C.byref(err))
+        if not h:
+            raise OracleError(f"hyo_grid_from_masks failed: err={err.value}")
+        self._h = C.c_void_p(h)
+        self.nreg = nreg
+        shp = (self.ld2, self.ld1)
+        m = {k: np.zeros(shp, np.int32) for k in ("ip", "iu", "iv", "ipim1", "ipip1", "ipjm1", "ipjp1")}
+        L.hyo_grid_masks(self._h, *[_p(m[k]) for k in ("ip", "iu", "iv", "ipim1", "ipip1", "ipjm1", "ipjp1")])
+        self.masks = m
+        if threads:
+            self.set_threads(threads)
+        return self
 
     def set_threads(self, n: int):
         lib().hyo_set_threads(self._h, int(n))
