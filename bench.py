@@ -31,6 +31,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "hycom-src_gb300")
 for _p in (ROOT, PKG):
@@ -1149,6 +1151,9 @@ def main():
     spec = dict(idm=b.nx, jdm=b.ny, kdm=kdm, nbdy=b.nbdy, nreg=nreg, ntr=2, ip=masks["ip"], iu=masks["iu"],
                 iv=masks["iv"], scp2=sc, scp2i=si)
     others = [f for f in args.forms.split(",") if f]
+    # sea-only count beside the dense interior one (interior cells with ip = 1)
+    nb = b.nbdy
+    sea_cells = int((np.asarray(masks["ip"])[nb:nb + b.ny, nb:nb + b.nx] != 0).sum())
     tsadvc = None
     if "tsadvc" in others:
         tsadvc = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local)
@@ -1203,7 +1208,8 @@ def main():
             "vs_baseline": None, "dtype": "f32-mixed" if prec == "mixed" else "f64",
             "data": "synthetic (seeded generator, HYCOM units/layout)",
             "config": dict(config_of(args, wl, f"ensemble-{args.form}"), tile=head["tile"],
-                           tracers_per_pass=head["tracers_per_pass"]),
+                           tracers_per_pass=head["tracers_per_pass"],
+                           sea_updates_per_step=sea_cells * wl["kdm"] * 2),
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
             "clocks": head["clocks"], "headline": {k: v for k, v in head.items() if k != "clocks"},
             "forms": others_out, "wall_seconds": time.perf_counter() - t_start,
