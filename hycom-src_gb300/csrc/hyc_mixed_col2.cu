@@ -143,6 +143,10 @@ struct StM {
   float2 lx3, ly3;            // limited fluxes of row J-3
 };
 constexpr float kBig = 1.0e30f;   // land sentinel of the masked extrema (finite: no inf*0)
+// Store a row's results after every tracer of the pass is computed: the
+// tracer loop is then one branch-free block whose independent chains the
+// compiler can interleave (stores inside it split it at each tracer).
+constexpr bool kLateStore = true;
 
 }  // namespace
 
@@ -243,7 +247,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
             break;
           }
           const unsigned char *slot = ring + (g % kNS) * RG::SLOT;
-#pragma unroll 2
+#pragma unroll(PREP64 ? 2 : kRB)  // measured: full unroll 1.8 % faster with the FP32 prep, 2.5 % slower with FP64
           for (int rr = 0; rr < kRB; rr++) {
             const int J = j0 - 3 + blk * kRB + rr;
             // ---- inputs of row J
@@ -341,6 +345,18 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               va0 = mul2(make_float2(fabsf(v0m.x), fabsf(v0m.y)), half);
             }
 
+            float2 res[NQ];
+            auto store_row = [&](int q, float resA, float resB) {
+              float *p = fn[q] + (long long)a0 + (long long)(jo + nb - 1) * ld1;
+              if (stA) p[0] = resA;
+              if (stB) p[1] = resB;
+              if (images) {
+                if (stA && iA <= images) p[ii] = resA;
+                if (stA && iA > ii - images) p[-ii] = resA;
+                if (stB && iB <= images) p[1 + ii] = resB;
+                if (stB && iB > ii - images) p[1 - ii] = resB;
+              }
+            };
             if constexpr (!MP) {
 #pragma unroll
             for (int q = 0; q < NQ; q++) {
@@ -400,17 +416,8 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               const float2 t3 = fma2(fd3, nR3, s.lo3);
               const float resA = fmaxf(s.qn3.x, fminf(s.qx3.x, t3.x));
               const float resB = fmaxf(s.qn3.y, fminf(s.qx3.y, t3.y));
-              if ((stA || stB) && q < nq) {
-                float *p = fn[q] + (long long)a0 + (long long)(jo + nb - 1) * ld1;
-                if (stA) p[0] = resA;
-                if (stB) p[1] = resB;
-                if (images) {
-                  if (stA && iA <= images) p[ii] = resA;
-                  if (stA && iA > ii - images) p[-ii] = resA;
-                  if (stB && iB <= images) p[1 + ii] = resB;
-                  if (stB && iB > ii - images) p[1 - ii] = resB;
-                }
-              }
+              res[q] = make_float2(resA, resB);
+              if (!kLateStore && (stA || stB) && q < nq) store_row(q, resA, resB);
               // shift the pipeline one row
               s.lx3 = lx2;
               s.ly3 = ly2;
@@ -482,17 +489,8 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               const float2 t3 = fma2(fd3, nR3, s.lo3);
               const float resA = fmaxf(s.mn3.x, fminf(s.mx3.x, t3.x));
               const float resB = fmaxf(s.mn3.y, fminf(s.mx3.y, t3.y));
-              if ((stA || stB) && q < nq) {
-                float *p = fn[q] + (long long)a0 + (long long)(jo + nb - 1) * ld1;
-                if (stA) p[0] = resA;
-                if (stB) p[1] = resB;
-                if (images) {
-                  if (stA && iA <= images) p[ii] = resA;
-                  if (stA && iA > ii - images) p[-ii] = resA;
-                  if (stB && iB <= images) p[1 + ii] = resB;
-                  if (stB && iB > ii - images) p[1 - ii] = resB;
-                }
-              }
+              res[q] = make_float2(resA, resB);
+              if (!kLateStore && (stA || stB) && q < nq) store_row(q, resA, resB);
               // shift the pipeline one row
               s.lx3 = lx2;
               s.ly3 = ly2;
@@ -517,6 +515,11 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               s.fB1 = fB0;
               s.f1 = f0[q];
             }
+            }
+            if (kLateStore && (stA || stB)) {
+#pragma unroll
+              for (int q = 0; q < NQ; q++)
+                if (q < nq) store_row(q, res[q].x, res[q].y);
             }
             // shared per-row state
             L3 = L2;
