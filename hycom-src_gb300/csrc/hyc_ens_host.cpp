@@ -469,7 +469,8 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
   cudaError_t c;
   if (e->prec == HYC_PREC_MIXED && is_col2(e->shape))
     c = hyc::launch_mix_col2(advtyp, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm,
-                             std::min(e->strip_nq, e->maxntr), e->prep64, e->d_err, st);
+                             e->strip_nq == 3 ? (e->maxntr > 1 ? 3 : 1) : std::min(e->strip_nq, e->maxntr),
+                             e->prep64, e->d_err, st);
   else if (e->prec != HYC_PREC_MIXED && (advtyp == 0 || advtyp == 1)) {
     // FP64 PCM/MPDATA: the plain form's tile kernel per basin, then the periodic halo
     c = cudaSuccess;
@@ -853,8 +854,8 @@ int hyc_ens_set_option(hyc_ens *e, int32_t option, int32_t value) {
     return HYC_OK;
   }
   if (option == HYC_OPT_STRIP_TRACERS) {
-    if (e->prec != HYC_PREC_MIXED || (value != 1 && value != 2))
-      return efail(e, HYC_ERR_ARG, "HYC_OPT_STRIP_TRACERS: 1 or 2, mixed form");
+    if (e->prec != HYC_PREC_MIXED || value < 1 || value > 3)
+      return efail(e, HYC_ERR_ARG, "HYC_OPT_STRIP_TRACERS: 1, 2 or 3 (warp pairs), mixed form");
     if (e->strip_nq != value && e->gexec) {
       cudaGraphExecDestroy(e->gexec);
       e->gexec = nullptr;
@@ -1023,6 +1024,8 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
   std::vector<std::pair<hyc::TileShape, int>> trials;
   for (const auto &c : cands) {
     if (!shape_ok(e, c) || !scheme_ok(e, advtyp, c)) continue;
+    // (warp pairs, HYC_OPT_STRIP_TRACERS = 3, measured 15 % slower than two
+    // tracers per warp on every shape: not a trial)
     if (is_col2(c) && e->maxntr > 1) trials.push_back({c, 1});
     trials.push_back({c, 2});
   }

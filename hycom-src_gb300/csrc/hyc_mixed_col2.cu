@@ -150,30 +150,76 @@ constexpr bool kLateStore = true;
 
 }  // namespace
 
-template <int SCHEME, int NQ, bool PREP64>
-__global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
+// PAIR: two warps share one ring and one item, each advancing one of the
+// pass's two tracers (one tracer of pipeline state per warp: fewer
+// registers, 3 CTAs and 12 warps per SM instead of 8, the inputs of a row
+// still read once).  The even warp takes items from the queue and hands
+// them to its partner through a shared-memory mailbox (mbarriers ibar /
+// tbar), issues the TMA blocks, and refills a slot only after both warps
+// have released it (mbarrier empty, two arrivals).  Every wait is bounded.
+template <int SCHEME, int NQ, bool PREP64, bool PAIR>
+struct Col2Geom {
+  static constexpr int NI = PAIR ? 2 : NQ;  // tracers in the ring per pass
+  using RG = Ring<SCHEME, NI, PREP64>;
+  static constexpr int NRING = PAIR ? kWarps / 2 : kWarps;
+  static constexpr int NBAR = PAIR ? 2 * kNS + 3 : kNS;  // full[kNS], empty[kNS], ibar, tbar, mailbox
+  static constexpr size_t SMEM = (size_t)NRING * RG::WARP + (size_t)NRING * NBAR * 8 + 128;
+};
+
+template <int SCHEME, int NQ, bool PREP64, bool PAIR = false>
+__global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
     mix_col2_kernel(const MixBasin *__restrict__ basins, const int4 *__restrict__ items, int nitems, int *head,
                     int *err) {
-  using RG = Ring<SCHEME, NQ, PREP64>;
+  static_assert(!PAIR || NQ == 1, "a warp of a pair advances one tracer");
+  using GE = Col2Geom<SCHEME, NQ, PREP64, PAIR>;
+  using RG = typename GE::RG;
+  constexpr int NI = GE::NI;
   constexpr bool MP = SCHEME == kMPDATA;
   using St = typename std::conditional<MP, StM, St2>::type;
   extern __shared__ unsigned char c2raw_[];
   unsigned char *sm = (unsigned char *)(((uintptr_t)c2raw_ + 127) & ~(uintptr_t)127);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  unsigned char *ring = sm + wid * RG::WARP;
-  uint64_t *bar = (uint64_t *)(sm + kWarps * RG::WARP) + wid * kNS;
-  if (lane == 0) {
+  const int owner = PAIR ? (wid >> 1) : wid, sub = PAIR ? (wid & 1) : 0;
+  const bool lead = !PAIR || sub == 0;  // takes items and issues the copies
+  unsigned char *ring = sm + owner * RG::WARP;
+  uint64_t *bar = (uint64_t *)(sm + GE::NRING * RG::WARP) + owner * GE::NBAR;  // full[kNS]
+  uint64_t *empty = bar + kNS, *ibar = bar + 2 * kNS, *tbar = ibar + 1;
+  int *mailbox = (int *)(tbar + 1);
+  if (lead && lane == 0) {
     for (int s = 0; s < kNS; s++) tma::bar_init(bar + s, 1);
+    if (PAIR) {
+      for (int s = 0; s < kNS; s++) tma::bar_init(empty + s, 2);
+      tma::bar_init(ibar, 1);
+      tma::bar_init(tbar, 1);
+    }
     tma::fence_bar_init();
   }
-  __syncwarp();
+  if (PAIR)
+    __syncthreads();  // the partner warps use the barriers their lead initialised
+  else
+    __syncwarp();
   uint32_t tg = 0;  // blocks this warp has consumed (slot and phase of the next one)
+  uint32_t ni = 0;  // items handed over within the pair
   const float onemu = (float)kOnemu;
 
   for (;;) {
     int it = 0;
-    if (lane == 0) it = atomicAdd(head, 1);
+    if (!PAIR) {
+      if (lane == 0) it = atomicAdd(head, 1);
+    } else if (lane == 0) {
+      if (lead) {
+        // the partner has read the previous item before the mailbox is reused
+        const bool okx = ni == 0 || tma::wait(tbar, (ni - 1) & 1u, err);
+        it = okx ? atomicAdd(head, 1) : nitems;
+        *(volatile int *)mailbox = it;
+        tma::arrive(ibar);
+      } else {
+        it = tma::wait(ibar, ni & 1u, err) ? *(volatile int *)mailbox : nitems;
+        tma::arrive(tbar);
+      }
+    }
     it = __shfl_sync(kFull, it, 0);
+    ni++;
     if (it >= nitems) break;
     const int4 w = items[it];
     const MixBasin &B = basins[w.x];
@@ -183,7 +229,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     const int s0 = 56 * w.y;  // strip start (padded column)
     const int j0 = 1 + w.z * B.seg, j1 = min(j0 + B.seg, jj + 1);
     const int nblk = (j1 - j0 + 6 + kRB - 1) / kRB;
-    const int nqp = (ntr + NQ - 1) / NQ;
+    const int nqp = (ntr + NI - 1) / NI;
     const int ka = w.w * B.kchunk, kb = min(kdm, ka + B.kchunk);  // this item's layers
     const int T = (kb - ka) * nqp * nblk;
     // this lane's columns: padded a0 = s0 + 2*lane (A) and a0 + 1 (B)
@@ -192,19 +238,21 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     const bool outA = lane >= 2 && lane < 30 && iA >= 1 && iA <= ii;
     const bool outB = lane >= 2 && lane < 30 && iB >= 1 && iB <= ii;
 
-    auto issue = [&](int t) {  // lane 0: block t of this item into its slot
+    auto issue = [&](int t) -> bool {  // lane 0 of the lead: block t of this item into its slot
       const int kk = t / (nqp * nblk);
       const int rem = t - kk * nqp * nblk;
       const int k = ka + kk;
       const int qp = rem / nblk, blk = rem - qp * nblk;
       const int y = j0 - 3 + blk * kRB + nb - 1;
       const uint32_t g = tg + t;
+      // PAIR: both warps have released the slot's previous block
+      if (PAIR && g >= (uint32_t)kNS && !tma::wait(empty + (g % kNS), ((g / kNS) - 1) & 1u, err)) return false;
       unsigned char *slot = ring + (g % kNS) * RG::SLOT;
       uint64_t *b = bar + (g % kNS);
       tma::expect_tx(b, RG::TX_BYTES);
 #pragma unroll
-      for (int q = 0; q < NQ; q++) {
-        const int qq = min(qp * NQ + q, ntr - 1);
+      for (int q = 0; q < NI; q++) {
+        const int qq = min(qp * NI + q, ntr - 1);
         tma::load3(slot + RG::OFF_FO + q * kRB * RG::FROW, B.c2_old, b, s0, y, qq * kdm + k);
         if (!MP) tma::load3(slot + RG::OFF_FC + q * kRB * RG::FROW, B.c2_cur, b, s0, y, qq * kdm + k);
       }
@@ -213,24 +261,35 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
       tma::load3(slot + RG::OFF_DP, B.c2_dp, b, s0, y, k);
       tma::load2(slot + RG::OFF_GE, B.c2_ge, b, 4 * s0, y);
       if (PREP64) tma::load2(slot + RG::OFF_SI, B.c2_si, b, s0, y);
+      return true;
     };
-    if (lane == 0)
-      for (int t = 0; t < kNS && t < T; t++) issue(t);
+    int nissued = 0;  // lead lane 0: blocks of this item in flight
+    if (lead && lane == 0)
+      while (nissued < kNS && nissued < T && issue(nissued)) nissued++;
+    const bool short_issue = lead && nissued < kNS && nissued < T;  // meaningful on lane 0 only
+    if (__shfl_sync(kFull, short_issue ? 1 : 0, 0) != 0) {
+      // PAIR: the partner stopped releasing slots; let the copies in flight land, then stop
+      if (lead && lane == 0)
+        for (int d = 0; d < nissued; d++) tma::wait(bar + ((tg + d) % kNS), ((tg + d) / kNS) & 1u, nullptr);
+      return;
+    }
 
     int t = 0;
     bool ok = true;
     for (int k = ka; k < kb && ok; k++) {
       for (int qp = 0; qp < nqp && ok; qp++) {
-        const int nq = min(NQ, ntr - qp * NQ);
+        // this warp's tracers of the pass: qp*NQ + q, or (PAIR) the partner's slot sub
+        const int qb = PAIR ? qp * 2 + sub : qp * NQ;
+        const int nq = PAIR ? (qb < ntr ? 1 : 0) : min(NQ, ntr - qp * NQ);
         float *fn[NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; q++) fn[q] = fnew + ((long long)(qp * NQ + (q < nq ? q : 0)) * kdm + k) * sl;
+        for (int q = 0; q < NQ; q++) fn[q] = fnew + ((long long)min(qb + (q < nq ? q : 0), ntr - 1) * kdm + k) * sl;
         St S[NQ];
         float P[NQ];  // posdef of each tracer of the pass (MPDATA)
 #pragma unroll
         for (int q = 0; q < NQ; q++) {
           S[q] = St{};
-          P[q] = B.posdef[min(qp * NQ + q, ntr - 1)];
+          P[q] = B.posdef[min(qb + q, ntr - 1)];
         }
         const float2 z2 = make_float2(0.f, 0.f);
         float2 u1 = z2, u1m = z2, v1 = z2, R2 = z2, nR3 = z2, QF2 = z2, DS1 = z2, DS2 = z2, DS3 = z2, QS1 = z2;
@@ -259,8 +318,9 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
             float2 f0[NQ], c0[NQ];
 #pragma unroll
             for (int q = 0; q < NQ; q++) {
-              f0[q] = ((const float2 *)(slot + RG::OFF_FO + (q * kRB + rr) * RG::FROW))[lane];
-              c0[q] = MP ? z2 : ((const float2 *)(slot + RG::OFF_FC + (q * kRB + rr) * RG::FROW))[lane];
+              const int qr = PAIR ? sub : q;  // ring row of this tracer
+              f0[q] = ((const float2 *)(slot + RG::OFF_FO + (qr * kRB + rr) * RG::FROW))[lane];
+              c0[q] = MP ? z2 : ((const float2 *)(slot + RG::OFF_FC + (qr * kRB + rr) * RG::FROW))[lane];
             }
 
             // ---- thickness factors of row J-1 (mod_tsadvc.F90:1905-1942)
@@ -544,7 +604,19 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
             dB1 = d0.y;
           }
           __syncwarp();  // every lane is done with the slot before it is refilled
-          if (lane == 0 && t + kNS < T) issue(t + kNS);
+          if (PAIR && lane == 0) tma::arrive(empty + (g % kNS));
+          if (lead) {
+            bool okw = true;
+            if (lane == 0 && t + kNS < T) okw = issue(t + kNS);
+            if (!__shfl_sync(kFull, okw, 0)) {
+              // the partner stopped: the copies already in flight land, then stop
+              for (int d = 1; d < kNS && t + d < T; d++)
+                tma::wait(bar + ((g + d) % kNS), ((g + d) / kNS) & 1u, nullptr);
+              ok = false;
+              t++;
+              break;
+            }
+          }
         }
       }
     }
@@ -597,6 +669,13 @@ cudaError_t launch_mix_col2(int scheme, const MixBasin *basins, const int4 *item
     return cudaGetLastError();
   };
 #define HYC_COL2(S, Q, P) pick(mix_col2_kernel<S, Q, P>, Ring<S, Q, P>::SMEM)
+#define HYC_PAIR(S, P) pick(mix_col2_kernel<S, 1, P, true>, Col2Geom<S, 1, P, true>::SMEM)
+  if (nq == 3) {  // warp pairs, one tracer per warp
+    if (scheme == kFCT2) return prep64 ? HYC_PAIR(kFCT2, true) : HYC_PAIR(kFCT2, false);
+    if (scheme == kMPDATA) return prep64 ? HYC_PAIR(kMPDATA, true) : HYC_PAIR(kMPDATA, false);
+    return cudaErrorInvalidValue;
+  }
+#undef HYC_PAIR
   if (scheme == kFCT2) {
     if (nq >= 2) return prep64 ? HYC_COL2(kFCT2, 2, true) : HYC_COL2(kFCT2, 2, false);
     return prep64 ? HYC_COL2(kFCT2, 1, true) : HYC_COL2(kFCT2, 1, false);

@@ -21,6 +21,10 @@ __device__ __forceinline__ void fence_bar_init() { asm volatile("fence.mbarrier_
 __device__ __forceinline__ void expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sa(bar)), "r"(bytes) : "memory");
 }
+// one arrival (release) on an mbarrier
+__device__ __forceinline__ void arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sa(bar)) : "memory");
+}
 __device__ __forceinline__ bool try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(

@@ -544,7 +544,8 @@ class Ensemble(_StreamFollower):
         self._chk(lib().hyc_ens_set_posdef(self._h, b, q, float(posdef)))
 
     def set_strip_tracers(self, n: int):
-        """Two-column strip kernel: tracers advanced per pass (1 or 2)."""
+        """Two-column strip kernel: tracers advanced per pass (1 or 2), or 3:
+        two warps per staged block, one tracer each."""
         self._chk(lib().hyc_ens_set_option(self._h, 3, int(n)))
 
     def option(self, name: str) -> int:

@@ -462,9 +462,13 @@ int hyc_ens_stats(hyc_ens *ens, hyc_stats *out, int32_t reset);
  * plain loads (0). */
 #define HYC_OPT_TMA 2
 /* HYC_OPT_STRIP_TRACERS (mixed form, two-column strip kernel; default 2):
- * tracers advanced per pass over a layer.  2 shares the per-cell thickness
- * factors between two tracers; 1 needs fewer registers, so more warps fit
- * on an SM.  hyc_ens_tune tries both. */
+ * tracers advanced per pass over a layer.  2: one warp advances two
+ * tracers and shares the per-cell thickness factors between them; 1: one
+ * tracer per pass, fewer registers, more warps per SM; 3: two warps share
+ * a staged block and advance one tracer each (the inputs of a row are
+ * read once, and 12 warps fit on an SM instead of 8; each warp forms the
+ * thickness factors itself, which costs more than the extra warps gain:
+ * measured 15 % slower than 2).  hyc_ens_tune tries 1 and 2. */
 #define HYC_OPT_STRIP_TRACERS 3
 int hyc_ens_set_option(hyc_ens *ens, int32_t option, int32_t value);
 /*

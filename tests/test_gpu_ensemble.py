@@ -193,14 +193,16 @@ def test_mixed_kernels_agree(cuda, prep64):
     cell; contraction, the approximate reciprocal in the limiter ratios and
     the FP64 reciprocal's Newton step may differ by a few ulp)."""
     outs = []
-    for mode in ("col2-32", "col2-64", "col2-128", "col2-64-1", "col", "tma", "tile"):
+    modes = ("col2-32", "col2-64", "col2-128", "col2-64-1", "col", "tma", "tile", "col2-64-3", "col2-256-3")
+    for mode in modes:
         members = make_members()
         ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
         ens.set_prep64(prep64)
         if mode.startswith("col2"):
             ens.set_tile(56, int(mode.split("-")[1]))
-            ens.set_strip_tracers(1 if mode.endswith("-1") else 2)
-            assert ens.option("strip_tracers") == (1 if mode.endswith("-1") else 2)
+            nq = int(mode.split("-")[2]) if mode.count("-") == 2 else 2
+            ens.set_strip_tracers(nq)
+            assert ens.option("strip_tracers") == nq
         elif mode == "col":
             ens.set_tile(26, 32)
         else:
@@ -216,6 +218,11 @@ def test_mixed_kernels_agree(cuda, prep64):
         for o in outs[1:]:
             d = np.abs(o[i][..., ip] - outs[0][i][..., ip]).max() / np.abs(outs[0][i][..., ip]).max()
             assert d < 1e-6, (i, d)
+        # warp pairs run the one-tracer pipeline on the same staged rows: the
+        # same values as one tracer per pass, for any segment height
+        one = outs[modes.index("col2-64-1")][i]
+        for mode in ("col2-64-3", "col2-256-3"):
+            assert np.array_equal(outs[modes.index(mode)][i], one), (i, mode)
 
 
 def test_put_get_slices(cuda):
@@ -317,14 +324,16 @@ def test_fp64_ensemble_pcm_mpdata_bitwise(cuda, advtyp):
     ens.close()
 
 
-@pytest.mark.parametrize("prep64", [True, False])
-def test_mixed_mpdata_one_step_error(cuda, prep64):
+@pytest.mark.parametrize("prep64,nq", [(True, 2), (False, 2), (False, 3)])
+def test_mixed_mpdata_one_step_error(cuda, prep64, nq):
     """One FP32-mixed MPDATA step (two-column strip kernel, posdef handled
-    outside the FP32 values) is within 1e-6 of the FP64 oracle relative to
-    each tracer's max |value|, for temp (posdef 256) and saln (posdef 0)."""
+    outside the FP32 values; nq = 3: warp pairs) is within 1e-6 of the FP64
+    oracle relative to each tracer's max |value|, for temp (posdef 256) and
+    saln (posdef 0)."""
     members = make_ts_members()
     ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
     ens.set_prep64(prep64)
+    ens.set_strip_tracers(nq)
     for i in range(len(members)):
         ens.set_posdef(i, 0, 256.0)
     load(ens, members)
