@@ -313,8 +313,10 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
             ms = float(t.item())
         ms /= args.steps
         ws = dist.get_world_size() if dist else 1
-        s_t = 8 if prec == "fp64" else 4  # fluxes as the tracers; dp stays FP64 in both
-        bpu = bytes_per_update(s_t, s_t, 8, 2, kdm)
+        s_t = 8 if prec == "fp64" else 4  # fluxes as the tracers
+        # dp: FP64, except that the strip kernel with the FP32 thickness prep stages the FP32 copy made at put
+        s_dp = 4 if (prec == "mixed" and not ENS_FORMS[form][1] and tx == 56) else 8
+        bpu = bytes_per_update(s_t, s_t, s_dp, 2, kdm)
         ach = ups_step * bpu / (ms / 1e3) / 1e9
         out[form] = {"value": ws * ups_step / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "tile": [tx, ty],
                      "tracers_per_pass": nq, "kernel": KERNEL_OF_TILE.get(tx, "fct tile kernel"),
@@ -852,7 +854,8 @@ def run_ensemble_workload(args, wl, dev):
             dist.barrier()
         ms = reduce([e0.elapsed_time(e1) / steps], dist.ReduceOp.MAX if dist else None)[0]
         s_t = 8 if prec == "fp64" else 4
-        nbytes = sum(s["idm"] * s["jdm"] * s["kdm"] * s["ntr"] * bytes_per_update(s_t, s_t, 8, s["ntr"], s["kdm"])
+        s_dp = 4 if (form == "mixed-fp32prep" and tx == 56) else 8  # the strip kernel stages dp in FP32 then
+        nbytes = sum(s["idm"] * s["jdm"] * s["kdm"] * s["ntr"] * bytes_per_update(s_t, s_t, s_dp, s["ntr"], s["kdm"])
                      for s in specs)
         nbytes = reduce([nbytes], dist.ReduceOp.SUM if dist else None)[0]
         ach = nbytes / (ms / 1e3) / 1e9
@@ -1026,8 +1029,9 @@ def run_c4(args, wl, dev):
             del ens
             torch.cuda.empty_cache()
         rate = t_ups / (t_ms / 1e3)
+        s_dp = 4 if tile[0] == 56 else 8  # FP32 prep: the strip kernel stages dp in FP32
         nbytes = sum(sp["idm"] * sp["jdm"] * sp["kdm"] * sp["ntr"] *
-                     (bytes_per_update(4, 4, 8, sp["ntr"], sp["kdm"]) - (4 if adv == 1 else 0)) for sp in specs)
+                     (bytes_per_update(4, 4, s_dp, sp["ntr"], sp["kdm"]) - (4 if adv == 1 else 0)) for sp in specs)
         ach = nbytes * (t_ups / ups_step) / (t_ms / 1e3) / 1e9
         res[name] = {"value": rate, "unit": UNIT, "ms_per_step_all_basins": t_ms / (gsteps * reps), "tile": list(tile),
                      "tracers_per_pass": nq, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,

@@ -38,7 +38,7 @@ struct MixBasin {
   // two-column strip kernel: TMA maps (box 64 x 4 rows) of the old and
   // centre levels, uflx, vflx, dp, the per-cell factors (float4 as 4*ld1
   // floats per row) and dt2*scp2i (FP64)
-  const CUtensorMap *c2_old, *c2_cur, *c2_u, *c2_v, *c2_dp, *c2_ge, *c2_si;
+  const CUtensorMap *c2_old, *c2_cur, *c2_u, *c2_v, *c2_dp, *c2_ge, *c2_si, *c2_dp32;
 };
 
 bool mix_shape_ok(TileShape t);

@@ -29,6 +29,7 @@ struct EBasin {
   double *scp2 = nullptr, *scp2i = nullptr;
   void *uflx = nullptr, *vflx = nullptr;  // FP32 (mixed) or FP64
   double *dp = nullptr;
+  float *dp32 = nullptr;  // dp rounded to FP32 at put (mixed form): the strip kernel's FP32 thickness prep
   void *lev[3] = {nullptr, nullptr, nullptr};  // tracer state, physical levels
   float2 *dsqs = nullptr;                       // column kernel metric factors (mixed form)
   double *dtsi = nullptr;                       // dt2*scp2i (strip kernel, FP64 thickness prep)
@@ -53,7 +54,7 @@ struct hyc_ens {
   int maxntr = 1;        // largest tracer count (column kernel processes tracers in pairs)
   int strip_nq = 2;      // two-column strip kernel: tracers per pass (1 or 2)
   CUtensorMap *d_tmaps = nullptr;  // [nbasin][6]: level 0,1,2, uflx, vflx, dp
-  CUtensorMap *d_cmaps = nullptr;  // [nbasin][8]: strip kernel maps (levels 0-2, u, v, dp, geo4, si)
+  CUtensorMap *d_cmaps = nullptr;  // [nbasin][9]: strip kernel maps (levels 0-2, u, v, dp, geo4, si, dp32)
   int tm_tx = 0, tm_ty = 0;        // shape the maps were encoded for
   int *d_err = nullptr;            // device error flag (bounded waits that gave up)
   // device tables, one per rotation
@@ -147,6 +148,7 @@ void free_all(hyc_ens *e) {
     cudaFree(b.uflx);
     cudaFree(b.vflx);
     cudaFree(b.dp);
+    cudaFree(b.dp32);
     cudaFree(b.dsqs);
     cudaFree(b.dtsi);
     cudaFree(b.geo4);
@@ -232,10 +234,10 @@ bool encode2t(CUtensorMap *m, void *base, CUtensorMapDataType dt, size_t es, int
 int encode_strip_maps(hyc_ens *e) {
   const int bx = hyc::kCol2Box, by = hyc::kCol2Rows;
   const CUtensorMapDataType F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32, F64 = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
-  std::vector<CUtensorMap> h(e->b.size() * 8);
+  std::vector<CUtensorMap> h(e->b.size() * 9);
   for (size_t i = 0; i < e->b.size(); i++) {
     EBasin &b = e->b[i];
-    CUtensorMap *m = &h[i * 8];
+    CUtensorMap *m = &h[i * 9];
     bool ok = true;
     for (int l = 0; l < 3; l++) ok &= encode3t(m + l, b.lev[l], F32, 4, b.ld1, b.ld2, (long long)b.ntr * b.kdm, bx, by);
     ok &= encode3t(m + 3, b.uflx, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
@@ -243,6 +245,7 @@ int encode_strip_maps(hyc_ens *e) {
     ok &= encode3t(m + 5, b.dp, F64, 8, b.ld1, b.ld2, b.kdm, bx, by);
     ok &= encode2t(m + 6, b.geo4, F32, 4, 4 * b.ld1, b.ld2, 4 * bx, by);
     ok &= encode2t(m + 7, b.dtsi, F64, 8, b.ld1, b.ld2, bx, by);
+    ok &= encode3t(m + 8, b.dp32, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
     if (!ok) return efail(e, HYC_ERR_CUDA, "cuTensorMapEncodeTiled failed for the strip maps (basin %zu)", i);
   }
   ECK(cudaMemcpy(e->d_cmaps, h.data(), h.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "strip maps copy");
@@ -332,7 +335,7 @@ int build_tables(hyc_ens *e, double dt2) {
         for (int q = 0; q < b.ntr && q < hyc::kMaxFields; q++) m.posdef[q] = (float)b.posdef[q];
         m.dsqs = b.dsqs;
         if (e->d_cmaps) {
-          const CUtensorMap *c = e->d_cmaps + i * 8;
+          const CUtensorMap *c = e->d_cmaps + i * 9;
           m.c2_old = c + lo;
           m.c2_cur = c + lc;
           m.c2_u = c + 3;
@@ -340,6 +343,7 @@ int build_tables(hyc_ens *e, double dt2) {
           m.c2_dp = c + 5;
           m.c2_ge = c + 6;
           m.c2_si = c + 7;
+          m.c2_dp32 = c + 8;
         }
         if (e->d_tmaps) {
           m.tm_old = e->d_tmaps + i * 6 + lo;
@@ -587,7 +591,8 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
     if (ok && precision == HYC_PREC_MIXED)
       ok = cudaMalloc(&b.dsqs, b.slice * sizeof(float2)) == cudaSuccess &&
            cudaMalloc(&b.dtsi, b.slice * sizeof(double)) == cudaSuccess &&
-           cudaMalloc(&b.geo4, b.slice * sizeof(float4)) == cudaSuccess;
+           cudaMalloc(&b.geo4, b.slice * sizeof(float4)) == cudaSuccess &&
+           cudaMalloc(&b.dp32, b.slice * b.kdm * sizeof(float)) == cudaSuccess;
     e->b.push_back(b);
     if (!ok) return bail(efail(nullptr, HYC_ERR_NOMEM, "basin %d: device allocation failed", i));
     EBasin &bb = e->b.back();
@@ -596,7 +601,8 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
               cudaMemcpy(bb.scp2i, si.data(), bb.slice * 8, cudaMemcpyHostToDevice) == cudaSuccess &&
               cudaMemset(bb.uflx, 0, bb.slice * bb.kdm * es) == cudaSuccess &&
               cudaMemset(bb.vflx, 0, bb.slice * bb.kdm * es) == cudaSuccess &&
-              cudaMemset(bb.dp, 0, bb.slice * bb.kdm * 8) == cudaSuccess;
+              cudaMemset(bb.dp, 0, bb.slice * bb.kdm * 8) == cudaSuccess &&
+              (!bb.dp32 || cudaMemset(bb.dp32, 0, bb.slice * bb.kdm * 4) == cudaSuccess);
     for (int l = 0; l < 3 && cp; l++) cp = cudaMemset(bb.lev[l], 0, bb.slice * bb.kdm * bb.ntr * es) == cudaSuccess;
     if (!cp) return bail(efail(nullptr, HYC_ERR_CUDA, "basin %d: upload failed", i));
   }
@@ -616,7 +622,7 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
     if (all6 && encode_fn() && cudaMalloc(&e->d_tmaps, nbasin * 6 * sizeof(CUtensorMap)) == cudaSuccess)
       e->use_tma = true;
     e->shape = hyc::TileShape{hyc::kColStrip, 64};  // column-strip kernel
-    if (encode_fn() && cudaMalloc(&e->d_cmaps, nbasin * 8 * sizeof(CUtensorMap)) == cudaSuccess) {
+    if (encode_fn() && cudaMalloc(&e->d_cmaps, nbasin * 9 * sizeof(CUtensorMap)) == cudaSuccess) {
       if (encode_strip_maps(e) == HYC_OK) {
         e->shape = hyc::TileShape{hyc::kCol2Strip, 128};  // two-column strip kernel
       } else {
@@ -762,6 +768,9 @@ static int move(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns_
       if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put halo: %s", cudaGetErrorString(c));
     }
     c = hyc::launch_repitch(stage, 0, b.ld1r, rsl, dst, dfp32, b.ld1, b.slice, b.ld1r, b.ld2, ns, e->stream);
+    if (c == cudaSuccess && what == HYC_E_DP && b.dp32)  // the FP32 copy the strip kernel stages
+      c = hyc::launch_repitch(stage, 0, b.ld1r, rsl, b.dp32 + (size_t)s0 * b.slice, 1, b.ld1, b.slice, b.ld1r, b.ld2,
+                              ns, e->stream);
     if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put: %s", cudaGetErrorString(c));
     span_close(e, t1, HYC_T_XCTILR, e->stream);
     ECK(cudaEventRecord(e->ev_used[q], e->stream), "event");

@@ -56,8 +56,8 @@ struct Ring {
   static constexpr int OFF_FC = OFF_FO + NQ * kRB * FROW;
   static constexpr int OFF_U = OFF_FC + NC * kRB * FROW;
   static constexpr int OFF_V = OFF_U + kRB * FROW;
-  static constexpr int OFF_DP = OFF_V + kRB * FROW;        // double per cell
-  static constexpr int OFF_GE = OFF_DP + kRB * kW * 8;     // float4 per cell
+  static constexpr int OFF_DP = OFF_V + kRB * FROW;        // dp: double (PREP64) or float per cell
+  static constexpr int OFF_GE = OFF_DP + kRB * kW * (PREP64 ? 8 : 4);  // float4 per cell
   static constexpr int OFF_SI = OFF_GE + kRB * kW * 16;    // double per cell (PREP64)
   static constexpr int TX_BYTES = OFF_SI + (PREP64 ? kRB * kW * 8 : 0);
   static constexpr int SLOT = (TX_BYTES + 127) / 128 * 128;
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
       }
       tma::load3(slot + RG::OFF_U, B.c2_u, b, s0, y, k);
       tma::load3(slot + RG::OFF_V, B.c2_v, b, s0, y, k);
-      tma::load3(slot + RG::OFF_DP, B.c2_dp, b, s0, y, k);
+      tma::load3(slot + RG::OFF_DP, PREP64 ? B.c2_dp : B.c2_dp32, b, s0, y, k);
       tma::load2(slot + RG::OFF_GE, B.c2_ge, b, 4 * s0, y);
       if (PREP64) tma::load2(slot + RG::OFF_SI, B.c2_si, b, s0, y);
       return true;
@@ -296,7 +296,9 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
         float2 v1m = z2, H2 = z2;  // MPDATA: masked v of row J-1, fco+fcn of row J-2
         float2 L1 = z2, L2 = z2, L3 = z2;  // land flags (1 = land) of rows J-1, J-2, J-3
         float L2e = 0.f;                   // land flag east of column B, row J-2
-        double dA1 = 0.0, dB1 = 0.0, sA1 = 0.0, sB1 = 0.0;
+        using DT = typename std::conditional<PREP64, double, float>::type;
+        DT dA1 = 0, dB1 = 0;
+        double sA1 = 0.0, sB1 = 0.0;
         for (int blk = 0; blk < nblk; blk++, t++) {
           const uint32_t g = tg + t;
           if (!__all_sync(kFull, tma::wait(bar + (g % kNS), (g / kNS) & 1u, err))) {
@@ -312,7 +314,9 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
             // ---- inputs of row J
             const float2 u0 = ((const float2 *)(slot + RG::OFF_U + rr * RG::FROW))[lane];
             const float2 v0 = ((const float2 *)(slot + RG::OFF_V + rr * RG::FROW))[lane];
-            const double2 d0 = ((const double2 *)(slot + RG::OFF_DP + rr * kW * 8))[lane];
+            // dp as staged: FP64 for the FP64 prep, FP32 (rounded at put) for the FP32 one
+            using DT2 = typename std::conditional<PREP64, double2, float2>::type;
+            const DT2 d0 = ((const DT2 *)(slot + RG::OFF_DP + rr * kW * sizeof(DT2) / 2))[lane];
             const float4 gA = ((const float4 *)(slot + RG::OFF_GE + rr * kW * 16))[2 * lane];
             const float4 gB = ((const float4 *)(slot + RG::OFF_GE + rr * kW * 16))[2 * lane + 1];
             float2 f0[NQ], c0[NQ];
