@@ -409,7 +409,8 @@ int hyc_ens_get(hyc_ens *ens, int32_t basin, int32_t what, double *dst, int32_t 
  * As hyc_ens_get, but returns once the values are staged on the device:
  * the copy into dst runs on a copy stream of the ensemble and overlaps the
  * puts and steps queued after it (host<->device links are full duplex).
- * dst must stay valid and is not to be read until hyc_ens_wait returns.
+ * dst must stay valid and is not to be read (nor passed to hyc_ens_put)
+ * until hyc_ens_wait returns.
  * A later get_async waits for the previous one's copy-out on the device.
  */
 int hyc_ens_get_async(hyc_ens *ens, int32_t basin, int32_t what, double *dst, int32_t where);
