@@ -395,3 +395,43 @@ def test_get_async_overlaps_and_equals_get(cuda):
         assert np.array_equal(pinned.numpy(), ref)
         assert np.array_equal(dev.cpu().numpy(), ref)
     ens.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_all_land_basin_beside_a_sea_basin(cuda, prec):
+    """A basin with no sea point (masks all zero) in the same ensemble as an
+    ordinary one: its levels pass through unchanged, and the other basin's
+    step equals the step it takes alone, bit for bit."""
+    members = make_members(SPECS[:1])
+    land = members[0]
+    b = land["b"]
+    spec_land = dict(spec_of(land), ip=np.zeros_like(land["g"].masks["ip"]), iu=np.zeros_like(land["g"].masks["iu"]),
+                     iv=np.zeros_like(land["g"].masks["iv"]))
+    both = hycadv.Ensemble([spec_land, spec_of(members[0])], precision=prec)
+    alone = hycadv.Ensemble([spec_of(members[0])], precision=prec)
+    for ens, idx in ((both, [0, 1]), (alone, [0])):
+        for i in idx:
+            mm, nn = levels(1)
+            m = members[0]
+            ens.put(i, "old", np.ascontiguousarray(m["trc"][:, nn - 1]))
+            ens.put(i, "cur", np.ascontiguousarray(m["trc"][:, mm - 1]))
+            ens.put(i, "uflx", np.ascontiguousarray(m["c"]["uflx"]))
+            ens.put(i, "vflx", np.ascontiguousarray(m["c"]["vflx"]))
+            ens.put(i, "dp", np.ascontiguousarray(m["c"]["dp"][nn - 1]))
+        ens.step(2, DELT1, 1)
+    m = members[0]
+    shape = (m["ntr"] * m["kdm"], b.ld2, b.ld1)
+    got_land, got_sea, want = np.zeros(shape), np.zeros(shape), np.zeros(shape)
+    both.get(0, "cur", got_land)
+    both.get(1, "cur", got_sea)
+    alone.get(0, "cur", want)
+    mm, _ = levels(1)
+    cur = m["trc"][:, mm - 1].reshape(shape)
+    if prec == "mixed":  # stored in FP32
+        cur = cur.astype(np.float32).astype(np.float64)
+    inner = np.zeros((b.ld2, b.ld1), bool)
+    inner[b.J, b.I] = True
+    assert np.array_equal(got_land[:, inner], cur[:, inner])
+    assert np.array_equal(got_sea, want)
+    both.close()
+    alone.close()
