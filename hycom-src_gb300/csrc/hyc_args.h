@@ -113,6 +113,7 @@ struct CnuityArgs {
   double *uflxav, *vflxav, *dpav;   // (ld1,ld2,kdm) or null
   double *onetacnt;                 // (ld1,ld2), btrmas
   double delt1, ra2fac;
+  double dtinv;                     // 1/delt1, divided once on the host
   double *w;                        // work slices
   long long *keys;                  // 2*kdm dpkmin keys, or null
 };

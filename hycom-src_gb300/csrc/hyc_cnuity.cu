@@ -223,7 +223,21 @@ __global__ void cn_update(const CnuityArgs A, int k, int M, int slot) {
   if (A.keys && slot >= 0) row_min(A, x, in && sea, d, slot);
 }
 
-// loop 77, :595-645 at margin 1: the barotropic correction fluxes of layer k
+// loop 77: RN(1/p(kk+1)) of every sea cell at margin 2, into util1 (free
+// until the interface diffusion).  p(kk+1) does not change during loop 77
+// before its last layer's fluxes are formed, so one reciprocal per cell
+// serves every layer's division dp/p(kk+1).
+__global__ void cn_rpb(const CnuityArgs A) {
+  Cell x;
+  if (!cell_of(A, 2, x)) return;
+  const long long c = x.c;
+  if (!(A.msk[c] & kIP)) return;
+  W(A, W_U1)[c] = 1. / A.p[(long long)A.kdm * A.slice + c];
+}
+
+// loop 77, :595-645 at margin 1: the barotropic correction fluxes of layer k.
+// q = dp/p(kk+1) by div_rcp with the cell's reciprocal: the IEEE quotient
+// bit for bit, for 5 FP64 operations instead of a division.
 __global__ void cn_btflux(const CnuityArgs A, int k) {
   Cell x;
   if (!cell_of(A, 1, x)) return;
@@ -231,17 +245,18 @@ __global__ void cn_btflux(const CnuityArgs A, int k) {
   const uint8_t mk = A.msk[c];
   const int nn = A.n - 1;
   const double *dk = A.dp + ((long long)k + (long long)nn * A.kdm) * sl, *pb = A.p + (long long)A.kdm * sl;
+  const double *rpb = W(A, W_U1);
   if (mk & kIU) {
     const double ut = W(A, W_UTN)[c];
-    const double q = ge0(ut) ? dk[c - 1] / pb[c - 1] : dk[c] / pb[c];
-    const double uf = ut * q;
+    const long long cu = ge0(ut) ? c - 1 : c;
+    const double uf = ut * div_rcp(dk[cu], pb[cu], rpb[cu]);
     W(A, W_UF)[c] = uf;
     A.uflx[(long long)k * sl + c] = A.uflx[(long long)k * sl + c] + uf;
   }
   if (mk & kIV) {
     const double vt = W(A, W_VTN)[c];
-    const double q = ge0(vt) ? dk[c - ld] / pb[c - ld] : dk[c] / pb[c];
-    const double vf = vt * q;
+    const long long cv = ge0(vt) ? c - ld : c;
+    const double vf = vt * div_rcp(dk[cv], pb[cv], rpb[cv]);
     W(A, W_VF)[c] = vf;
     A.vflx[(long long)k * sl + c] = A.vflx[(long long)k * sl + c] + vf;
   }
@@ -317,30 +332,49 @@ __global__ void cn_thk_util(const CnuityArgs A, int k) {
 }
 
 // :838-900 (biharmonic) / :1030-1060 (Laplacian) at margin 4: limited
-// interface fluxes at interface k (1-based)
-__global__ void cn_thk_flux(const CnuityArgs A, int k, int bih, int iflip) {
+// interface fluxes at interface k (1-based).  The per-cell terms of the
+// face bounds, G = .25*(p(kk+1)-p(k))*scp2 and (biharmonic) H =
+// .25*(p(k)-pold)*scp2 (iflip 0) or .25*(pold-p(k))*scp2 (iflip 1), are
+// formed once per cell in shared memory, each by the reference's own
+// operations, and every face takes them from there (each is used by up to
+// four faces): flxhi = G(i), flxlo = -G(i-1) (negation is exact), and the
+// biharmonic bounds uflux + H, uflux - H of the cells the reference names.
+constexpr int kTX = 32, kTY = 8;  // the block of every cnuity launch
+__global__ void __launch_bounds__(kTX * kTY) cn_thk_flux(const CnuityArgs A, int k, int bih, int iflip) {
+  __shared__ double sG[kTY + 1][kTX + 1], sH[kTY + 1][kTX + 1];
   Cell x;
-  if (!cell_of(A, 4, x)) return;
-  const long long c = x.c, sl = A.slice, ld = A.ld1;
-  const uint8_t mk = A.msk[c];
+  const bool in = cell_of(A, 4, x);
+  const int tx = threadIdx.x + 1, ty = threadIdx.y + 1;
+  const long long sl = A.slice, ld = A.ld1;
   const double *pk = A.p + (long long)(k - 1) * sl, *ptop = A.p + (long long)A.kdm * sl;
   const double *pold = W(A, W_POLD), *scp2 = A.scp2;
-  const double dtinv = 1. / A.delt1;
+  auto terms = [&](long long c, int sy, int sx) {
+    sG[sy][sx] = .25 * (ptop[c] - pk[c]) * scp2[c];
+    if (bih) sH[sy][sx] = iflip == 0 ? .25 * (pk[c] - pold[c]) * scp2[c] : .25 * (pold[c] - pk[c]) * scp2[c];
+  };
+  // the box starts at margin 4, so the west and south neighbours of its
+  // first column and row (margin 5) lie inside the array
+  if (in) {
+    terms(x.c, ty, tx);
+    if (tx == 1) terms(x.c - 1, ty, 0);
+    if (ty == 1) terms(x.c - ld, 0, tx);
+  }
+  __syncthreads();
+  if (!in) return;
+  const long long c = x.c;
+  const uint8_t mk = A.msk[c];
+  const double dtinv = A.dtinv;
   double *uk1 = A.uflx + (long long)(k - 2) * sl, *uk = A.uflx + (long long)(k - 1) * sl;
   double *vk1 = A.vflx + (long long)(k - 2) * sl, *vk = A.vflx + (long long)(k - 1) * sl;
+  const double g = sG[ty][tx];
   if (mk & kIU) {
     double *uf = W(A, W_UF);
-    double flxhi = .25 * (ptop[c] - pk[c]) * scp2[c];
-    double flxlo = -.25 * (ptop[c - 1] - pk[c - 1]) * scp2[c - 1];
+    double flxhi = g, flxlo = -sG[ty][tx - 1];
     double f;
     if (bih) {
-      if (iflip == 0) {
-        flxhi = mn(flxhi, uf[c] + .25 * (pk[c - 1] - pold[c - 1]) * scp2[c - 1]);
-        flxlo = mx(flxlo, uf[c] - .25 * (pk[c] - pold[c]) * scp2[c]);
-      } else {
-        flxhi = mn(flxhi, uf[c] + .25 * (pold[c] - pk[c]) * scp2[c]);
-        flxlo = mx(flxlo, uf[c] - .25 * (pold[c - 1] - pk[c - 1]) * scp2[c - 1]);
-      }
+      const double hw = sH[ty][tx - 1], h = sH[ty][tx];
+      flxhi = mn(flxhi, uf[c] + (iflip == 0 ? hw : h));
+      flxlo = mx(flxlo, uf[c] - (iflip == 0 ? h : hw));
       const double thkdfu = A.delt1 * A.thkdfu[c];
       f = mn(flxhi, mx(flxlo, thkdfu * (W(A, W_U1)[c - 1] - W(A, W_U1)[c])));
     } else {
@@ -353,17 +387,12 @@ __global__ void cn_thk_flux(const CnuityArgs A, int k, int bih, int iflip) {
   }
   if (mk & kIV) {
     double *vf = W(A, W_VF);
-    double flxhi = .25 * (ptop[c] - pk[c]) * scp2[c];
-    double flxlo = -.25 * (ptop[c - ld] - pk[c - ld]) * scp2[c - ld];
+    double flxhi = g, flxlo = -sG[ty - 1][tx];
     double f;
     if (bih) {
-      if (iflip == 0) {
-        flxhi = mn(flxhi, vf[c] + .25 * (pk[c - ld] - pold[c - ld]) * scp2[c - ld]);
-        flxlo = mx(flxlo, vf[c] - .25 * (pk[c] - pold[c]) * scp2[c]);
-      } else {
-        flxhi = mn(flxhi, vf[c] + .25 * (pold[c] - pk[c]) * scp2[c]);
-        flxlo = mx(flxlo, vf[c] - .25 * (pold[c - ld] - pk[c - ld]) * scp2[c - ld]);
-      }
+      const double hs = sH[ty - 1][tx], h = sH[ty][tx];
+      flxhi = mn(flxhi, vf[c] + (iflip == 0 ? hs : h));
+      flxlo = mx(flxlo, vf[c] - (iflip == 0 ? h : hs));
       const double thkdfv = A.delt1 * A.thkdfv[c];
       f = mn(flxhi, mx(flxlo, thkdfv * (W(A, W_U2)[c - ld] - W(A, W_U2)[c])));
     } else {
@@ -461,7 +490,7 @@ __global__ void cn_ra(const CnuityArgs A) {
 }
 
 dim3 grid_for(const CnuityArgs &a, int M) {
-  return dim3((unsigned)((a.ii + 2 * M + 31) / 32), (unsigned)((a.jj + 2 * M + 7) / 8));
+  return dim3((unsigned)((a.ii + 2 * M + kTX - 1) / kTX), (unsigned)((a.jj + 2 * M + kTY - 1) / kTY));
 }
 
 }  // namespace
@@ -469,7 +498,7 @@ dim3 grid_for(const CnuityArgs &a, int M) {
 size_t cnuity_work_slices() { return W_N; }
 
 cudaError_t launch_cnuity_layers(const CnuityArgs &a, int *launches, cudaStream_t s) {
-  const dim3 b(32, 8);
+  const dim3 b(kTX, kTY);
   int nl = 0;
   cn_init<<<grid_for(a, 6), b, 0, s>>>(a);
   nl++;
@@ -486,9 +515,11 @@ cudaError_t launch_cnuity_layers(const CnuityArgs &a, int *launches, cudaStream_
 }
 
 cudaError_t launch_cnuity_rest(const CnuityArgs &a, int *launches, cudaStream_t s) {
-  const dim3 b(32, 8);
+  const dim3 b(kTX, kTY);
   int nl = 0;
   if (!a.btrmas) {
+    cn_rpb<<<grid_for(a, 2), b, 0, s>>>(a);
+    nl++;
     for (int k = 0; k < a.kdm; k++) {  // loop 77
       cn_btflux<<<grid_for(a, 1), b, 0, s>>>(a, k);
       cn_update<<<grid_for(a, 0), b, 0, s>>>(a, k, 0, -1);

@@ -1145,6 +1145,7 @@ int hyc_cnuity(hyc_ctx *c, int32_t m, int32_t n, const hyc_cnuity_params *p, dou
   }
   a.onetacnt = F[HYC_F_ONETACNT].dev;
   a.delt1 = p->delt1;
+  a.dtinv = 1. / p->delt1;  // cnuity.F90:758, :987 (the same IEEE quotient as on the device)
   a.ra2fac = p->ra2fac;
   a.w = c->d_cnw;
   a.keys = want_keys ? c->d_cnkeys : nullptr;
