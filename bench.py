@@ -58,11 +58,12 @@ SCHEME_NAMES = {0: "PCM", 1: "MPDATA", 2: "FCT2", 4: "FCT4"}
 FALLBACK_HBM_GBS = 6800.0
 
 
-def bytes_per_update(s_t: int, s_f: int, s_dp: int, ntr: int, kdm: int) -> float:
+def bytes_per_update(s_t: int, s_f: int, s_dp: int, ntr: int, kdm: int, nlev: int = 3) -> float:
     """Minimal DRAM bytes per cell*layer*tracer update: read fld(n), fld(m),
-    write fld(n) per tracer; uflx, vflx, dp(n) per cell-layer shared by the
-    tracers; scp2, scp2i (8+8) and the ip/iu/iv masks (1 byte each) per cell."""
-    return 3 * s_t + (2 * s_f + s_dp) / ntr + 19.0 / (kdm * ntr)
+    write fld(n) per tracer (nlev = 2 for PCM and MPDATA, which read no
+    centre level); uflx, vflx, dp(n) per cell-layer shared by the tracers;
+    scp2, scp2i (8+8) and the ip/iu/iv masks (1 byte each) per cell."""
+    return nlev * s_t + (2 * s_f + s_dp) / ntr + 19.0 / (kdm * ntr)
 
 
 def peak_hbm():
@@ -230,19 +231,26 @@ def reference_arm(args, wl):
     return 0
 
 
-ENS_FORMS = {  # form -> (precision, FP64 thickness prep)
-    "fp64": ("fp64", True),
-    "mixed": ("mixed", True),
-    "mixed-fp32prep": ("mixed", False),
+ENS_FORMS = {  # form -> (precision, FP64 thickness prep, advtyp)
+    "fp64": ("fp64", True, 2),
+    "mixed": ("mixed", True, 2),
+    "mixed-fp32prep": ("mixed", False, 2),
+    "fp64-fct4": ("fp64", True, 4),
+    "mixed-fp32prep-fct4": ("mixed", False, 4),
+    "fp64-mpdata": ("fp64", True, 1),
+    "mixed-fp32prep-mpdata": ("mixed", False, 1),
 }
+FP64_REF = {2: "fp64", 4: "fp64-fct4", 1: "fp64-mpdata"}  # the FP64 form each mixed form is checked against
 KERNEL_OF_TILE = {26: "mix_fct2_col_kernel", 56: "mix_fct2_col2_kernel"}
 
 
 def make_ensemble(spec, form, stream):
     import hycadv
 
-    prec, prep64 = ENS_FORMS[form]
+    prec, prep64, adv = ENS_FORMS[form]
     ens = hycadv.Ensemble([spec], precision=prec)
+    if adv == 1:
+        ens.set_posdef(0, 0, 256.0)  # temperature (mod_tsadvc.F90:1761)
     if prec == "mixed":
         ens.set_prep64(prep64)
     ens.set_stream(stream)  # graphs are recorded on the library's own stream and replayed here
@@ -262,10 +270,11 @@ def put_basin(ens, case, kdm):
 
 
 def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local, forms):
-    """The basin through the ensemble (batched) API in each form: load, tune,
-    one step from the inputs (kept for the error and content checks), then
-    W warm-up steps and K timed steps replayed from one CUDA graph, bracketed
-    by barriers; content of each tracer before and after one step."""
+    """The basin through the ensemble (batched) API in each form (FCT2, FCT4
+    or MPDATA): load, tune, one step from the inputs (an FP32-mixed form's is
+    compared with the FP64 form of its scheme, which runs first), then W
+    warm-up steps and K timed steps replayed from one CUDA graph, bracketed by
+    barriers; content of each tracer before and after one step."""
     import torch
 
     kdm = wl["kdm"]
@@ -274,7 +283,7 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
     out, first = {}, {}
     sea = sea_mask(b, masks, dev)
     for form in forms:
-        prec, _ = ENS_FORMS[form]
+        prec, _, adv = ENS_FORMS[form]
         ens = make_ensemble(spec, form, stream)
         put_basin(ens, case, kdm)
         if args.tile and prec == "mixed":  # fixed shape (profiling): no tuner launches
@@ -282,18 +291,18 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
             ens.set_tile(tx, ty)
             ens.set_strip_tracers(nq_)
         else:
-            tx, ty, _ = ens.tune(2, wl["delt1"])
+            tx, ty, _ = ens.tune(adv, wl["delt1"])
         nq = ens.option("strip_tracers") if prec == "mixed" else None
         c_old = [ens.content(0, q, "old", wl["delt1"]) for q in range(2)]
-        ens.step(2, wl["delt1"], 1)  # from the inputs: compare one step
+        ens.step(adv, wl["delt1"], 1)  # from the inputs: compare one step
         c_new = [ens.content(0, q, "cur", wl["delt1"]) for q in range(2)]
         got = torch.empty((2, kdm, b.ld2, b.ld1), dtype=torch.float64, device=dev)
         ens.get(0, "cur", got)
         first[form] = got[:, :, sea].clone()
         del got
         for _ in range(args.warmup):
-            ens.step(2, wl["delt1"], 1)
-        ens.step(2, wl["delt1"], args.steps, graph=True)  # capture (and one more warm pass)
+            ens.step(adv, wl["delt1"], 1)
+        ens.step(adv, wl["delt1"], args.steps, graph=True)  # capture (and one more warm pass)
         torch.cuda.synchronize(dev)
         if dist:
             dist.barrier()
@@ -301,7 +310,7 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with ClockSampler(local) as clk:
             e0.record(stream)
-            ens.step(2, wl["delt1"], args.steps, graph=True)
+            ens.step(adv, wl["delt1"], args.steps, graph=True)
             e1.record(stream)
             torch.cuda.synchronize(dev)
         if dist:
@@ -316,9 +325,11 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
         s_t = 8 if prec == "fp64" else 4  # fluxes as the tracers
         # dp: FP64, except that the strip kernel with the FP32 thickness prep stages the FP32 copy made at put
         s_dp = 4 if (prec == "mixed" and not ENS_FORMS[form][1] and tx == 56) else 8
-        bpu = bytes_per_update(s_t, s_t, s_dp, 2, kdm)
+        # MPDATA reads no centre level: 2 tracer slices per update instead of 3
+        bpu = bytes_per_update(s_t, s_t, s_dp, 2, kdm, 2 if adv == 1 else 3)
         ach = ups_step * bpu / (ms / 1e3) / 1e9
-        out[form] = {"value": ws * ups_step / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "tile": [tx, ty],
+        out[form] = {"value": ws * ups_step / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "advtyp": adv,
+                     "tile": [tx, ty],
                      "tracers_per_pass": nq, "kernel": KERNEL_OF_TILE.get(tx, "fct tile kernel"),
                      "algorithmic_bytes_per_update": bpu, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
                      "graph_steps": args.steps, "clocks": clk.summary(),
@@ -327,19 +338,19 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
         ens.close()
         del ens
         torch.cuda.empty_cache()
-    if "fp64" in first:
-        ref = first["fp64"]
-        for form in first:
-            if form == "fp64":
-                continue
-            errs = {}
-            for q, name in enumerate(("temp", "saln")):
-                d = first[form][q] - ref[q]
-                scale = ref[q].abs().max()
-                errs[name] = {"max_rel": float(d.abs().max() / scale),
-                              "rms_rel": float(d.pow(2).mean().sqrt() / scale)}
-            out[form]["vs_fp64_one_step"] = errs
-            out[form]["speedup_vs_fp64_ensemble"] = out[form]["value"] / out["fp64"]["value"]
+    for form in first:
+        rf = FP64_REF[ENS_FORMS[form][2]]
+        if form == rf or rf not in first:
+            continue
+        ref = first[rf]
+        errs = {}
+        for q, name in enumerate(("temp", "saln")):
+            d = first[form][q] - ref[q]
+            scale = ref[q].abs().max()
+            errs[name] = {"max_rel": float(d.abs().max() / scale),
+                          "rms_rel": float(d.pow(2).mean().sqrt() / scale)}
+        out[form]["vs_fp64_one_step"] = errs
+        out[form]["speedup_vs_fp64_ensemble"] = out[form]["value"] / out[rf]["value"]
     return out
 
 
@@ -604,7 +615,7 @@ def run_e2e(args, wl, b, spec, case, form, tile, nq, dev, stream, dist):
         for k in ("old", "cur", "uflx", "vflx", "dp"):
             ens.put(0, k, host[k])  # synchronous: the host buffer is free again on return
         t1 = time.perf_counter()
-        ens.step(2, wl["delt1"], 1)
+        ens.step(ENS_FORMS[form][2], wl["delt1"], 1)
         t2 = time.perf_counter()
         # staged on the device after the step; the copy to host overlaps the
         # next step's puts (the timed region ends with ens.wait())
@@ -1104,10 +1115,12 @@ def main():
     ap.add_argument("--form", default="mixed-fp32prep", choices=sorted(ENS_FORMS),
                     help="headline form (ensemble API): FP32-mixed with FP64 thickness prep, with compensated "
                          "FP32 prep, or FP64")
-    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-full,cnuity,fp64,mixed,mixed-fp32prep",
+    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-full,cnuity,fp64,mixed,mixed-fp32prep,"
+                                       "fp64-fct4,mixed-fp32prep-fct4,fp64-mpdata,mixed-fp32prep-mpdata",
                     help="forms measured beside the headline (tsadvc[-fct4|-mpdata|-pcm] = FP64 plain through "
                          "hyc_tsadvc, FCT2 unless named; tsadvc-full = asselin_save + tsadvc + its "
-                         "diffusion + asselin_filter; cnuity = the continuity equation)")
+                         "diffusion + asselin_filter; cnuity = the continuity equation; fp64[-fct4|-mpdata], "
+                         "mixed[-fp32prep][-fct4|-mpdata] = the ensemble API, FCT2 unless named)")
     ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--c4-steps", type=int, default=100, help="c4: steps per basin")
     ap.add_argument("--tile", default="", help="mixed forms: fixed tile 'tx,ty,tracers_per_pass' instead of the tuner")
@@ -1171,8 +1184,8 @@ def main():
     if "cnuity" in others:
         schemes["cnuity"] = run_cnuity(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local)
     ens_forms = [f for f in others if f in ENS_FORMS and f != args.form]
-    if "fp64" in ens_forms:  # the reference of the error checks runs first
-        ens_forms = ["fp64"] + [f for f in ens_forms if f != "fp64"]
+    # the FP64 references of the error checks run first
+    ens_forms = [f for f in ens_forms if ENS_FORMS[f][0] == "fp64"] + [f for f in ens_forms if ENS_FORMS[f][0] != "fp64"]
     ens_forms = ens_forms + [args.form]
     forms = run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local, ens_forms)
     head = forms[args.form]
@@ -1193,9 +1206,10 @@ def main():
     if rank == 0:
         peak, peak_kind = peak_hbm()
         prec = ENS_FORMS[args.form][0]
-        key = {"mixed": "col2_mixed", "mixed-fp32prep": "col2_mixed_fp32prep", "fp64": "fct2_fp64_ens"}[args.form]
+        key = {"mixed": "col2_mixed", "mixed-fp32prep": "col2_mixed_fp32prep", "fp64": "fct2_fp64_ens"}.get(args.form)
         roof = {"bound": "hbm", "achieved": head["achieved_GBs"], "peak": peak, "unit": "GB/s",
-                "frac": head["frac_of_measured_hbm"], "traffic": profile_traffic(f"{key}_{args.workload}"),
+                "frac": head["frac_of_measured_hbm"],
+                "traffic": profile_traffic(f"{key}_{args.workload}") if key else None,
                 "peak_kind": peak_kind, "kernel": head["kernel"],
                 "algorithmic_bytes_per_update": head["algorithmic_bytes_per_update"],
                 "avg_launch_ms": head["ms_per_step"], "tile": head["tile"],

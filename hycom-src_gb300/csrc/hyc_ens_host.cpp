@@ -502,10 +502,10 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
 }
 
 // Schemes per form and kernel: FP64 FCT2/FCT4 (queue kernel) and PCM/MPDATA
-// (plain tile kernel); FP32-mixed FCT2 (every kernel) and MPDATA (two-column
-// strip kernel).
+// (plain tile kernel); FP32-mixed FCT2 (every kernel), MPDATA and FCT4
+// (two-column strip kernel).
 bool scheme_ok(const hyc_ens *e, int advtyp, hyc::TileShape t) {
-  if (e->prec == HYC_PREC_MIXED) return advtyp == 2 || (advtyp == 1 && is_col2(t));
+  if (e->prec == HYC_PREC_MIXED) return advtyp == 2 || ((advtyp == 1 || advtyp == 4) && is_col2(t));
   return advtyp == 0 || advtyp == 1 || advtyp == 2 || advtyp == 4;
 }
 

@@ -1,4 +1,4 @@
-// hyc_mixed_col2.cu -- FP32-mixed FCT2 and MPDATA ensemble kernel: a warp marches a
+// hyc_mixed_col2.cu -- FP32-mixed FCT2, FCT4 and MPDATA ensemble kernel: a warp marches a
 // 64-column strip north through the rows, two columns per lane, with the
 // rows streamed into a per-warp shared-memory ring by TMA.
 //
@@ -119,11 +119,12 @@ __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(fminf(a.x,
 struct St2 {
   float2 f1;                 // fld at J-1
   float2 fA1, fB1, fA2, fB2;  // fld at J-1, J-2 masked for maxima (A) / minima (B)
-  float2 c1;                 // fldc at J-1
+  float2 c1, c2, c3;         // fldc at J-1 (J-2, J-3: FCT4's y stencil)
   float2 fx1, fy1;           // low-order x (west face) / y (south face) fluxes of row J-1
   float2 lo2, lo3;           // fldlo at J-2, J-3
   float2 mxA2, mnB2, mxA3, mnB3;  // fmxlo/fmnlo at J-2, J-3, masked
-  float2 ax2, ay1, ay2;      // antidiffusive x-flux of row J-2; y-fluxes of rows J-1, J-2
+  float2 ax2, ay1, ay2;      // antidiffusive x-flux of row J-2; y-fluxes of the south faces of
+                             // rows J-1, J-2 (FCT4: ay1 = face J-2, its face J-1 formed at row J)
   float2 rp3, rm3;           // Zalesak ratios at J-3
   float2 lx3, ly3;           // limited fluxes of row J-3
   float2 qx3, qn3;           // fqmax/fqmin at J-3
@@ -175,6 +176,7 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
   using RG = typename GE::RG;
   constexpr int NI = GE::NI;
   constexpr bool MP = SCHEME == kMPDATA;
+  constexpr bool F4 = SCHEME == kFCT4;
   using St = typename std::conditional<MP, StM, St2>::type;
   extern __shared__ unsigned char c2raw_[];
   unsigned char *sm = (unsigned char *)(((uintptr_t)c2raw_ + 127) & ~(uintptr_t)127);
@@ -293,7 +295,8 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
         }
         const float2 z2 = make_float2(0.f, 0.f);
         float2 u1 = z2, u1m = z2, v1 = z2, R2 = z2, nR3 = z2, QF2 = z2, DS1 = z2, DS2 = z2, DS3 = z2, QS1 = z2;
-        float2 v1m = z2, H2 = z2;  // MPDATA: masked v of row J-1, fco+fcn of row J-2
+        float2 v1m = z2, H2 = z2;  // MPDATA, FCT4: masked v of row J-1; MPDATA: fco+fcn of row J-2
+        float2 IU1 = z2, IV1 = z2, IV2 = z2;  // FCT4: iu of row J-1, iv of rows J-1, J-2 (0/1)
         float2 L1 = z2, L2 = z2, L3 = z2;  // land flags (1 = land) of rows J-1, J-2, J-3
         float L2e = 0.f;                   // land flag east of column B, row J-2
         using DT = typename std::conditional<PREP64, double, float>::type;
@@ -380,7 +383,8 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
             const float2 un0 = neg2(u0m), vn0 = neg2(v0m);
             const float2 up0 = sub2(u0m, un0), vp0 = sub2(v0m, vn0);  // max(x,0) = x - min(x,0), exact
             const float2 half = make_float2(0.5f, 0.5f);
-            const float2 u1h = mul2(u1m, half), v0h = mul2(v0m, half);
+            const float2 u1h = mul2(u1m, half), v0h = mul2(v0m, half), v1h = mul2(v1m, half);
+            const float2 F14 = make_float2(7.f / 12.f, 7.f / 12.f), F24 = make_float2(-1.f / 12.f, -1.f / 12.f);
             // land flags (1 = land): scp2/dt2 is stored as 0 on land
             const float2 L0 = make_float2(gA.y > 0.f ? 0.f : 1.f, gB.y > 0.f ? 0.f : 1.f);
             const bool ip1A = L1.x == 0.f, ip1B = L1.y == 0.f;
@@ -409,6 +413,17 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
               va0 = mul2(make_float2(fabsf(v0m.x), fabsf(v0m.y)), half);
             }
 
+            // FCT4 (mod_tsadvc.F90:1534-1555): 4th-order antidiffusive fluxes where
+            // both neighbouring faces are open, else 2nd order -- x faces of row J-1
+            // (iu(i-1), iu(i+1) of row J-1), the y face J-1 (iv of rows J-2 and J)
+            bool x4A = false, x4B = false, y4A = false, y4B = false;
+            if (F4) {
+              const float iuwB = __shfl_up_sync(kFull, IU1.y, 1), iueA = __shfl_down_sync(kFull, IU1.x, 1);
+              x4A = iuwB != 0.f && IU1.y != 0.f;
+              x4B = IU1.x != 0.f && iueA != 0.f;
+              y4A = IV2.x != 0.f && gA.w != 0.f;
+              y4B = IV2.y != 0.f && gB.w != 0.f;
+            }
             float2 res[NQ];
             auto store_row = [&](int q, float resA, float resB) {
               float *p = fn[q] + (long long)a0 + (long long)(jo + nb - 1) * ld1;
@@ -439,9 +454,24 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
               const float2 fdv = mul2(comp_div2(east(s.fx1), s.fx1, fy0, s.fy1), DS1);
               const float2 t1 = fma2(c, W1, mul2(fdv, nR1));
               const float2 lo1 = make_float2(fmaxf(fmnA, fminf(fmxA, t1.x)), fmaxf(fmnB, fminf(fmxB, t1.y)));
-              // S3: antidiffusive fluxes, x of row J-1 and y of row J (:817-833)
-              const float2 ax1 = sub2(mul2(u1h, add2(s.c1, west(s.c1))), s.fx1);
-              const float2 ay0 = sub2(mul2(v0h, add2(c0[q], s.c1)), fy0);
+              // S3: antidiffusive fluxes, x of row J-1 and y of row J (:817-833); FCT4:
+              // x of row J-1 and y of the face J-1 (:1534-1555), whose stencil
+              // reaches row J
+              float2 ax1, ayn;
+              if constexpr (!F4) {
+                ax1 = sub2(mul2(u1h, add2(s.c1, west(s.c1))), s.fx1);
+                ayn = sub2(mul2(v0h, add2(c0[q], s.c1)), fy0);
+              } else {
+                const float cwB = __shfl_up_sync(kFull, s.c1.y, 1), cwA = __shfl_up_sync(kFull, s.c1.x, 1);
+                const float ceA = __shfl_down_sync(kFull, s.c1.x, 1);
+                const float2 inx = add2(s.c1, make_float2(cwB, s.c1.x));                    // c(i) + c(i-1)
+                const float2 outx = add2(make_float2(s.c1.y, ceA), make_float2(cwA, cwB));  // c(i+1) + c(i-2)
+                const float2 hx4 = mul2(u1m, fma2(F14, inx, mul2(F24, outx)));
+                ax1 = sub2(sel(x4A, x4B, hx4, mul2(u1h, inx)), s.fx1);
+                const float2 iny = add2(s.c1, s.c2), outy = add2(c0[q], s.c3);  // rows J-1 + J-2, J + J-3
+                const float2 hy4 = mul2(v1m, fma2(F14, iny, mul2(F24, outy)));
+                ayn = sub2(sel(y4A, y4B, hy4, mul2(v1h, iny)), s.fy1);
+              }
               const float2 mx1 = make_float2(max3f(c.x, s.c1.x, lo1.x), max3f(c.y, s.c1.y, lo1.y));  // :792-793
               const float2 mn1 = make_float2(min3f(c.x, s.c1.x, lo1.x), min3f(c.y, s.c1.y, lo1.y));
               const float2 mxA1 = fma2(L1, nbig, mx1), mnB1 = fma2(L1, pbig, mn1);
@@ -452,7 +482,8 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
               const float2 fqmin = make_float2(min3f(min3f(s.mnB2.x, nw.x, ne.x), s.mnB3.x, mnB1.x),
                                                min3f(min3f(s.mnB2.y, nw.y, ne.y), s.mnB3.y, mnB1.y));
               const float2 fxa = s.ax2, fxb = sel(ip2B, ip2E, east(s.ax2), s.ax2);  // ipip1 quirk (:873-883)
-              const float2 fya = s.ay2, fyb = sel(ip1A, ip1B, s.ay1, s.ay2);
+              // the south face of row J-2 and, with the ipjp1 quirk, its north face
+              const float2 fya = F4 ? s.ay1 : s.ay2, fyb = F4 ? sel(ip1A, ip1B, ayn, s.ay1) : sel(ip1A, ip1B, s.ay1, s.ay2);
               const float2 nxa = neg2(fxa), nxb = neg2(fxb), nya = neg2(fya), nyb = neg2(fyb);
               const float2 pxa = sub2(fxa, nxa), pxb = sub2(fxb, nxb), pya = sub2(fya, nya), pyb = sub2(fyb, nyb);
               const float2 famax = sub2(add2(sub2(pxa, nxb), pya), nyb);
@@ -472,7 +503,7 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
               // lx = max(ax,0)*min(rp,rm_w) + min(ax,0)*min(rp_w,rm): one product is
               // zero, so the rounding is that of the reference's single product
               const float2 nax = neg2(s.ax2), pax = sub2(s.ax2, nax);
-              const float2 nay = neg2(s.ay2), pay = sub2(s.ay2, nay);
+              const float2 nay = neg2(fya), pay = sub2(fya, nay);
               const float2 lx2 = fma2(pax, min2(rp2, rm2w), mul2(nax, min2(rp2w, rm2)));
               const float2 ly2 = fma2(pay, min2(rp2, s.rm3), mul2(nay, min2(s.rp3, rm2)));
               // S6: update of row J-3 (:962-982)
@@ -491,7 +522,7 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
               s.rm3 = rm2;
               s.ax2 = ax1;
               s.ay2 = s.ay1;
-              s.ay1 = ay0;
+              s.ay1 = ayn;
               s.mxA3 = s.mxA2;
               s.mnB3 = s.mnB2;
               s.mxA2 = mxA1;
@@ -500,6 +531,8 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
               s.lo2 = lo1;
               s.fx1 = fx0;
               s.fy1 = fy0;
+              s.c3 = s.c2;
+              s.c2 = s.c1;
               s.c1 = c0[q];
               s.fA2 = s.fA1;
               s.fB2 = s.fB1;
@@ -599,9 +632,12 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
             L1 = L0;
             u1 = u0;
             u1m = u0m;
-            if (MP) {
-              v1m = v0m;
-              H2 = H1;
+            if (MP || F4) v1m = v0m;
+            if (MP) H2 = H1;
+            if (F4) {
+              IU1 = make_float2(gA.z, gB.z);
+              IV2 = IV1;
+              IV1 = make_float2(gA.w, gB.w);
             }
             v1 = v0;
             dA1 = d0.x;
@@ -687,6 +723,10 @@ cudaError_t launch_mix_col2(int scheme, const MixBasin *basins, const int4 *item
   if (scheme == kMPDATA) {
     if (nq >= 2) return prep64 ? HYC_COL2(kMPDATA, 2, true) : HYC_COL2(kMPDATA, 2, false);
     return prep64 ? HYC_COL2(kMPDATA, 1, true) : HYC_COL2(kMPDATA, 1, false);
+  }
+  if (scheme == kFCT4) {
+    if (nq >= 2) return prep64 ? HYC_COL2(kFCT4, 2, true) : HYC_COL2(kFCT4, 2, false);
+    return prep64 ? HYC_COL2(kFCT4, 1, true) : HYC_COL2(kFCT4, 1, false);
   }
 #undef HYC_COL2
   return cudaErrorInvalidValue;

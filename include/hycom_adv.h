@@ -436,8 +436,8 @@ int hyc_ens_tune(hyc_ens *ens, int32_t advtyp, double delt1, int32_t *tx, int32_
 /*
  * Advance every basin nsteps leapfrog steps.  advtyp: FP64 form 0 (PCM),
  * 1 (MPDATA), 2 (FCT2), 4 (FCT4); FP32-mixed form 2 (FCT2) with every
- * kernel and 1 (MPDATA) with the two-column strip kernel (tx = 56).  PCM and
- * MPDATA read only level t-1 (mod_tsadvc.F90:152, :495).
+ * kernel, 1 (MPDATA) and 4 (FCT4) with the two-column strip kernel
+ * (tx = 56).  PCM and MPDATA read only level t-1 (mod_tsadvc.F90:152, :495).
  * use_graph = 1: the nsteps launches are captured once into a CUDA graph
  * (per nsteps/advtyp/delt1/tile) and replayed.  Asynchronous.
  */

@@ -142,17 +142,21 @@ def test_mixed_one_step_error(cuda, prep64):
     ens.close()
 
 
-@pytest.mark.parametrize("prec,prep64,cons_tol,err_tol",
-                         [("fp64", True, 1e-13, 0.0), ("mixed", True, 1e-6, 1e-4), ("mixed", False, 1e-6, 1e-4)])
-def test_ensemble_multistep_conservation_extrema(cuda, prec, prep64, cons_tol, err_tol):
-    """20 steps: tracer content conserved (FP64 to round-off), no new extrema,
-    and the FP32-mixed drift from the oracle stays within the envelope of the
-    leapfrog-FCT dynamics (an FP64 run perturbed by one FP32 rounding of its
-    inputs already drifts ~1e-5 in 20 steps)."""
+@pytest.mark.parametrize("prec,prep64,cons_tol,err_tol,advtyp",
+                         [("fp64", True, 1e-13, 0.0, 2), ("mixed", True, 1e-6, 1e-4, 2), ("mixed", False, 1e-6, 1e-4, 2),
+                          ("mixed", False, 1e-6, 1e-4, 4)])
+def test_ensemble_multistep_conservation_extrema(cuda, prec, prep64, cons_tol, err_tol, advtyp):
+    """20 steps of FCT2 or FCT4: tracer content conserved (FP64 to round-off),
+    no new extrema, and the FP32-mixed drift from the oracle stays within
+    the envelope of the leapfrog-FCT dynamics (an FP64 run perturbed by one
+    FP32 rounding of its inputs already drifts ~1e-6 to 1e-5 in 20 steps,
+    FCT2 and FCT4 alike)."""
     members = make_members()
     ens = hycadv.Ensemble([spec_of(m) for m in members], precision=prec)
     if prec == "mixed":
         ens.set_prep64(prep64)
+        if advtyp == 4:
+            ens.set_tile(56, 64)
     load(ens, members)
     nsteps = 20
     start = [(m["trc"][..., m["g"].masks["ip"] != 0].min(), m["trc"][..., m["g"].masks["ip"] != 0].max())
@@ -163,13 +167,13 @@ def test_ensemble_multistep_conservation_extrema(cuda, prec, prep64, cons_tol, e
             mm, nn = levels(step)
             ens.put(i, "dp", np.ascontiguousarray(m["c"]["dp"][nn - 1]))
         c_old = [[ens.content(i, q, "old", DELT1) for q in range(m["ntr"])] for i, m in enumerate(members)]
-        ens.step(2, DELT1, 1)
+        ens.step(advtyp, DELT1, 1)
         c_new = [[ens.content(i, q, "cur", DELT1) for q in range(m["ntr"])] for i, m in enumerate(members)]
         for i, m in enumerate(members):
             for q in range(m["ntr"]):
                 worst_cons = max(worst_cons, abs(c_new[i][q] - c_old[i][q]) / abs(c_old[i][q]))
-            oracle_step(m, step, 2)
-    print(f"{prec}: worst relative content change in one step {worst_cons:.2e}")
+            oracle_step(m, step, advtyp)
+    print(f"{prec} advtyp {advtyp}: worst relative content change in one step {worst_cons:.2e}")
     assert worst_cons < cons_tol
     for i, m in enumerate(members):
         mm, nn = levels(nsteps)
@@ -349,19 +353,54 @@ def test_mixed_mpdata_one_step_error(cuda, prep64, nq):
     ens.close()
 
 
-def test_mixed_mpdata_needs_strip_kernel(cuda):
-    """FP32-mixed MPDATA runs only in the two-column strip kernel; other
-    tiles refuse it, and the tuner picks a strip shape."""
+@pytest.mark.parametrize("advtyp", [1, 4])
+def test_mixed_mpdata_fct4_need_strip_kernel(cuda, advtyp):
+    """FP32-mixed MPDATA and FCT4 run only in the two-column strip kernel;
+    other tiles refuse them, and the tuner picks a strip shape."""
     members = make_ts_members(SPECS[:1])
     ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
     load(ens, members)
     ens.set_tile(26, 32)
     with pytest.raises(hycadv.HycError):
-        ens.step(1, DELT1, 1)
-    tx, ty, _ = ens.tune(1, DELT1)
+        ens.step(advtyp, DELT1, 1)
+    tx, ty, _ = ens.tune(advtyp, DELT1)
     assert tx == 56
-    ens.step(1, DELT1, 1)
+    ens.step(advtyp, DELT1, 1)
     ens.close()
+
+
+@pytest.mark.parametrize("prep64,nq", [(True, 2), (False, 2), (False, 1)])
+def test_mixed_fct4_one_step_error(cuda, prep64, nq):
+    """One FP32-mixed FCT4 step (two-column strip kernel: 4th-order
+    antidiffusive fluxes, 2nd order next to closed faces,
+    mod_tsadvc.F90:1534-1555) is within 1e-6 of the FP64 oracle relative to
+    each tracer's max |value|, closed and periodic basins, 1 to 3 tracers."""
+    members = make_members()
+    ens = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
+    ens.set_prep64(prep64)
+    ens.set_tile(56, 64)
+    ens.set_strip_tracers(nq)
+    load(ens, members)
+    ens.step(4, DELT1, 1)
+    for i, m in enumerate(members):
+        want = oracle_step(m, 1, 4)
+        got = get_cur(ens, i, m)
+        ip = sea_interior(m)
+        for q in range(m["ntr"]):
+            err = np.abs(got[q][..., ip] - want[q][..., ip]).max() / np.abs(want[q][..., ip]).max()
+            print(f"fct4 prep64={prep64} nq={nq} basin {i} tracer {q}: {err:.2e}")
+            assert err < 1e-6, (i, q, err)
+    # FCT4 differs from FCT2 on these inputs (the 4th-order stencil is live)
+    members = make_members()
+    ens2 = hycadv.Ensemble([spec_of(m) for m in members], precision="mixed")
+    ens2.set_prep64(prep64)
+    ens2.set_tile(56, 64)
+    ens2.set_strip_tracers(nq)
+    load(ens2, members)
+    ens2.step(2, DELT1, 1)
+    assert any(not np.array_equal(get_cur(ens, i, m), get_cur(ens2, i, m)) for i, m in enumerate(members))
+    ens.close()
+    ens2.close()
 
 
 def test_get_async_overlaps_and_equals_get(cuda):
