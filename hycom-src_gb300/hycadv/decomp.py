@@ -17,6 +17,14 @@ The exchange runs over torch.distributed point-to-point (gloo on CPU,
 NCCL between GPUs; each message lands in the receiver's own buffer), or
 between in-process tiles (:meth:`Decomp.exchange_tiles`) for tests on one
 device.
+
+Conservation sums use the reference's reproducible xcsum
+(mod_xc_mp.h:3353-3533): partial row sums over strips 2*nbdy+1 columns
+wide, each formed on the block that owns the strip's centre (from its
+halo), then added in global column order, and the rows in global row
+order -- so a decomposed basin's sum equals the single-domain sum bit for
+bit, whatever the block layout (:meth:`Decomp.xcsum`,
+:meth:`Decomp.xcsum_tiles`).
 """
 from __future__ import annotations
 
@@ -189,3 +197,57 @@ class Decomp:
             for d, b in bufs.items():
                 fills[d] = b
             self._apply(t, rank, fills, w, phase)
+
+    # -- reproducible sums (xcsum) ------------------------------------------
+    def _centres(self):
+        """Global centres of the partial-sum strips (mod_xc_mp.h:2915)."""
+        return list(range(1 + self.nbdy, self.nx + self.nbdy + 1, 2 * self.nbdy + 1))
+
+    def _partials(self, a_local, mask_local, r: int) -> dict:
+        """Rank r's partial row sums {(j, l): sum} over the strips whose
+        centre it owns (its interior, or for the last block of a row of
+        blocks the nbdy columns east of it, mod_xc_mp.h:2895-2936), summed in
+        column order from its window (halo included, mod_xc_mp.h:3410-3424)."""
+        nb = self.nbdy
+        i0, i1, j0, j1 = self.extent(r)
+        last = self.coords(r)[0] == self.px - 1
+        a = np.asarray(a_local, dtype=np.float64)
+        m = np.asarray(mask_local)
+        out = {}
+        for l, c in enumerate(self._centres()):
+            if not (i0 <= c <= i1 or (last and i1 < c <= i1 + nb)):
+                continue
+            lo, hi = max(c - nb, 1), min(c + nb, self.nx)
+            cols = range(lo - i0 + nb, hi - i0 + nb + 1)  # local index of global column i: i - i0 + nb
+            for j in range(j0, j1 + 1):
+                row = j - j0 + nb
+                s = 0.0
+                for q in cols:
+                    if m[row, q] == 1:
+                        s = s + float(a[row, q])
+                out[(j, l)] = s
+        return out
+
+    def _total(self, parts) -> float:
+        allp = {}
+        for p in parts:
+            allp.update(p)
+        total = 0.0
+        for j in range(1, self.ny + 1):
+            s8 = 0.0
+            for l in range(len(self._centres())):
+                s8 = s8 + allp[(j, l)]
+            total = total + s8
+        return total
+
+    def xcsum_tiles(self, tiles: list, masks: list) -> float:
+        """xcsum of a field held as every rank's local array (halos filled)."""
+        return self._total([self._partials(t, m, r) for r, (t, m) in enumerate(zip(tiles, masks))])
+
+    def xcsum(self, a_local, mask_local, dist, rank: int) -> float:
+        """xcsum over all ranks (every rank calls it; all get the same
+        value).  a_local (ld2, ld1) needs its halo filled first (the
+        reference refreshes it with xctilr before summing)."""
+        parts = [None] * self.size
+        dist.all_gather_object(parts, self._partials(a_local, mask_local, rank))
+        return self._total(parts)

@@ -57,6 +57,25 @@ def test_exchange_equals_xctilr():
             assert np.array_equal(t, d.window(ref, r)), (periodic, r)
 
 
+def test_xcsum_tiles_equal_single_domain():
+    """In process: the reproducible sum over blocks (strips straddling block
+    edges, the last block owning the strips past its edge) equals the
+    single-domain xcsum bit for bit, closed and periodic, several layouts."""
+    from helpers import basin, oracle_grid
+
+    for periodic, nx, ny, px, py in ((False, 40, 33, 3, 2), (True, 41, 30, 2, 3), (False, 27, 19, 4, 1)):
+        b = basin(nx, ny, periodic, 9)
+        g = oracle_grid(b, threads=1)
+        rng = np.random.default_rng(nx)
+        a = rng.standard_normal((b.ld2, b.ld1)) * 1.0e3
+        g.xctilr(a, b.nbdy, b.nbdy)
+        want = g.xcsum(a, g.masks["ip"])
+        d = Decomp(b.nx, b.ny, b.nbdy, px, py, periodic)
+        tiles = [d.window(a, r) for r in range(d.size)]
+        masks = [d.window(g.masks["ip"], r) for r in range(d.size)]
+        assert d.xcsum_tiles(tiles, masks) == want, (periodic, px, py)
+
+
 def _rank(rank, world, port, out_dir, cfg):
     import sys
 
@@ -98,6 +117,15 @@ def _rank(rank, world, port, out_dir, cfg):
         for k in ("temp", "saln", "tracer"):
             ok &= bool(np.array_equal(d.interior(loc[k], rank), d.interior(win(c[k]), rank)))
     ok &= not np.array_equal(d.interior(loc["temp"], rank), d.interior(t0, rank))  # the blocks did advance
+    # the conservation sum of the new level over all blocks (one gather of
+    # partial sums) equals the single-domain xcsum bit for bit
+    from helpers import levels
+
+    nn = levels(3)[1]
+    d.exchange(torch.from_numpy(loc["temp"]), b.nbdy, dist, rank)
+    ipl = win(g.masks["ip"])
+    for k in range(loc["temp"].shape[1]):
+        ok &= d.xcsum(loc["temp"][nn - 1, k], ipl, dist, rank) == g.xcsum(c["temp"][nn - 1, k], g.masks["ip"])
     flag = torch.tensor([0 if ok else 1], dtype=torch.int64)
     dist.all_reduce(flag, op=dist.ReduceOp.SUM)
     if rank == 0:
