@@ -59,6 +59,7 @@ cudaError_t launch_mix_col2(int scheme, const MixBasin *basins, const int4 *item
                             int nq, bool prep64, int *err, cudaStream_t s);
 cudaError_t launch_geo4(const double *scp2, const double *scp2i, const uint8_t *msk, double dt2, long long n,
                         float4 *out, cudaStream_t s);
+cudaError_t launch_wait_probe(int arrive, int *err, cudaStream_t s);
 cudaError_t launch_dtsi(const double *scp2i, double dt2, long long n, double *out, cudaStream_t s);
 cudaError_t launch_dsqs(const double *scp2, const double *scp2i, double dt2, long long n, float2 *out,
                         cudaStream_t s);

@@ -818,6 +818,24 @@ int hyc_ens_get_async(hyc_ens *e, int32_t basin, int32_t what, double *dst, int3
   return move(e, basin, what, 0, -1, dst, where, false, true);
 }
 
+int hyc_selftest_wait(int32_t device, int32_t arrive, int32_t *gave_up) {
+  if (!gave_up) return efail(nullptr, HYC_ERR_ARG, "hyc_selftest_wait: null argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+    return efail(nullptr, HYC_ERR_CUDA, "hyc_selftest_wait: no CUDA device %d", device);
+  Dev g(device);
+  int *d = nullptr, flag = 0;
+  cudaError_t c = cudaMalloc(&d, sizeof(int));
+  if (c == cudaSuccess) c = cudaMemset(d, 0, sizeof(int));
+  if (c == cudaSuccess) c = hyc::launch_wait_probe(arrive != 0, d, nullptr);
+  if (c == cudaSuccess) c = cudaDeviceSynchronize();
+  if (c == cudaSuccess) c = cudaMemcpy(&flag, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (c != cudaSuccess) return efail(nullptr, HYC_ERR_CUDA, "hyc_selftest_wait: %s", cudaGetErrorString(c));
+  *gave_up = flag;
+  return HYC_OK;
+}
+
 int hyc_ens_wait(hyc_ens *e) {
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   Dev g(e->device);

@@ -665,6 +665,26 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
   }
 }
 
+// Failure path of the streaming kernels, exercised without a fault: one
+// thread waits on an mbarrier through the same bounded wait the strip kernel
+// uses for its TMA blocks.  arrive = 0: nothing completes the phase, the wait
+// gives up after its limit, records the failure in *err and the kernel
+// returns; arrive = 1: the phase completes first and *err is left alone.
+__global__ void wait_probe_kernel(int arrive, int *err) {
+  __shared__ uint64_t probe_bar;
+  if (threadIdx.x == 0) {
+    tma::bar_init(&probe_bar, 1);
+    tma::fence_bar_init();
+    if (arrive) tma::arrive(&probe_bar);
+    tma::wait(&probe_bar, 0, err);
+  }
+}
+
+cudaError_t launch_wait_probe(int arrive, int *err, cudaStream_t s) {
+  wait_probe_kernel<<<1, 32, 0, s>>>(arrive, err);
+  return cudaGetLastError();
+}
+
 // per-cell factors of the strip kernel: dt2*scp2i, scp2/dt2 (0 on land, so
 // the Zalesak ratios of land cells stay finite), iu and iv as 0/1
 __global__ void geo4_kernel(const double *scp2, const double *scp2i, const uint8_t *msk, double dt2, long long n,

@@ -51,7 +51,7 @@ EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "
            "hyc_ens_last_error", "hyc_ens_set_option", "hyc_ens_get_option", "hyc_ens_set_posdef",
            "hyc_za_read", "hyc_za_parse_b", "hyc_za_check", "hyc_set_diffusion_grid", "hyc_tsdff",
            "hyc_asselin_save", "hyc_asselin_filter", "hyc_ens_get_async", "hyc_ens_wait",
-           "hyc_set_cnuity_grid", "hyc_cnuity")
+           "hyc_set_cnuity_grid", "hyc_cnuity", "hyc_selftest_wait")
 ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
 TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4, "tsdff": 5, "asselin": 6, "cnuity": 7}
@@ -129,6 +129,7 @@ def lib() -> C.CDLL:
         L.hyc_ens_get.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int32]
         L.hyc_ens_get_async.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int32]
         L.hyc_ens_wait.argtypes = [vp]
+        L.hyc_selftest_wait.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_int32)]
         L.hyc_ens_put_slices.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
         L.hyc_ens_get_slices.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
         L.hyc_ens_set_tile.argtypes = [vp, C.c_int32, C.c_int32]
@@ -154,6 +155,14 @@ def lib() -> C.CDLL:
 
 def version() -> str:
     return lib().hyc_version().decode()
+
+
+def selftest_wait(arrive: bool, device: int = 0) -> int:
+    """hyc_selftest_wait: 1 when a bounded device wait on a barrier nothing
+    completes gave up and reported it, 0 when the barrier completed."""
+    out = C.c_int32(-1)
+    _check(lib().hyc_selftest_wait(int(device), int(bool(arrive)), C.byref(out)))
+    return out.value
 
 
 def _err(h=None) -> str:

@@ -512,6 +512,18 @@ int hyc_za_parse_b(const char *line, char *cfield, int32_t *layer, int32_t *leve
  */
 int hyc_za_check(double hmin_a, double hmax_a, double hmin_b, double hmax_b);
 
+/*
+ * Self-test of the streaming kernels' failure path, which faults nothing:
+ * one thread on the GPU waits on an mbarrier through the bounded wait the
+ * TMA-fed kernels use (limit 2 s).  arrive = 0: nothing completes the
+ * barrier, the wait gives up, records the failure in a device error flag
+ * and the kernel returns (*gave_up = 1; the device stays usable -- a step
+ * kernel in that state makes hyc_ens_stats return HYC_ERR_CUDA); arrive = 1:
+ * the barrier completes first (*gave_up = 0).  No counterpart in the
+ * reference, which has no recovery path (xcstop).  Synchronous.
+ */
+int hyc_selftest_wait(int32_t device, int32_t arrive, int32_t *gave_up);
+
 /* Library build identification, e.g. "hycadv 0.1 sm_103a". */
 const char *hyc_version(void);
 
