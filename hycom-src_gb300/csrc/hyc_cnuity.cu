@@ -96,7 +96,11 @@ __global__ void cn_init(const CnuityArgs A) {
   }
 }
 
-// loop 76, :240-285 at margin 5: low-order and antidiffusive fluxes of layer k
+// loop 76, :240-285 at margin 5: low-order and antidiffusive fluxes of layer k.
+// BT = btrmas.  Without it onetamas and the face factors oneta_u/v are 1.0
+// (:142-145), and x*1.0 == x exactly, so those products (and their loads)
+// are skipped; the FP64 pipe bounds this kernel.
+template <bool BT>
 __global__ void cn_flux(const CnuityArgs A, int k) {
   Cell x;
   if (!cell_of(A, 5, x)) return;
@@ -108,20 +112,22 @@ __global__ void cn_flux(const CnuityArgs A, int k) {
   const long long lm = ((long long)k + (long long)mm * A.kdm) * sl;
   if (mk & kIU) {
     const double utotm = (A.u[lm + c] + A.ubavg[mm * sl + c]) * A.scuy[c];
-    const double q = ge0(utotm) ? mn(dk[c - 1], mx(0., A.depthu[c] - u3[c - 1])) * omn[c - 1]
-                                : mn(dk[c], mx(0., A.depthu[c] - u3[c])) * omn[c];
-    const double uf = utotm * q;
+    const long long cq = ge0(utotm) ? c - 1 : c;
+    const double q0 = mn(dk[cq], mx(0., A.depthu[c] - u3[cq]));
+    const double uf = utotm * (BT ? q0 * omn[cq] : q0);
     W(A, W_UF)[c] = uf;
-    W(A, W_UF2)[c] = utotm * A.dpu[lm + c] * W(A, W_OU)[c] - uf;
+    const double ud = utotm * A.dpu[lm + c];
+    W(A, W_UF2)[c] = (BT ? ud * W(A, W_OU)[c] : ud) - uf;
     A.uflx[(long long)k * sl + c] = uf;
   }
   if (mk & kIV) {
     const double vtotm = (A.v[lm + c] + A.vbavg[mm * sl + c]) * A.scvx[c];
-    const double q = ge0(vtotm) ? mn(dk[c - ld], mx(0., A.depthv[c] - u3[c - ld])) * omn[c - ld]
-                                : mn(dk[c], mx(0., A.depthv[c] - u3[c])) * omn[c];
-    const double vf = vtotm * q;
+    const long long cq = ge0(vtotm) ? c - ld : c;
+    const double q0 = mn(dk[cq], mx(0., A.depthv[c] - u3[cq]));
+    const double vf = vtotm * (BT ? q0 * omn[cq] : q0);
     W(A, W_VF)[c] = vf;
-    W(A, W_VF2)[c] = vtotm * A.dpv[lm + c] * W(A, W_OV)[c] - vf;
+    const double vd = vtotm * A.dpv[lm + c];
+    W(A, W_VF2)[c] = (BT ? vd * W(A, W_OV)[c] : vd) - vf;
     A.vflx[(long long)k * sl + c] = vf;
   }
 }
@@ -136,7 +142,8 @@ __device__ __forceinline__ void row_min(const CnuityArgs &A, const Cell &x, bool
   if ((threadIdx.x & 31) == 0 && k != LLONG_MAX) atomicMin(&A.keys[slot], k);
 }
 
-// loop 19, :294-315 at margin 4: low-order update of dp(k,n)
+// loop 19, :294-315 at margin 4: low-order update of dp(k,n) (BT as cn_flux)
+template <bool BT>
 __global__ void cn_low(const CnuityArgs A, int k) {
   Cell x;
   const bool in = cell_of(A, 4, x);
@@ -148,7 +155,8 @@ __global__ void cn_low(const CnuityArgs A, int k) {
     double *dk = A.dp + ((long long)k + (long long)nn * A.kdm) * sl;
     const double *uf = W(A, W_UF), *vf = W(A, W_VF);
     W(A, W_U3)[c] = W(A, W_U3)[c] + dk[c];
-    d = dk[c] * W(A, W_OM)[nn * sl + c] - ((uf[c + 1] - uf[c]) + (vf[c + ld] - vf[c])) * A.delt1 * A.scp2i[c];
+    d = (BT ? dk[c] * W(A, W_OM)[nn * sl + c] : dk[c]) -
+        ((uf[c + 1] - uf[c]) + (vf[c + ld] - vf[c])) * A.delt1 * A.scp2i[c];
     dk[c] = d;
     A.dpo[((long long)k + (long long)mm * A.kdm) * sl + c] = d;
     sea = true;
@@ -503,8 +511,13 @@ cudaError_t launch_cnuity_layers(const CnuityArgs &a, int *launches, cudaStream_
   cn_init<<<grid_for(a, 6), b, 0, s>>>(a);
   nl++;
   for (int k = 0; k < a.kdm; k++) {  // loop 76
-    cn_flux<<<grid_for(a, 5), b, 0, s>>>(a, k);
-    cn_low<<<grid_for(a, 4), b, 0, s>>>(a, k);
+    if (a.btrmas) {
+      cn_flux<true><<<grid_for(a, 5), b, 0, s>>>(a, k);
+      cn_low<true><<<grid_for(a, 4), b, 0, s>>>(a, k);
+    } else {
+      cn_flux<false><<<grid_for(a, 5), b, 0, s>>>(a, k);
+      cn_low<false><<<grid_for(a, 4), b, 0, s>>>(a, k);
+    }
     cn_ratio<<<grid_for(a, 4), b, 0, s>>>(a, k);
     cn_clip<<<grid_for(a, 3), b, 0, s>>>(a, k);
     cn_update<<<grid_for(a, 2), b, 0, s>>>(a, k, 2, a.kdm + k);
