@@ -1,12 +1,12 @@
 """A second, independent restatement of advem_fct2 (mod_tsadvc.F90:645-997),
-advem_fct4 (:1370-1706) and advem_mpdata (:207-493) in vectorised numpy —
-whole-array stages over the reference's margins instead of the oracle's
-cell loops — checked against the C oracle bit for bit on small basins with
-coasts, islands and a periodic channel.  These are the known-answer tests of
-the leapfrog schemes: two restatements written apart must agree on every
-value, the Zalesak limiter's coastal ipip1/ipjp1 quirk, the section-edge
-zeroing, FCT4's fall back to 2nd order next to closed faces and MPDATA's
-posdef offset included."""
+advem_fct4 (:1370-1706), advem_mpdata (:207-493) and advem_pcm (:495-643)
+in vectorised numpy -- whole-array stages over the reference's margins
+instead of the oracle's cell loops -- checked against the C oracle bit for
+bit on small basins with coasts, islands and a periodic channel.  These are
+the known-answer tests of the four schemes: two restatements written apart
+must agree on every value, the Zalesak limiter's coastal ipip1/ipjp1
+quirk, the section-edge zeroing, FCT4's fall back to 2nd order next to
+closed faces and MPDATA's posdef offset included."""
 import numpy as np
 import pytest
 
@@ -208,6 +208,29 @@ def mpdata_numpy(g, fld, u, v, fco, fcn, posdef, scal, scali, dt2):
     return out
 
 
+def pcm_numpy(g, fld, u, v, fco, fcn, scal, scali, dt2):
+    """advem_pcm (mod_tsadvc.F90:495-643): donor cell, clipped to the sea-only
+    5-point extrema; margins 1 and 0 (mbdy = 2)."""
+    S = Slice(g, fld.shape)
+    sh, ip, iu, iv = S.sh, S.ip, S.iu, S.iv
+    flx, fly, fmx, fmn = S.nan(), S.nan(), S.nan(), S.nan()
+    r = S.region(1)
+    m = r & iu
+    flx[m] = (u * np.where(u >= 0.0, sh(fld, -1, 0), fld))[m]
+    m = r & iv
+    fly[m] = (v * np.where(v >= 0.0, sh(fld, 0, -1), fld))[m]
+    m = r & ip
+    fmx[m] = S.five(fld, np.maximum)[m]
+    fmn[m] = S.five(fld, np.minimum)[m]
+    S.zero_edges(flx, fly, 1)
+    out = fld.copy()
+    m = S.region(0) & ip
+    fd = ((sh(flx, 1, 0) - flx) + (sh(fly, 0, 1) - fly)) * dt2 * scali
+    q = fld * (fco + ONEMU) - fd
+    out[m] = np.maximum(fmn, np.minimum(fmx, q / (fcn + ONEMU)))[m]
+    return out
+
+
 def slice_case(nx, ny, periodic, seed):
     b = basin(nx, ny, periodic, seed)
     g = oracle_grid(b, threads=1)
@@ -249,5 +272,15 @@ def test_mpdata_numpy_equals_oracle(nx, ny, periodic, seed, posdef):
     want = mpdata_numpy(g, fld, u, v, fco, fcn, posdef, c["scp2"], c["scp2i"], 1800.0)
     got = fld.copy()
     g.advem(1, got, fldc, u, v, fco, fcn, posdef, c["scp2"], c["scp2i"], 1800.0)
+    assert np.array_equal(got[sea], want[sea])
+    assert not np.array_equal(got[sea], fld[sea])
+
+
+@pytest.mark.parametrize("nx,ny,periodic,seed", CASES)
+def test_pcm_numpy_equals_oracle(nx, ny, periodic, seed):
+    b, g, c, fld, fldc, u, v, fco, fcn, sea = slice_case(nx, ny, periodic, seed)
+    want = pcm_numpy(g, fld, u, v, fco, fcn, c["scp2"], c["scp2i"], 1800.0)
+    got = fld.copy()
+    g.advem(0, got, fldc, u, v, fco, fcn, 0.0, c["scp2"], c["scp2i"], 1800.0)
     assert np.array_equal(got[sea], want[sea])
     assert not np.array_equal(got[sea], fld[sea])
