@@ -129,3 +129,83 @@ def test_rejects_th3d_advection():
     a = assel_case(b, g, ntracr=0)
     with pytest.raises(O.OracleError):
         g.asselin_filter(1, 2, a, ra2fac=0.125, oneta0=0.1, advflg=1)
+
+
+def asselin_numpy(g, b, a, m, n, ra2fac, oneta0, thbase):
+    """asselin_save then asselin_filter (mod_asselin.F90:28-82, :84-268,
+    hybrid layers advecting temperature, no mxlmy) restated apart from the
+    oracle as whole-slice numpy, in place on a copy of the arrays."""
+    mm, nn = m - 1, n - 1
+    inner = np.zeros((b.ld2, b.ld1), bool)
+    inner[b.J, b.I] = True
+    sea = inner & (g.masks["ip"] != 0)
+    for lv in (nn, mm):  # :46-51
+        a["oneta"][lv][sea] = np.maximum(oneta0, 1.0 + a["pbavg"][lv] / a["pbot"])[sea]
+        a["onetao"][lv][sea] = a["oneta"][lv][sea]
+    for k, o in (("temp", "otemp"), ("saln", "osaln"), ("th3d", "oth3d")):  # :53-60
+        a[o][:, inner] = a[k][nn][:, inner]
+    if a["tracer"] is not None:
+        a["otracer"][:, :, inner] = a["tracer"][:, nn][:, :, inner]
+    g.xctilr(a["oneta"], 6, 6)  # :77-78
+    g.xctilr(a["onetao"], 6, 6)
+    return sea
+
+
+def asselin_filter_numpy(a, sea, m, n, ra2fac, oneta0, thbase):
+    from oracle import oracle as O
+
+    mm, nn = m - 1, n - 1
+    for lv in (nn, mm):  # :110-115
+        a["oneta"][lv][sea] = np.maximum(oneta0, 1.0 + a["pbavg"][lv] / a["pbot"])[sea]
+    onezm = 9806.e-20
+    kdm = a["temp"].shape[1]
+    for k in range(kdm):
+        dpold = a["dpo"][nn, k] * a["onetao"][nn]
+        dpmid = a["dpo"][mm, k] * a["onetao"][mm]
+        dpnew = a["dp"][nn, k] * a["oneta"][nn]
+        q = 0.5 * ra2fac * ((dpold + dpnew) - 2.0 * dpmid)
+        dpmidn = dpmid + q
+        with np.errstate(divide="ignore", invalid="ignore"):  # land cells carry zeros
+            a["dp"][mm, k][sea] = (dpmidn / a["oneta"][mm])[sea]
+            qd = 1.0 / dpmidn
+        live = sea & (dpmidn > onezm)
+
+        def filt(old, mid, new):  # :140-156, :170-178, :205-213
+            smin = np.minimum(np.minimum(old, mid), new)
+            so, sm, sn = dpold * (old - smin), dpmid * (mid - smin), dpnew * (new - smin)
+            with np.errstate(invalid="ignore"):
+                return smin + (sm + 0.5 * ra2fac * ((so + sn) - 2.0 * sm)) * qd
+
+        a["saln"][mm, k][live] = filt(a["osaln"][k], a["saln"][mm, k], a["saln"][nn, k])[live]
+        a["temp"][mm, k][live] = filt(a["otemp"][k], a["temp"][mm, k], a["temp"][nn, k])[live]
+        t, s = a["temp"][mm, k][live], a["saln"][mm, k][live]
+        a["th3d"][mm, k][live] = [O.sig(x, y) - thbase for x, y in zip(t, s)]
+        if a["tracer"] is not None:
+            for q_ in range(a["tracer"].shape[0]):
+                tr = a["tracer"][q_]
+                tr[mm, k][live] = filt(a["otracer"][q_, k], tr[mm, k], tr[nn, k])[live]
+
+
+@pytest.mark.parametrize("periodic,ntracr", [(False, 2), (True, 0)])
+def test_asselin_numpy_equals_oracle(periodic, ntracr):
+    """Known answer: save, a new level n, filter -- the numpy restatement
+    equals the oracle bit for bit (dp(m), T, S, th3d, tracers, oneta)."""
+    b = basin(46, 34, periodic, 63)
+    g = oracle_grid(b, threads=1)
+    a = assel_case(b, g, kdm=3, ntracr=ntracr, seed=63)
+    rng = np.random.default_rng(63)
+    m, n = 1, 2
+    w = {k: (None if v is None else v.copy()) for k, v in a.items()}
+    g.asselin_save(m, n, a, oneta0=0.1)
+    sea = asselin_numpy(g, b, w, m, n, 0.125, 0.1, 34.0)
+    advance(a, n, rng)  # the same new level n for both
+    for k in ("temp", "saln", "dp", "pbavg"):
+        w[k][n - 1] = a[k][n - 1]
+    if a["tracer"] is not None:
+        w["tracer"][:, n - 1] = a["tracer"][:, n - 1]
+    g.asselin_filter(m, n, a, ra2fac=0.125, oneta0=0.1, thbase=34.0)
+    asselin_filter_numpy(w, sea, m, n, 0.125, 0.1, 34.0)
+    for k in ("dp", "temp", "saln", "th3d", "tracer", "oneta", "onetao", "otemp", "osaln", "oth3d"):
+        if a[k] is not None:
+            assert np.array_equal(a[k], w[k]), k
+    assert not np.array_equal(a["temp"][m - 1], assel_case(b, g, kdm=3, ntracr=ntracr, seed=63)["temp"][m - 1])
