@@ -241,6 +241,9 @@ ENS_FORMS = {  # form -> (precision, FP64 thickness prep, advtyp)
     "mixed-fp32prep-mpdata": ("mixed", False, 1),
 }
 FP64_REF = {2: "fp64", 4: "fp64-fct4", 1: "fp64-mpdata"}  # the FP64 form each mixed form is checked against
+# the ncu capture (profiles/) whose DRAM traffic a form's strip kernel launch is quoted with
+TRAFFIC_KEY = {"mixed-fp32prep": "col2_mixed_fp32prep", "mixed-fp32prep-fct4": "col2_mixed_fp32prep_fct4",
+               "mixed-fp32prep-mpdata": "col2_mixed_fp32prep_mpdata"}
 KERNEL_OF_TILE = {26: "mix_fct2_col_kernel", 56: "mix_fct2_col2_kernel"}
 
 
@@ -328,7 +331,9 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
         # MPDATA reads no centre level: 2 tracer slices per update instead of 3
         bpu = bytes_per_update(s_t, s_t, s_dp, 2, kdm, 2 if adv == 1 else 3)
         ach = ups_step * bpu / (ms / 1e3) / 1e9
+        tkey = TRAFFIC_KEY.get(form) if tx == 56 else None
         out[form] = {"value": ws * ups_step / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "advtyp": adv,
+                     "traffic_bytes_per_launch": profile_traffic(f"{tkey}_{args.workload}") if tkey else None,
                      "tile": [tx, ty],
                      "tracers_per_pass": nq, "kernel": KERNEL_OF_TILE.get(tx, "fct tile kernel"),
                      "algorithmic_bytes_per_update": bpu, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
