@@ -236,15 +236,16 @@ ENS_FORMS = {  # form -> (precision, FP64 thickness prep, advtyp)
     "mixed": ("mixed", True, 2),
     "mixed-fp32prep": ("mixed", False, 2),
     "fp64-fct4": ("fp64", True, 4),
-    "mixed-fp32prep-fct4": ("mixed", False, 4),
+    "mixed-fct4": ("mixed", True, 4),
     "fp64-mpdata": ("fp64", True, 1),
-    "mixed-fp32prep-mpdata": ("mixed", False, 1),
+    "mixed-mpdata": ("mixed", True, 1),
 }
 FP64_REF = {2: "fp64", 4: "fp64-fct4", 1: "fp64-mpdata"}  # the FP64 form each mixed form is checked against
 # the ncu capture (profiles/) whose DRAM traffic a form's strip kernel launch is quoted with
-TRAFFIC_KEY = {"mixed-fp32prep": "col2_mixed_fp32prep", "mixed-fp32prep-fct4": "col2_mixed_fp32prep_fct4",
-               "mixed-fp32prep-mpdata": "col2_mixed_fp32prep_mpdata"}
-KERNEL_OF_TILE = {26: "mix_fct2_col_kernel", 56: "mix_fct2_col2_kernel"}
+TRAFFIC_KEY = {"mixed": "col2_mixed", "mixed-fp32prep": "col2_mixed_fp32prep", "mixed-fct4": "col2_mixed_fct4",
+               "mixed-mpdata": "col2_mixed_mpdata", "fp64": "fct2_fp64_ens"}
+KERNEL_OF_FORM = {"mixed": "mix_col2_kernel<FCT2,2,PREP64>", "mixed-fp32prep": "mix_col2_kernel<FCT2,2,FP32 prep>",
+                  "mixed-fct4": "mix_col2_kernel<FCT4,2,PREP64>", "mixed-mpdata": "mix_col2_kernel<MPDATA,2,PREP64>"}
 
 
 def make_ensemble(spec, form, stream):
@@ -325,17 +326,15 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
             ms = float(t.item())
         ms /= args.steps
         ws = dist.get_world_size() if dist else 1
-        s_t = 8 if prec == "fp64" else 4  # fluxes as the tracers
-        # dp: FP64, except that the strip kernel with the FP32 thickness prep stages the FP32 copy made at put
-        s_dp = 4 if (prec == "mixed" and not ENS_FORMS[form][1] and tx == 56) else 8
+        s_t = 8 if prec == "fp64" else 4  # fluxes as the tracers; dp is FP64 in every form
         # MPDATA reads no centre level: 2 tracer slices per update instead of 3
-        bpu = bytes_per_update(s_t, s_t, s_dp, 2, kdm, 2 if adv == 1 else 3)
+        bpu = bytes_per_update(s_t, s_t, 8, 2, kdm, 2 if adv == 1 else 3)
         ach = ups_step * bpu / (ms / 1e3) / 1e9
-        tkey = TRAFFIC_KEY.get(form) if tx == 56 else None
+        tkey = TRAFFIC_KEY.get(form)
         out[form] = {"value": ws * ups_step / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "advtyp": adv,
                      "traffic_bytes_per_launch": profile_traffic(f"{tkey}_{args.workload}") if tkey else None,
                      "tile": [tx, ty],
-                     "tracers_per_pass": nq, "kernel": KERNEL_OF_TILE.get(tx, "fct tile kernel"),
+                     "tracers_per_pass": nq, "kernel": KERNEL_OF_FORM.get(form, "fct tile/queue kernel (FP64)"),
                      "algorithmic_bytes_per_update": bpu, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
                      "graph_steps": args.steps, "clocks": clk.summary(),
                      "content_change_one_step": {n: abs(c_new[q] - c_old[q]) / abs(c_old[q])
@@ -735,7 +734,43 @@ def sea_mask(b, masks, dev):
 
 
 def run_ensemble_workload(args, wl, dev):
-    """c2 (precision form) and c3 (batching form) through the ensemble API.
+    """c2 (precision form) and c3 (batching form) through the ensemble API,
+    printed as their own bench line (see ensemble_workload)."""
+    import torch
+
+    ws, rank, local = dist_setup()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+    forms = [f for f in args.ens_forms.split(",") if f]
+    t_start = time.perf_counter()
+    out = ensemble_workload(args, wl, args.workload, dev, dist, forms)
+    res, desc, ups, steps = out["forms"], out["workload"], out["updates_per_step"], out["steps"]
+    peak, peak_kind = peak_hbm()
+    head_form = "mixed" if "mixed" in res else forms[-1]
+    head = res[head_form]
+    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": ws, "steps": steps,
+            "warmup": 1, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-mixed" if head_form != "fp64" else "f64",
+            "data": "synthetic (seeded generator, HYCOM units/layout)", "impl": f"ensemble-{args.workload}",
+            "config": {"workload": desc, "form": head_form, "updates_per_step": ups,
+                       "l2": "inputs larger than L2 (state resident in HBM)"},
+            "roofline": {"bound": "hbm", "achieved": head["achieved_GBs"], "peak": peak, "unit": "GB/s",
+                         "frac": head["frac_of_measured_hbm"], "traffic": None, "peak_kind": peak_kind},
+            "clocks": head["clocks"], "wall_seconds": time.perf_counter() - t_start, "forms": res}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def ensemble_workload(args, wl, workload, dev, dist, forms, fp64_steps=None):
+    """c2 (precision form) or c3 (batching form) through the ensemble API.
 
     Every form (FP64 plain, FP32-mixed with FP64 thickness prep, FP32-mixed
     with compensated FP32 prep) is loaded from the same seeded inputs,
@@ -758,13 +793,6 @@ def run_ensemble_workload(args, wl, dev):
     from hycadv import shard as hshard
 
     ws, rank, local = dist_setup()
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
-    torch.cuda.set_device(local)
-    dev = torch.device(f"cuda:{local}")
 
     def reduce(vals, op):
         if not dist:
@@ -773,7 +801,7 @@ def run_ensemble_workload(args, wl, dev):
         dist.all_reduce(t, op=op)
         return t.tolist()
 
-    if args.workload == "c3":
+    if workload == "c3":
         members = c3_members(wl)
         if args.layers:
             for m in members:
@@ -787,7 +815,6 @@ def run_ensemble_workload(args, wl, dev):
         members = [dict(nx=wl["nx"], ny=wl["ny"], kdm=args.layers or wl["kdm"], ntr=wl["ntr"], seed=wl["seed"])]
         nbasin_all = ws
         steps = args.steps
-    forms = [f for f in args.ens_forms.split(",") if f]
     if forms[0] != "fp64":
         raise SystemExit("--ens-forms must start with fp64 (the reference the others are compared with)")
     t_start = time.perf_counter()
@@ -838,7 +865,7 @@ def run_ensemble_workload(args, wl, dev):
                 del new
             del buf
         torch.cuda.empty_cache()
-        names = ["temp", "saln"] + [f"passive{q - 1}" for q in range(2, 6 if args.workload == "c3" else ntr_max)]
+        names = ["temp", "saln"] + [f"passive{q - 1}" for q in range(2, 6 if workload == "c3" else ntr_max)]
         while len(per_q) < len(names):  # every rank reports the same tracer slots
             per_q.append({"max_rel": 0.0, "sq": 0.0, "n": 0, "cons": 0.0, "extrema_excess": 0.0})
         if dist:
@@ -854,7 +881,8 @@ def run_ensemble_workload(args, wl, dev):
                 r["max_rel_err_vs_fp64"] = acc["max_rel"]
                 r["rms_rel_err_vs_fp64"] = (acc["sq"] / max(acc["n"], 1)) ** 0.5
             rep[names[q]] = r
-        ens.step(2, wl["delt1"], steps, graph=True)  # capture (and warm up)
+        fsteps = fp64_steps if (form == "fp64" and fp64_steps) else steps
+        ens.step(2, wl["delt1"], fsteps, graph=True)  # capture (and warm up)
         torch.cuda.synchronize(dev)
         if dist:
             dist.barrier()
@@ -863,20 +891,19 @@ def run_ensemble_workload(args, wl, dev):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with ClockSampler(local) as clk:
             e0.record(st)
-            ens.step(2, wl["delt1"], steps, graph=True)
+            ens.step(2, wl["delt1"], fsteps, graph=True)
             e1.record(st)
             torch.cuda.synchronize(dev)
         if dist:
             dist.barrier()
-        ms = reduce([e0.elapsed_time(e1) / steps], dist.ReduceOp.MAX if dist else None)[0]
+        ms = reduce([e0.elapsed_time(e1) / fsteps], dist.ReduceOp.MAX if dist else None)[0]
         s_t = 8 if prec == "fp64" else 4
-        s_dp = 4 if (form == "mixed-fp32prep" and tx == 56) else 8  # the strip kernel stages dp in FP32 then
-        nbytes = sum(s["idm"] * s["jdm"] * s["kdm"] * s["ntr"] * bytes_per_update(s_t, s_t, s_dp, s["ntr"], s["kdm"])
+        nbytes = sum(s["idm"] * s["jdm"] * s["kdm"] * s["ntr"] * bytes_per_update(s_t, s_t, 8, s["ntr"], s["kdm"])
                      for s in specs)
         nbytes = reduce([nbytes], dist.ReduceOp.SUM if dist else None)[0]
         ach = nbytes / (ms / 1e3) / 1e9
         res[form] = {"value": ups / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "tile": [tx, ty],
-                     "graph_steps": steps, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
+                     "graph_steps": fsteps, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
                      "algorithmic_bytes_per_step": nbytes, "load_seconds": t_load, "per_tracer": rep,
                      "clocks": clk.summary()}
         ens.close()
@@ -884,30 +911,16 @@ def run_ensemble_workload(args, wl, dev):
         torch.cuda.empty_cache()
     refs.clear()
     for f in forms[1:]:
-        res[f"{f}_speedup_vs_fp64"] = res[f]["value"] / res["fp64"]["value"]
-    head_form = "mixed-fp32prep" if "mixed-fp32prep" in res else forms[-1]
-    head = res[head_form]
-    if args.workload == "c3":
+        res[f]["speedup_vs_fp64"] = res[f]["value"] / res["fp64"]["value"]
+    if workload == "c3":
         desc = (f"c3: {nbasin_all} closed basins, nx 120-1500, ny 90-1100, kdm 22/32/41, 2-6 tracers (T, S, "
                 f"passive), FCT2, max Courant {wl['courant']}, delt1 {wl['delt1']} s, {steps}-step CUDA graph"
                 + (f", sharded over {ws} GPUs" if ws > 1 else ""))
     else:
         desc = (f"c2: periodic-x basin {wl['nx']}x{wl['ny']}x{members[0]['kdm']}, T+S+8 passive tracers "
                 f"(log-uniform 1e-6..1e2 with fronts), FCT2, max Courant {wl['courant']}, delt1 {wl['delt1']} s")
-    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": ws, "steps": steps,
-            "warmup": 1, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32-mixed" if head_form != "fp64" else "f64",
-            "data": "synthetic (seeded generator, HYCOM units/layout)", "impl": f"ensemble-{args.workload}",
-            "config": {"workload": desc, "form": head_form, "updates_per_step": ups,
-                       "l2": "inputs larger than L2 (state resident in HBM)"},
-            "roofline": {"bound": "hbm", "achieved": head["achieved_GBs"], "peak": peak, "unit": "GB/s",
-                         "frac": head["frac_of_measured_hbm"], "traffic": None, "peak_kind": peak_kind},
-            "clocks": head["clocks"], "wall_seconds": time.perf_counter() - t_start, "forms": res}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
-    return 0
+    return {"forms": res, "workload": desc, "updates_per_step": ups, "steps": steps,
+            "wall_seconds": time.perf_counter() - t_start}
 
 
 def c4_members(wl, layers=0):
@@ -921,14 +934,14 @@ def c4_members(wl, layers=0):
 
 def mixed_state_bytes(spec):
     """Device bytes of one FP32-mixed ensemble basin (three tracer levels,
-    fluxes, dp and the per-cell tables)."""
+    fluxes, dp, masks, metrics and the per-cell words)."""
     ld1 = (spec["idm"] + 2 * spec["nbdy"] + 3) // 4 * 4
     sl = ld1 * (spec["jdm"] + 2 * spec["nbdy"])
-    return sl * spec["kdm"] * (3 * spec["ntr"] * 4 + 2 * 4 + 8) + sl * (1 + 8 + 8 + 8 + 16 + 8)
+    return sl * spec["kdm"] * (3 * spec["ntr"] * 4 + 2 * 4 + 8) + sl * (1 + 8 + 8 + 8)
 
 
 def run_c4(args, wl, dev):
-    """Combined workload: FP32-mixed FCT2 and MPDATA (compensated FP32 prep)
+    """Combined workload: FP32-mixed FCT2 and MPDATA (the precision form)
     over 48 basins advanced in resident waves (each wave: load, then all
     steps replayed from a 10-step CUDA graph).  The error against the FP64
     form, the content change and the new-extrema check come from one step of
@@ -967,8 +980,6 @@ def run_c4(args, wl, dev):
         refs = {}
         for prec in ("fp64", "mixed"):
             ens = hycadv.Ensemble([specs[small]], precision=prec)
-            if prec == "mixed":
-                ens.set_prep64(False)
             ens.set_posdef(0, 0, 256.0)
             bounds = load_member(ens, 0, members[small], geos[small], wl, dev)
             ens.tune(adv, wl["delt1"])
@@ -1013,7 +1024,6 @@ def run_c4(args, wl, dev):
         t_ms, t_ups, load_s, tile, nq, clk_all = 0.0, 0.0, 0.0, None, None, []
         for wv in waves:
             ens = hycadv.Ensemble([specs[i] for i in wv], precision="mixed")
-            ens.set_prep64(False)
             for j in range(len(wv)):
                 ens.set_posdef(j, 0, 256.0)
             t0 = time.perf_counter()
@@ -1045,9 +1055,8 @@ def run_c4(args, wl, dev):
             del ens
             torch.cuda.empty_cache()
         rate = t_ups / (t_ms / 1e3)
-        s_dp = 4 if tile[0] == 56 else 8  # FP32 prep: the strip kernel stages dp in FP32
         nbytes = sum(sp["idm"] * sp["jdm"] * sp["kdm"] * sp["ntr"] *
-                     (bytes_per_update(4, 4, s_dp, sp["ntr"], sp["kdm"]) - (4 if adv == 1 else 0)) for sp in specs)
+                     (bytes_per_update(4, 4, 8, sp["ntr"], sp["kdm"]) - (4 if adv == 1 else 0)) for sp in specs)
         ach = nbytes * (t_ups / ups_step) / (t_ms / 1e3) / 1e9
         res[name] = {"value": rate, "unit": UNIT, "ms_per_step_all_basins": t_ms / (gsteps * reps), "tile": list(tile),
                      "tracers_per_pass": nq, "achieved_GBs": ach, "frac_of_measured_hbm": ach / peak,
@@ -1089,7 +1098,7 @@ def run_c4(args, wl, dev):
             "ms_per_step": head["ms_per_step_all_basins"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32-mixed", "data": "synthetic (seeded generator, HYCOM units/layout)",
             "impl": "ensemble-c4",
-            "config": {"workload": desc, "form": "mixed-fp32prep", "updates_per_step": ups_step,
+            "config": {"workload": desc, "form": "mixed", "updates_per_step": ups_step,
                        "l2": "inputs larger than L2 (state resident in HBM)"},
             "roofline": {"bound": "hbm", "achieved": head["achieved_GBs"], "peak": peak, "unit": "GB/s",
                          "frac": head["frac_of_measured_hbm"], "traffic": None, "peak_kind": peak_kind},
@@ -1117,19 +1126,21 @@ def main():
     ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS))
     ap.add_argument("--advtyp", type=int, default=2, choices=[0, 1, 2, 4])
     ap.add_argument("--layers", type=int, default=0, help="override kdm (smaller profiling case)")
-    ap.add_argument("--form", default="mixed-fp32prep", choices=sorted(ENS_FORMS),
-                    help="headline form (ensemble API): FP32-mixed with FP64 thickness prep, with compensated "
-                         "FP32 prep, or FP64")
-    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-full,cnuity,fp64,mixed,mixed-fp32prep,"
-                                       "fp64-fct4,mixed-fp32prep-fct4,fp64-mpdata,mixed-fp32prep-mpdata",
+    ap.add_argument("--form", default="mixed", choices=sorted(ENS_FORMS),
+                    help="headline form (ensemble API): mixed = the precision form (FP32 fluxes, limiter and "
+                         "update; FP64 thickness prep and dp), mixed-fp32prep = the same with the thickness "
+                         "factors in compensated FP32, fp64 = the FP64 form")
+    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-full,cnuity,fp64,mixed-fp32prep,"
+                                       "fp64-fct4,mixed-fct4,fp64-mpdata,mixed-mpdata,c3",
                     help="forms measured beside the headline (tsadvc[-fct4|-mpdata|-pcm] = FP64 plain through "
                          "hyc_tsadvc, FCT2 unless named; tsadvc-full = asselin_save + tsadvc + its "
                          "diffusion + asselin_filter; cnuity = the continuity equation; fp64[-fct4|-mpdata], "
-                         "mixed[-fp32prep][-fct4|-mpdata] = the ensemble API, FCT2 unless named)")
+                         "mixed[-fp32prep|-fct4|-mpdata] = the ensemble API, FCT2 unless named; c3 = the "
+                         "96-basin batched workload, FP64 and mixed)")
     ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--c4-steps", type=int, default=100, help="c4: steps per basin")
     ap.add_argument("--tile", default="", help="mixed forms: fixed tile 'tx,ty,tracers_per_pass' instead of the tuner")
-    ap.add_argument("--ref-layers", type=int, default=4, help="layers in the CPU sample")
+    ap.add_argument("--ref-layers", type=int, default=0, help="layers in the CPU sample (0: all of the workload's)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -1137,6 +1148,8 @@ def main():
                     help="c2/c3: ensemble forms to run, fp64 first")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.ref_layers <= 0:
+        args.ref_layers = args.layers or WORKLOADS[args.workload]["kdm"]
     args.tile = tuple(int(x) for x in args.tile.split(",")) if args.tile else None
     wl = dict(WORKLOADS[args.workload])
     if args.layers > 0:
@@ -1201,17 +1214,23 @@ def main():
     del case
     torch.cuda.empty_cache()
 
+    c3 = None
+    if "c3" in others:  # the batched workload: FP64 (3 graph steps) and the precision form (K steps)
+        c3 = ensemble_workload(args, dict(WORKLOADS["c3"]), "c3", dev, dist, ["fp64", "mixed"], fp64_steps=3)
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, desc, n, _ = run_cpu_sample(wl, nlayers=args.ref_layers, min_seconds=args.cpu_seconds, steps_max=20,
-                                          warmup=1, advtyp=args.advtyp, threads=threads, gen_device=dev)
+                                          warmup=1, advtyp=args.advtyp, threads=threads, gen_device=dev,
+                                          min_steps=2)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
 
     if rank == 0:
         peak, peak_kind = peak_hbm()
         prec = ENS_FORMS[args.form][0]
-        key = {"mixed": "col2_mixed", "mixed-fp32prep": "col2_mixed_fp32prep", "fp64": "fct2_fp64_ens"}.get(args.form)
+        key = TRAFFIC_KEY.get(args.form)
         roof = {"bound": "hbm", "achieved": head["achieved_GBs"], "peak": peak, "unit": "GB/s",
                 "frac": head["frac_of_measured_hbm"],
                 "traffic": profile_traffic(f"{key}_{args.workload}") if key else None,
@@ -1225,6 +1244,15 @@ def main():
         if tsadvc:
             others_out["fp64-tsadvc"] = tsadvc
             head["speedup_vs_fp64_tsadvc"] = head["value"] / tsadvc["value"]
+        if c3:
+            others_out["c3"] = c3
+        # one compact line of the figures the forms below hold in full
+        summary = {f: round(r["value"] / 1e9, 2) for f, r in others_out.items()
+                   if isinstance(r, dict) and "value" in r}
+        if c3:
+            for f, r in c3["forms"].items():
+                summary[f"c3-{f}"] = round(r["value"] / 1e9, 2)
+                summary[f"c3-{f}-frac_hbm"] = round(r["frac_of_measured_hbm"], 3)
         line = {
             "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -1234,7 +1262,8 @@ def main():
                            tracers_per_pass=head["tracers_per_pass"],
                            sea_updates_per_step=sea_cells * wl["kdm"] * 2),
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
-            "clocks": head["clocks"], "headline": {k: v for k, v in head.items() if k != "clocks"},
+            "clocks": head["clocks"], "gupdates_per_s": summary,
+            "headline": {k: v for k, v in head.items() if k != "clocks"},
             "forms": others_out, "wall_seconds": time.perf_counter() - t_start,
         }
         print(json.dumps(line), flush=True)

@@ -32,10 +32,8 @@ UNITS = {
     "hyc_cnuity.cu": ["-lineinfo", "-fmad=false"],
     "hyc_host.cpp": [],
     "hyc_noalloc.cu": ["-lineinfo"],
-    "hyc_mixed.cu": ["-lineinfo"],
-    "hyc_mixed_tma.cu": ["-lineinfo"],
-    "hyc_mixed_col.cu": ["-lineinfo"],
     "hyc_mixed_col2.cu": ["-lineinfo"],
+    "hyc_ens_util.cu": ["-lineinfo"],
     "hyc_ens_host.cpp": [],
     "hyc_za.cpp": [],
 }

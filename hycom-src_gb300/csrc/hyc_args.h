@@ -30,6 +30,10 @@ struct TileArgs {
   // tsadvc mode, per layer k (0-based): uflx + k*slice, vflx + k*slice, dpn + k*slice
   const double *uflx, *vflx, *dpn;
   const double *oneta_n;  // onetamas(:,:,m) when btrmas (mod_tsadvc.F90:1806), else null
+  // tsadvc mode, isopycnic layer 1 only: the fluxes whose divergence gives
+  // fco (the smoothed mixed-layer fluxes, mod_tsadvc.F90:1860-1897) when the
+  // fields advected by uflx/vflx are not the ones smoothed; null otherwise
+  const double *ufco, *vfco;
   // advem mode (single slice)
   const double *fco, *fcn;
   double dt2;

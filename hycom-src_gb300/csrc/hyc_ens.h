@@ -17,56 +17,28 @@ namespace hyc {
 struct MixBasin {
   int ii, jj, nbdy, ld1, ld2;
   long long slice;
-  int ntx, nty, kdm, ntr;
+  int kdm, ntr;
   int images;  // periodic-x halo images to write (0 when closed)
+  int seg;     // rows per strip segment
+  int kchunk;  // layers per work item
   int pad;
-  double dt2;
-  const uint8_t *msk;
-  const double *scp2, *scp2i;
-  const float *uflx, *vflx;   // kdm slices
-  const double *dp;           // kdm slices, dp(:,:,k,n)
-  const float *fold, *fcur;   // ntr*kdm slices, levels t-1 and t
-  float *fnew;                // ntr*kdm slices, level t+1
-  // TMA descriptors (device memory) for the current tile shape: levels t-1
-  // and t (3-D: ld1 x ld2 x ntr*kdm, FP32), uflx, vflx (FP32) and dp (FP64)
-  const CUtensorMap *tm_old, *tm_cur, *tm_u, *tm_v, *tm_dp;
-  // column kernel: (dt2*scp2i, scp2/dt2) per cell, rows per segment
-  const float2 *dsqs;
-  int seg;
-  int kchunk;  // two-column strip kernel: layers per work item
+  float *fnew;  // ntr*kdm slices, level t+1
   float posdef[kMaxFields];  // MPDATA offset of each tracer (mod_tsadvc.F90:1755-1763)
-  // two-column strip kernel: TMA maps (box 64 x 4 rows) of the old and
-  // centre levels, uflx, vflx, dp, the per-cell factors (float4 as 4*ld1
-  // floats per row) and dt2*scp2i (FP64)
-  const CUtensorMap *c2_old, *c2_cur, *c2_u, *c2_v, *c2_dp, *c2_ge, *c2_si, *c2_dp32;
+  // TMA maps (box 64 x 4 rows, device memory): levels t-1 and t (3-D, ld1 x
+  // ld2 x ntr*kdm, FP32), uflx, vflx (FP32), dp (FP64) and the per-cell
+  // words (2-D, FP64)
+  const CUtensorMap *c2_old, *c2_cur, *c2_u, *c2_v, *c2_dp, *c2_cg;
 };
 
-bool mix_shape_ok(TileShape t);
-cudaError_t launch_mix_fct2(TileShape t, const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm,
-                            bool prep64, cudaStream_t s);
-
-bool mix_tma_shape_ok(TileShape t);
-cudaError_t launch_mix_fct2_tma(TileShape t, const MixBasin *basins, const int4 *items, int nitems, int *head,
-                                int nsm, bool prep64, int *err, cudaStream_t s);
-// one warp per 32-column strip (26 updated), segments of `seg` rows
-constexpr int kColStrip = 26;
-cudaError_t launch_mix_fct2_col(const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm, int nq,
-                                bool prep64, int seg, cudaStream_t s);
 // two columns per lane, 64-column strips (56 updated) streamed by TMA
 constexpr int kCol2Strip = 56;
 constexpr int kCol2Box = 64, kCol2Rows = 4;
 cudaError_t launch_mix_col2(int scheme, const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm,
                             int nq, bool prep64, int *err, cudaStream_t s);
-cudaError_t launch_geo4(const double *scp2, const double *scp2i, const uint8_t *msk, double dt2, long long n,
-                        float4 *out, cudaStream_t s);
+// per-cell words: dt2*scp2i with the ip, iu, iv bits of msk in the three lowest mantissa bits
+cudaError_t launch_cell_words(const double *scp2i, const uint8_t *msk, double dt2, long long n, double *out,
+                              cudaStream_t s);
 cudaError_t launch_wait_probe(int arrive, int *err, cudaStream_t s);
-cudaError_t launch_dtsi(const double *scp2i, double dt2, long long n, double *out, cudaStream_t s);
-cudaError_t launch_dsqs(const double *scp2, const double *scp2i, double dt2, long long n, float2 *out,
-                        cudaStream_t s);
-
-// TMA box width (elements) of a tile shape: TX + 12 for the nbdy = 6 halo
-inline int tma_box_x(TileShape t) { return (t.tx + 9 + 3) / 4 * 4; }
-inline int tma_box_y(TileShape t) { return t.ty + 6; }
 
 // FP64 ensemble: the FCT tile body over a queue of (basin, tile, layer)
 cudaError_t launch_fct_queue(int scheme, TileShape t, const TileArgs *basins, const int4 *items, int nitems,

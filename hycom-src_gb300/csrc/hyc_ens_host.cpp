@@ -29,11 +29,8 @@ struct EBasin {
   double *scp2 = nullptr, *scp2i = nullptr;
   void *uflx = nullptr, *vflx = nullptr;  // FP32 (mixed) or FP64
   double *dp = nullptr;
-  float *dp32 = nullptr;  // dp rounded to FP32 at put (mixed form): the strip kernel's FP32 thickness prep
   void *lev[3] = {nullptr, nullptr, nullptr};  // tracer state, physical levels
-  float2 *dsqs = nullptr;                       // column kernel metric factors (mixed form)
-  double *dtsi = nullptr;                       // dt2*scp2i (strip kernel, FP64 thickness prep)
-  float4 *geo4 = nullptr;                       // strip kernel per-cell factors
+  double *cell = nullptr;                       // strip kernel per-cell words (mixed form)
   long long work = 0;                           // cells*layers*tracers, for queue ordering
   std::vector<double> posdef;                   // MPDATA offset per tracer (0 unless set)
 };
@@ -50,12 +47,9 @@ struct hyc_ens {
   bool primed = false;   // NEW level initialised (land and halo cells) from CUR
   hyc::TileShape shape{32, 16};
   bool prep64 = true;  // FP32-mixed: thickness prep in FP64 (else compensated FP32)
-  bool use_tma = false;  // FP32-mixed: TMA-staged kernel (needs nbdy = 6 everywhere)
-  int maxntr = 1;        // largest tracer count (column kernel processes tracers in pairs)
-  int strip_nq = 2;      // two-column strip kernel: tracers per pass (1 or 2)
-  CUtensorMap *d_tmaps = nullptr;  // [nbasin][6]: level 0,1,2, uflx, vflx, dp
-  CUtensorMap *d_cmaps = nullptr;  // [nbasin][9]: strip kernel maps (levels 0-2, u, v, dp, geo4, si, dp32)
-  int tm_tx = 0, tm_ty = 0;        // shape the maps were encoded for
+  int maxntr = 1;        // largest tracer count
+  int strip_nq = 2;      // strip kernel: tracers per pass (1 or 2)
+  CUtensorMap *d_cmaps = nullptr;  // [nbasin][kMaps]: strip kernel maps (levels 0-2, u, v, dp, cell words)
   int *d_err = nullptr;            // device error flag (bounded waits that gave up)
   // device tables, one per rotation
   MixBasin *d_mix[3] = {nullptr, nullptr, nullptr};
@@ -134,11 +128,9 @@ struct Dev {
 
 size_t esz(const hyc_ens *e) { return e->prec == HYC_PREC_MIXED ? 4 : 8; }
 
-// tile shapes with tx == 26 select the column-strip kernel (ty = rows per segment)
-bool is_col(hyc::TileShape t) { return t.tx == hyc::kColStrip; }
 // tx == 56 selects the two-column strip kernel (ty = rows per segment)
 bool is_col2(hyc::TileShape t) { return t.tx == hyc::kCol2Strip; }
-bool is_strip(hyc::TileShape t) { return is_col(t) || is_col2(t); }
+constexpr int kMaps = 7;  // strip kernel maps per basin
 
 void free_all(hyc_ens *e) {
   for (auto &b : e->b) {
@@ -148,10 +140,7 @@ void free_all(hyc_ens *e) {
     cudaFree(b.uflx);
     cudaFree(b.vflx);
     cudaFree(b.dp);
-    cudaFree(b.dp32);
-    cudaFree(b.dsqs);
-    cudaFree(b.dtsi);
-    cudaFree(b.geo4);
+    cudaFree(b.cell);
     for (auto &l : b.lev) cudaFree(l);
   }
   for (int r = 0; r < 3; r++) {
@@ -174,7 +163,6 @@ void free_all(hyc_ens *e) {
   if (e->ev_gdone) cudaEventDestroy(e->ev_gdone);
   if (e->copy_stream) cudaStreamDestroy(e->copy_stream);
   if (e->in_stream) cudaStreamDestroy(e->in_stream);
-  cudaFree(e->d_tmaps);
   cudaFree(e->d_cmaps);
   cudaFree(e->d_err);
   if (e->gexec) cudaGraphExecDestroy(e->gexec);
@@ -214,10 +202,6 @@ bool encode3t(CUtensorMap *m, void *base, CUtensorMapDataType dt, size_t es, int
   return fn(m, dt, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
-bool encode3(CUtensorMap *m, void *base, bool fp64, int ld1, int ld2, long long nz, int bx, int by) {
-  return encode3t(m, base, fp64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, fp64 ? 8 : 4,
-                  ld1, ld2, nz, bx, by);
-}
 // 2-D tiled map over one (w x ld2) slice, box (bx, by)
 bool encode2t(CUtensorMap *m, void *base, CUtensorMapDataType dt, size_t es, int w, int ld2, int bx, int by) {
   EncodeTiledFn fn = encode_fn();
@@ -234,42 +218,19 @@ bool encode2t(CUtensorMap *m, void *base, CUtensorMapDataType dt, size_t es, int
 int encode_strip_maps(hyc_ens *e) {
   const int bx = hyc::kCol2Box, by = hyc::kCol2Rows;
   const CUtensorMapDataType F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32, F64 = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
-  std::vector<CUtensorMap> h(e->b.size() * 9);
+  std::vector<CUtensorMap> h(e->b.size() * kMaps);
   for (size_t i = 0; i < e->b.size(); i++) {
     EBasin &b = e->b[i];
-    CUtensorMap *m = &h[i * 9];
+    CUtensorMap *m = &h[i * kMaps];
     bool ok = true;
     for (int l = 0; l < 3; l++) ok &= encode3t(m + l, b.lev[l], F32, 4, b.ld1, b.ld2, (long long)b.ntr * b.kdm, bx, by);
     ok &= encode3t(m + 3, b.uflx, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
     ok &= encode3t(m + 4, b.vflx, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
     ok &= encode3t(m + 5, b.dp, F64, 8, b.ld1, b.ld2, b.kdm, bx, by);
-    ok &= encode2t(m + 6, b.geo4, F32, 4, 4 * b.ld1, b.ld2, 4 * bx, by);
-    ok &= encode2t(m + 7, b.dtsi, F64, 8, b.ld1, b.ld2, bx, by);
-    ok &= encode3t(m + 8, b.dp32, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
+    ok &= encode2t(m + 6, b.cell, F64, 8, b.ld1, b.ld2, bx, by);
     if (!ok) return efail(e, HYC_ERR_CUDA, "cuTensorMapEncodeTiled failed for the strip maps (basin %zu)", i);
   }
   ECK(cudaMemcpy(e->d_cmaps, h.data(), h.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "strip maps copy");
-  return HYC_OK;
-}
-
-int encode_maps(hyc_ens *e) {
-  if (e->tm_tx == e->shape.tx && e->tm_ty == e->shape.ty) return HYC_OK;
-  ECK(cudaStreamSynchronize(e->stream), "maps sync");
-  const int bx = hyc::tma_box_x(e->shape), by = hyc::tma_box_y(e->shape);
-  std::vector<CUtensorMap> h(e->b.size() * 6);
-  for (size_t i = 0; i < e->b.size(); i++) {
-    EBasin &b = e->b[i];
-    bool ok = true;
-    for (int l = 0; l < 3; l++)
-      ok &= encode3(&h[i * 6 + l], b.lev[l], false, b.ld1, b.ld2, (long long)b.ntr * b.kdm, bx, by);
-    ok &= encode3(&h[i * 6 + 3], b.uflx, false, b.ld1, b.ld2, b.kdm, bx, by);
-    ok &= encode3(&h[i * 6 + 4], b.vflx, false, b.ld1, b.ld2, b.kdm, bx, by);
-    ok &= encode3(&h[i * 6 + 5], b.dp, true, b.ld1, b.ld2, b.kdm, bx, by);
-    if (!ok) return efail(e, HYC_ERR_CUDA, "cuTensorMapEncodeTiled failed (basin %zu)", i);
-  }
-  ECK(cudaMemcpy(e->d_tmaps, h.data(), h.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "maps copy");
-  e->tm_tx = e->shape.tx;
-  e->tm_ty = e->shape.ty;
   return HYC_OK;
 }
 
@@ -295,12 +256,7 @@ int build_tables(hyc_ens *e, double dt2) {
   ECK(cudaStreamSynchronize(e->stream), "tables sync");  // earlier steps may still read the tables
   const int nb = (int)e->b.size();
   if (e->prec == HYC_PREC_MIXED)
-    for (auto &b : e->b) {
-      if (!b.dsqs) ECK(cudaMalloc(&b.dsqs, b.slice * sizeof(float2)), "dsqs");
-      ECK(hyc::launch_dsqs(b.scp2, b.scp2i, dt2, b.slice, b.dsqs, e->stream), "dsqs");
-      if (b.dtsi) ECK(hyc::launch_dtsi(b.scp2i, dt2, b.slice, b.dtsi, e->stream), "dtsi");
-      if (b.geo4) ECK(hyc::launch_geo4(b.scp2, b.scp2i, b.msk, dt2, b.slice, b.geo4, e->stream), "geo4");
-    }
+    for (auto &b : e->b) ECK(hyc::launch_cell_words(b.scp2i, b.msk, dt2, b.slice, b.cell, e->stream), "cell words");
   for (int r = 0; r < 3; r++) {
     const int lo = r, lc = (r + 1) % 3, ln = (r + 2) % 3;
     if (e->prec == HYC_PREC_MIXED) {
@@ -315,43 +271,20 @@ int build_tables(hyc_ens *e, double dt2) {
         m.ld1 = b.ld1;
         m.ld2 = b.ld2;
         m.slice = b.slice;
-        m.ntx = (b.idm + e->shape.tx - 1) / e->shape.tx;
-        m.nty = (b.jdm + e->shape.ty - 1) / e->shape.ty;
         m.kdm = b.kdm;
         m.ntr = b.ntr;
         m.images = b.nreg == 1 ? std::min(5, b.nbdy) : 0;
-        m.dt2 = dt2;
-        m.msk = b.msk;
-        m.scp2 = b.scp2;
-        m.scp2i = b.scp2i;
-        m.uflx = (const float *)b.uflx;
-        m.vflx = (const float *)b.vflx;
-        m.dp = b.dp;
-        m.fold = (const float *)b.lev[lo];
-        m.fcur = (const float *)b.lev[lc];
         m.fnew = (float *)b.lev[ln];
         m.seg = e->shape.ty;
         m.kchunk = col2_kchunk(e, b);
         for (int q = 0; q < b.ntr && q < hyc::kMaxFields; q++) m.posdef[q] = (float)b.posdef[q];
-        m.dsqs = b.dsqs;
-        if (e->d_cmaps) {
-          const CUtensorMap *c = e->d_cmaps + i * 9;
-          m.c2_old = c + lo;
-          m.c2_cur = c + lc;
-          m.c2_u = c + 3;
-          m.c2_v = c + 4;
-          m.c2_dp = c + 5;
-          m.c2_ge = c + 6;
-          m.c2_si = c + 7;
-          m.c2_dp32 = c + 8;
-        }
-        if (e->d_tmaps) {
-          m.tm_old = e->d_tmaps + i * 6 + lo;
-          m.tm_cur = e->d_tmaps + i * 6 + lc;
-          m.tm_u = e->d_tmaps + i * 6 + 3;
-          m.tm_v = e->d_tmaps + i * 6 + 4;
-          m.tm_dp = e->d_tmaps + i * 6 + 5;
-        }
+        const CUtensorMap *c = e->d_cmaps + i * kMaps;
+        m.c2_old = c + lo;
+        m.c2_cur = c + lc;
+        m.c2_u = c + 3;
+        m.c2_v = c + 4;
+        m.c2_dp = c + 5;
+        m.c2_cg = c + 6;
       }
       ECK(cudaMemcpy(e->d_mix[r], t.data(), nb * sizeof(MixBasin), cudaMemcpyHostToDevice), "mix table");
     } else {
@@ -410,17 +343,15 @@ int build_items(hyc_ens *e) {
     const EBasin &b = e->b[i];
     const int ntx = (b.idm + e->shape.tx - 1) / e->shape.tx, nty = (b.jdm + e->shape.ty - 1) / e->shape.ty;
     if (is_col2(e->shape)) {  // (basin, 56-column strip, segment, chunk of layers), all tracers
+      // the layer chunks of a segment are queued together: the per-cell
+      // words of the segment's rows are then read from DRAM about once
+      // and from L2 by the other chunks
       const int nstrip = (b.nbdy + b.idm - 4 + hyc::kCol2Strip - 1) / hyc::kCol2Strip;
       const int kc = col2_kchunk(e, b), nkc = (b.kdm + kc - 1) / kc;
-      for (int kq = 0; kq < nkc; kq++)
-        for (int sg = 0; sg < nty; sg++)
+      for (int sg = 0; sg < nty; sg++)
+        for (int kq = 0; kq < nkc; kq++)
           for (int st = 0; st < nstrip; st++)
             w.push_back({(long long)(std::min(b.kdm, (kq + 1) * kc) - kq * kc) * b.ntr, make_int4(i, st, sg, kq)});
-      continue;
-    }
-    if (is_col(e->shape)) {  // (basin, strip, segment), all layers and tracers
-      for (int sg = 0; sg < nty; sg++)
-        for (int st = 0; st < ntx; st++) w.push_back({(long long)b.kdm * b.ntr, make_int4(i, st, sg, 0)});
       continue;
     }
     for (int t = 0; t < ntx * nty; t++) {
@@ -471,10 +402,9 @@ int prime(hyc_ens *e) {
 int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
   ECK(cudaMemsetAsync(e->d_head + h, 0, sizeof(int), st), "queue reset");
   cudaError_t c;
-  if (e->prec == HYC_PREC_MIXED && is_col2(e->shape))
+  if (e->prec == HYC_PREC_MIXED)
     c = hyc::launch_mix_col2(advtyp, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm,
-                             e->strip_nq == 3 ? (e->maxntr > 1 ? 3 : 1) : std::min(e->strip_nq, e->maxntr),
-                             e->prep64, e->d_err, st);
+                             std::min(e->strip_nq, e->maxntr), e->prep64, e->d_err, st);
   else if (e->prec != HYC_PREC_MIXED && (advtyp == 0 || advtyp == 1)) {
     // FP64 PCM/MPDATA: the plain form's tile kernel per basin, then the periodic halo
     c = cudaSuccess;
@@ -486,14 +416,6 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
                                std::min(5, b.nbdy), std::min(5, b.nbdy), b.nreg, st);
     }
   }
-  else if (e->prec == HYC_PREC_MIXED && is_col(e->shape))
-    c = hyc::launch_mix_fct2_col(e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->maxntr, e->prep64,
-                                 e->shape.ty, st);
-  else if (e->prec == HYC_PREC_MIXED && e->use_tma)
-    c = hyc::launch_mix_fct2_tma(e->shape, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->prep64,
-                                 e->d_err, st);
-  else if (e->prec == HYC_PREC_MIXED)
-    c = hyc::launch_mix_fct2(e->shape, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm, e->prep64, st);
   else
     c = hyc::launch_fct_queue(advtyp, e->shape, e->d_targs[r], e->d_items, e->nitems, e->d_head + h, e->nsm, st);
   if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "step kernel: %s", cudaGetErrorString(c));
@@ -502,18 +424,15 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
 }
 
 // Schemes per form and kernel: FP64 FCT2/FCT4 (queue kernel) and PCM/MPDATA
-// (plain tile kernel); FP32-mixed FCT2 (every kernel), MPDATA and FCT4
-// (two-column strip kernel).
-bool scheme_ok(const hyc_ens *e, int advtyp, hyc::TileShape t) {
-  if (e->prec == HYC_PREC_MIXED) return advtyp == 2 || ((advtyp == 1 || advtyp == 4) && is_col2(t));
+// (plain tile kernel); FP32-mixed FCT2, FCT4 and MPDATA (strip kernel).
+bool scheme_ok(const hyc_ens *e, int advtyp) {
+  if (e->prec == HYC_PREC_MIXED) return advtyp == 1 || advtyp == 2 || advtyp == 4;
   return advtyp == 0 || advtyp == 1 || advtyp == 2 || advtyp == 4;
 }
 
 bool shape_ok(const hyc_ens *e, hyc::TileShape t) {
-  if (e->prec == HYC_PREC_MIXED && is_col2(t))
-    return e->d_cmaps && (t.ty == 32 || t.ty == 64 || t.ty == 128 || t.ty == 256 || t.ty == 512);
-  if (e->prec == HYC_PREC_MIXED && is_col(t)) return t.ty == 32 || t.ty == 64 || t.ty == 128;
-  if (e->prec == HYC_PREC_MIXED) return e->use_tma ? hyc::mix_tma_shape_ok(t) : hyc::mix_shape_ok(t);
+  if (e->prec == HYC_PREC_MIXED)
+    return is_col2(t) && (t.ty == 32 || t.ty == 64 || t.ty == 128 || t.ty == 256 || t.ty == 512);
   return (t.tx == 32 && t.ty == 16) || (t.tx == 16 && t.ty == 16);
 }
 
@@ -588,11 +507,7 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
               cudaMalloc(&b.vflx, b.slice * b.kdm * es) == cudaSuccess &&
               cudaMalloc(&b.dp, b.slice * b.kdm * 8) == cudaSuccess;
     for (int l = 0; l < 3 && ok; l++) ok = cudaMalloc(&b.lev[l], b.slice * b.kdm * b.ntr * es) == cudaSuccess;
-    if (ok && precision == HYC_PREC_MIXED)
-      ok = cudaMalloc(&b.dsqs, b.slice * sizeof(float2)) == cudaSuccess &&
-           cudaMalloc(&b.dtsi, b.slice * sizeof(double)) == cudaSuccess &&
-           cudaMalloc(&b.geo4, b.slice * sizeof(float4)) == cudaSuccess &&
-           cudaMalloc(&b.dp32, b.slice * b.kdm * sizeof(float)) == cudaSuccess;
+    if (ok && precision == HYC_PREC_MIXED) ok = cudaMalloc(&b.cell, b.slice * sizeof(double)) == cudaSuccess;
     e->b.push_back(b);
     if (!ok) return bail(efail(nullptr, HYC_ERR_NOMEM, "basin %d: device allocation failed", i));
     EBasin &bb = e->b.back();
@@ -601,8 +516,7 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
               cudaMemcpy(bb.scp2i, si.data(), bb.slice * 8, cudaMemcpyHostToDevice) == cudaSuccess &&
               cudaMemset(bb.uflx, 0, bb.slice * bb.kdm * es) == cudaSuccess &&
               cudaMemset(bb.vflx, 0, bb.slice * bb.kdm * es) == cudaSuccess &&
-              cudaMemset(bb.dp, 0, bb.slice * bb.kdm * 8) == cudaSuccess &&
-              (!bb.dp32 || cudaMemset(bb.dp32, 0, bb.slice * bb.kdm * 4) == cudaSuccess);
+              cudaMemset(bb.dp, 0, bb.slice * bb.kdm * 8) == cudaSuccess;
     for (int l = 0; l < 3 && cp; l++) cp = cudaMemset(bb.lev[l], 0, bb.slice * bb.kdm * bb.ntr * es) == cudaSuccess;
     if (!cp) return bail(efail(nullptr, HYC_ERR_CUDA, "basin %d: upload failed", i));
   }
@@ -616,20 +530,14 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
     return bail(efail(nullptr, HYC_ERR_NOMEM, "partials"));
   if (cudaMalloc(&e->d_err, sizeof(int)) != cudaSuccess || cudaMemset(e->d_err, 0, sizeof(int)) != cudaSuccess)
     return bail(efail(nullptr, HYC_ERR_NOMEM, "error flag"));
-  if (precision == HYC_PREC_MIXED) {
-    bool all6 = true;
-    for (auto &b : e->b) all6 &= b.nbdy == 6;
-    if (all6 && encode_fn() && cudaMalloc(&e->d_tmaps, nbasin * 6 * sizeof(CUtensorMap)) == cudaSuccess)
-      e->use_tma = true;
-    e->shape = hyc::TileShape{hyc::kColStrip, 64};  // column-strip kernel
-    if (encode_fn() && cudaMalloc(&e->d_cmaps, nbasin * 9 * sizeof(CUtensorMap)) == cudaSuccess) {
-      if (encode_strip_maps(e) == HYC_OK) {
-        e->shape = hyc::TileShape{hyc::kCol2Strip, 128};  // two-column strip kernel
-      } else {
-        cudaFree(e->d_cmaps);
-        e->d_cmaps = nullptr;
-      }
-    }
+  if (precision == HYC_PREC_MIXED) {  // the strip kernel streams its rows by TMA
+    if (!encode_fn())
+      return bail(efail(nullptr, HYC_ERR_UNSUPPORTED, "the mixed form needs cuTensorMapEncodeTiled (driver)"));
+    if (cudaMalloc(&e->d_cmaps, nbasin * kMaps * sizeof(CUtensorMap)) != cudaSuccess)
+      return bail(efail(nullptr, HYC_ERR_NOMEM, "strip maps"));
+    int rc = encode_strip_maps(e);
+    if (rc) return bail(rc);
+    e->shape = hyc::TileShape{hyc::kCol2Strip, 128};
   }
   *out = e;
   return HYC_OK;
@@ -768,9 +676,6 @@ static int move(hyc_ens *e, int32_t basin, int32_t what, int32_t s0, int32_t ns_
       if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put halo: %s", cudaGetErrorString(c));
     }
     c = hyc::launch_repitch(stage, 0, b.ld1r, rsl, dst, dfp32, b.ld1, b.slice, b.ld1r, b.ld2, ns, e->stream);
-    if (c == cudaSuccess && what == HYC_E_DP && b.dp32)  // the FP32 copy the strip kernel stages
-      c = hyc::launch_repitch(stage, 0, b.ld1r, rsl, b.dp32 + (size_t)s0 * b.slice, 1, b.ld1, b.slice, b.ld1r, b.ld2,
-                              ns, e->stream);
     if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "put: %s", cudaGetErrorString(c));
     span_close(e, t1, HYC_T_XCTILR, e->stream);
     ECK(cudaEventRecord(e->ev_used[q], e->stream), "event");
@@ -881,28 +786,13 @@ int hyc_ens_set_option(hyc_ens *e, int32_t option, int32_t value) {
     return HYC_OK;
   }
   if (option == HYC_OPT_STRIP_TRACERS) {
-    if (e->prec != HYC_PREC_MIXED || value < 1 || value > 3)
-      return efail(e, HYC_ERR_ARG, "HYC_OPT_STRIP_TRACERS: 1, 2 or 3 (warp pairs), mixed form");
+    if (e->prec != HYC_PREC_MIXED || value < 1 || value > 2)
+      return efail(e, HYC_ERR_ARG, "HYC_OPT_STRIP_TRACERS: 1 or 2, mixed form");
     if (e->strip_nq != value && e->gexec) {
       cudaGraphExecDestroy(e->gexec);
       e->gexec = nullptr;
     }
     e->strip_nq = value;
-    return HYC_OK;
-  }
-  if (option == HYC_OPT_TMA) {
-    if (e->prec != HYC_PREC_MIXED || (value && !e->d_tmaps))
-      return efail(e, HYC_ERR_ARG, "HYC_OPT_TMA needs the mixed form with nbdy = 6");
-    if (e->use_tma != (value != 0)) {
-      e->use_tma = value != 0;
-      if (!is_strip(e->shape)) e->shape = hyc::TileShape{32, 16};
-      e->tbl_dt2 = -1.0;
-      e->items_tx = 0;
-      if (e->gexec) {
-        cudaGraphExecDestroy(e->gexec);
-        e->gexec = nullptr;
-      }
-    }
     return HYC_OK;
   }
   return efail(e, HYC_ERR_ARG, "unknown option %d", option);
@@ -928,7 +818,6 @@ int hyc_ens_get_option(hyc_ens *e, int32_t option, int32_t *value) {
   if (!e || !value) return efail(e, HYC_ERR_ARG, "null argument");
   switch (option) {
     case HYC_OPT_PREP64: *value = e->prep64; return HYC_OK;
-    case HYC_OPT_TMA: *value = e->use_tma; return HYC_OK;
     case HYC_OPT_STRIP_TRACERS: *value = e->strip_nq; return HYC_OK;
     default: return efail(e, HYC_ERR_ARG, "unknown option %d", option);
   }
@@ -967,11 +856,11 @@ int hyc_ens_stats(hyc_ens *e, hyc_stats *out, int32_t reset) {
 int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32_t use_graph) {
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   if (nsteps < 1) return efail(e, HYC_ERR_ARG, "nsteps < 1");
-  if (!scheme_ok(e, advtyp, e->shape))
-    return efail(e, HYC_ERR_UNSUPPORTED, "ensemble advtyp %d not available for this precision and tile", advtyp);
+  if (!scheme_ok(e, advtyp))
+    return efail(e, HYC_ERR_UNSUPPORTED, "ensemble advtyp %d not available for this precision", advtyp);
   Dev g(e->device);
   int rc;
-  if ((rc = build_items(e)) || (e->use_tma && !is_strip(e->shape) && (rc = encode_maps(e))) ||
+  if ((rc = build_items(e)) ||
       (rc = build_tables(e, delt1)) || (rc = ensure_heads(e, nsteps)) || (rc = prime(e)))
     return rc;
   cudaEvent_t a = nullptr, z = nullptr;
@@ -1035,9 +924,7 @@ int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32
 int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t *ty, double *ms_out) {
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
   Dev g(e->device);
-  static const hyc::TileShape cands[] = {{32, 16}, {64, 16}, {32, 32}, {64, 8}, {128, 8}, {16, 16}, {32, 8},
-                                         {26, 32}, {26, 64}, {26, 128}, {56, 32}, {56, 64}, {56, 128}, {56, 256},
-                                         {56, 512}};
+  static const hyc::TileShape cands[] = {{32, 16}, {16, 16}, {56, 32}, {56, 64}, {56, 128}, {56, 256}, {56, 512}};
   hyc::TileShape best = e->shape;
   float best_ms = 1e30f;
   const hyc::TileShape keep = e->shape;
@@ -1050,9 +937,7 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
   const int keep_nq = e->strip_nq;
   std::vector<std::pair<hyc::TileShape, int>> trials;
   for (const auto &c : cands) {
-    if (!shape_ok(e, c) || !scheme_ok(e, advtyp, c)) continue;
-    // (warp pairs, HYC_OPT_STRIP_TRACERS = 3, measured 15 % slower than two
-    // tracers per warp on every shape: not a trial)
+    if (!shape_ok(e, c) || !scheme_ok(e, advtyp)) continue;
     if (is_col2(c) && e->maxntr > 1) trials.push_back({c, 1});
     trials.push_back({c, 2});
   }
@@ -1061,7 +946,7 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
     e->strip_nq = tr.second;
     e->shape = c;
     e->tbl_dt2 = -1.0;
-    if ((rc = build_items(e)) || (e->use_tma && !is_strip(e->shape) && (rc = encode_maps(e))) ||
+    if ((rc = build_items(e)) ||
         (rc = build_tables(e, delt1)) || (rc = ensure_heads(e, 1)))
       break;
     // the step kernel writes only the spare level: the state is unchanged

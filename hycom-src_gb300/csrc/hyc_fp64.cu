@@ -135,6 +135,46 @@ cudaError_t launch_copy_back(const TileArgs &a, int nlayers, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
+// Isopycnic mixed-layer flux smoothing, mod_tsadvc.F90:1860-1897: at the
+// open faces within `margin` of the interior, half the layer-1 flux plus a
+// quarter of each along-face neighbour's (the face's own flux where that
+// neighbour face is closed); every other face of the two output slices is
+// 0, as the reference's uflux/vflux are zeroed on entry (:1812-1813)
+// ---------------------------------------------------------------------------
+__global__ void iso_smooth_kernel(const double *uk, const double *vk, const uint8_t *msk, long long slice, int ii,
+                                  int jj, int nb, int ld1, int margin, double *us, double *vs) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < slice;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int jr = (int)(t / ld1), ia = (int)(t - (long long)jr * ld1);
+    const int i = ia - nb + 1, j = jr - nb + 1;
+    double uo = 0.0, vo = 0.0;
+    if (i >= 1 - margin && i <= ii + margin && j >= 1 - margin && j <= jj + margin) {
+      const uint8_t m = msk[t];
+      if (m & kIV) {
+        const double vfa = (msk[t - 1] & kIV) ? vk[t - 1] : vk[t];
+        const double vfb = (msk[t + 1] & kIV) ? vk[t + 1] : vk[t];
+        vo = .5 * vk[t] + .25 * (vfa + vfb);
+      }
+      if (m & kIU) {
+        const double ufa = (msk[t - ld1] & kIU) ? uk[t - ld1] : uk[t];
+        const double ufb = (msk[t + ld1] & kIU) ? uk[t + ld1] : uk[t];
+        uo = .5 * uk[t] + .25 * (ufa + ufb);
+      }
+    }
+    us[t] = uo;
+    vs[t] = vo;
+  }
+}
+
+cudaError_t launch_iso_smooth(const double *uk, const double *vk, const uint8_t *msk, long long slice, int ii, int jj,
+                              int nb, int ld1, int margin, double *us, double *vs, cudaStream_t s) {
+  int bx = (int)((slice + 255) / 256);
+  if (bx > 2048) bx = 2048;
+  iso_smooth_kernel<<<bx, 256, 0, s>>>(uk, vk, msk, slice, ii, jj, nb, ld1, margin, us, vs);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // xctilr, mod_xc_sm.h:1337-1428.  Every halo cell is computed directly from
 // interior cells (the reference's N/S pass followed by the E/W pass over
 // rows 1-nhl..jj+nhl gives the same values), so one launch has no ordering

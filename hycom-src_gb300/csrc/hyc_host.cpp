@@ -12,6 +12,25 @@
 #include <vector>
 
 #include "../../include/hycom_adv.h"
+
+#include <cstddef>
+
+// The parameter blocks are passed by reference from Fortran as bind(c)
+// derived types (ten int32 flags then delt1 and the trcflg pointer; four
+// int32 then delt1 and ra2fac; an int64, eight int64 counts, eight doubles):
+// their C layout must be exactly the one those types get.
+static_assert(sizeof(int32_t) == 4 && sizeof(double) == 8 && sizeof(void *) == 8, "LP64 ABI");
+static_assert(offsetof(hyc_tsadvc_params, advtyp) == 0 && offsetof(hyc_tsadvc_params, diagno) == 36 &&
+                  offsetof(hyc_tsadvc_params, delt1) == 40 && offsetof(hyc_tsadvc_params, trcflg) == 48 &&
+                  sizeof(hyc_tsadvc_params) == 56,
+              "hyc_tsadvc_params must match its bind(c) type");
+static_assert(offsetof(hyc_cnuity_params, nstep) == 0 && offsetof(hyc_cnuity_params, isopyc) == 12 &&
+                  offsetof(hyc_cnuity_params, delt1) == 16 && offsetof(hyc_cnuity_params, ra2fac) == 24 &&
+                  sizeof(hyc_cnuity_params) == 32,
+              "hyc_cnuity_params must match its bind(c) type");
+static_assert(offsetof(hyc_stats, calls) == 8 && offsetof(hyc_stats, ms) == 8 + 8 * HYC_NTIMERS &&
+                  sizeof(hyc_stats) == 8 + 16 * HYC_NTIMERS,
+              "hyc_stats must match its bind(c) type");
 #include "hyc_internal.h"
 #include "hyc_args.h"
 
@@ -46,6 +65,7 @@ struct hyc_ctx {
   long long *d_cnkeys = nullptr;  // cnuity dpkmin keys (2*kdm)
   Field fields[HYC_NFIELDS];
   double *d_scratch = nullptr;  // advem output slices (fields x layers)
+  double *d_iso = nullptr;      // smoothed layer-1 fluxes of isopycnic mode (2 slices)
   size_t scratch_elems = 0;
   unsigned char *d_fct2c = nullptr;  // advem_fct2c work arrays (per (field, layer) pair)
   size_t fct2c_bytes = 0;
@@ -411,6 +431,7 @@ int hyc_adv_finalize(hyc_ctx *c) {
     cudaFree(c->d_cnw);
     cudaFree(c->d_cnkeys);
     cudaFree(c->d_scratch);
+    cudaFree(c->d_iso);
     cudaFree(c->d_fct2c);
     cudaFree(c->d_tmp);
     cudaFree(c->d_keys);
@@ -618,7 +639,10 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
   if (!valid_advtyp(at)) return fail(c, HYC_ERR_ADVTYP, "advem called with advtyp = %d", p->advtyp);
   if (c->nbdy < kMbdy[at])
     return fail(c, HYC_ERR_NBDY, "nbdy (dimensions.h) must be at least %d for advtyp %d", kMbdy[at], at);
-  if (p->isopyc) return fail(c, HYC_ERR_UNSUPPORTED, "isopycnic (nhybrd=0) mode is not supported");
+  if (p->isopyc && (p->nhybrd != 0 || p->hybrid))
+    return fail(c, HYC_ERR_ARG, "isopycnic mode is nhybrd = 0 (no hybrid layers)");
+  if (p->isopyc && at == 2 && p->btrmas)
+    return fail(c, HYC_ERR_UNSUPPORTED, "isopycnic flux smoothing with advem_fct2c (btrmas) is not supported");
   if (p->ntracr < 0 || (p->ntracr > 0 && !p->trcflg)) return fail(c, HYC_ERR_ARG, "ntracr/trcflg");
   const int kk = c->kdm;
   const long long sl = c->slice;
@@ -637,7 +661,7 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
   if ((rc = need(HYC_F_VFLX, (long long)kk * sl, "vflx"))) return rc;
   if ((rc = need(HYC_F_DP, 2LL * kk * sl, "dp"))) return rc;
   if (use_temp && (rc = need(HYC_F_TEMP, 2LL * kk * sl, "temp"))) return rc;
-  if (use_th3d && (rc = need(HYC_F_TH3D, 2LL * kk * sl, "th3d"))) return rc;
+  if ((use_th3d || p->isopyc) && (rc = need(HYC_F_TH3D, 2LL * kk * sl, "th3d"))) return rc;
   if (p->ntracr > 0 && (rc = need(HYC_F_TRACER, 2LL * kk * sl * p->ntracr, "tracer"))) return rc;
   if (p->mxlmy && ((rc = need(HYC_F_Q2, 2LL * (kk + 2) * sl, "q2")) || (rc = need(HYC_F_Q2L, 2LL * (kk + 2) * sl, "q2l"))))
     return rc;
@@ -689,9 +713,22 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
   };
   const double pdzero = 0.0, pdtemp = 256.0, pdth3d = 32.0, pdq2 = 1.0;  // :1761-1763
   const int nh = p->nhybrd < kk ? p->nhybrd : kk;
+  // isopycnic mode (:1855-1859, :1983-1991): layer 1 advects th3d and saln
+  // with the smoothed fluxes; the tracers (and q2, q2l) of layer 1 keep
+  // the layer's own fluxes but share its thickness factors, which come
+  // from the smoothed ones; deeper layers advect saln (and the tracers)
+  // only.  iso1 = fields of layer 1 advected by the smoothed fluxes,
+  // isot = the rest of layer 1; fl = every field of layers >= 2.
+  std::vector<FieldDesc> iso1, isot;
+  const int k1 = p->isopyc ? 2 : 1;  // first layer of the general launch
   if (use_temp) add(F[HYC_F_TEMP].dev, (long long)kk * sl, 0, 1, nh, pdtemp);
   if (use_th3d) add(F[HYC_F_TH3D].dev, (long long)kk * sl, 0, 1, nh, pdth3d);
-  add(F[HYC_F_SALN].dev, (long long)kk * sl, 0, 1, kk, pdzero);
+  if (p->isopyc) {
+    add(F[HYC_F_TH3D].dev, (long long)kk * sl, 0, 1, 1, pdth3d);
+    add(F[HYC_F_SALN].dev, (long long)kk * sl, 0, 1, 1, pdzero);
+    iso1.swap(fl);
+  }
+  add(F[HYC_F_SALN].dev, (long long)kk * sl, 0, k1, kk, pdzero);
   for (int t = 0; t < p->ntracr; t++)
     add(F[HYC_F_TRACER].dev + (long long)t * 2 * kk * sl, (long long)kk * sl, 0, 1, kk,
         p->trcflg[t] == 2 ? pdtemp : pdzero);
@@ -699,6 +736,14 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
     add(F[HYC_F_Q2].dev, (long long)(kk + 2) * sl, 1, 1, kk, pdq2);
     add(F[HYC_F_Q2L].dev, (long long)(kk + 2) * sl, 1, 1, kk, pdq2);
   }
+  if (p->isopyc)  // split the tracers (and q2, q2l) at layer 1
+    for (auto &d : fl)
+      if (d.kmin == 1) {
+        FieldDesc e = d;
+        e.kmax = 1;
+        isot.push_back(e);
+        d.kmin = 2;
+      }
 
   TileArgs a;
   memset(&a, 0, sizeof a);
@@ -764,23 +809,47 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
     fl.clear();  // done: no tile launches below
   }
   const int chunk = hyc::kMaxFields;
-  const int nchunk0 = (int)fl.size() < chunk ? (int)fl.size() : chunk;
-  if (!fl.empty() && (rc = ensure_scratch(c, (size_t)nchunk0 * kk * sl))) return rc;
+  const size_t most = std::max(fl.size(), std::max(iso1.size(), isot.size()));
+  const int nchunk0 = (int)most < chunk ? (int)most : chunk;
+  if (most > 0 && (rc = ensure_scratch(c, (size_t)nchunk0 * kk * sl))) return rc;
   a.out = c->d_scratch;
-  for (size_t f0 = 0; f0 < fl.size(); f0 += chunk) {
-    int nf = (int)(fl.size() - f0) < chunk ? (int)(fl.size() - f0) : chunk;
-    a.nfld = nf;
-    for (int q = 0; q < nf; q++) a.f[q] = fl[f0 + q];
-    {
-      Timed t(c, HYC_T_ADVECT);
-      CK(hyc::launch_advect_tiles(at, a, kk, c->shape, s), "advect kernel");
+  // one group of fields over layers 1..nlay: tile kernel into the scratch, then back into level n
+  auto run = [&](const std::vector<FieldDesc> &grp, int nlay) -> int {
+    for (size_t f0 = 0; f0 < grp.size(); f0 += chunk) {
+      int nf = (int)(grp.size() - f0) < chunk ? (int)(grp.size() - f0) : chunk;
+      a.nfld = nf;
+      for (int q = 0; q < nf; q++) a.f[q] = grp[f0 + q];
+      {
+        Timed t(c, HYC_T_ADVECT);
+        CK(hyc::launch_advect_tiles(at, a, nlay, c->shape, s), "advect kernel");
+      }
+      {
+        Timed t(c, HYC_T_COPY);
+        CK(hyc::launch_copy_back(a, nlay, s), "copy back");
+      }
+      c->stats.launches += 2;
     }
-    {
-      Timed t(c, HYC_T_COPY);
-      CK(hyc::launch_copy_back(a, kk, s), "copy back");
-    }
-    c->stats.launches += 2;
+    return HYC_OK;
+  };
+  if (p->isopyc && (!iso1.empty() || !isot.empty())) {  // layer 1, :1860-1897
+    if (!c->d_iso) CK(cudaMalloc(&c->d_iso, 2 * sl * sizeof(double)), "malloc isopycnic fluxes");
+    double *us = c->d_iso, *vs = c->d_iso + sl;
+    CK(hyc::launch_iso_smooth(F[HYC_F_UFLX].dev, F[HYC_F_VFLX].dev, c->d_msk, sl, c->idm, c->jdm, c->nbdy, c->ld1,
+                              kMbdy[at] - 1, us, vs, s),
+       "isopycnic smoothing");
+    c->stats.launches += 1;
+    a.uflx = us;  // layer 1 of the launch reads uflx + 0*slice
+    a.vflx = vs;
+    if ((rc = run(iso1, 1))) return rc;
+    a.uflx = F[HYC_F_UFLX].dev;
+    a.vflx = F[HYC_F_VFLX].dev;
+    a.ufco = us;
+    a.vfco = vs;
+    if ((rc = run(isot, 1))) return rc;
+    a.ufco = nullptr;
+    a.vfco = nullptr;
   }
+  if ((rc = run(fl, kk))) return rc;
 
   // salinity range diagnostic, mod_tsadvc.F90:2065-2084
   if (xmin && xmax && (p->nstep % 3 == 0 || p->diagno)) {

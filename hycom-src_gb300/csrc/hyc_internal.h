@@ -46,6 +46,11 @@ size_t cnuity_work_slices();
 cudaError_t launch_cnuity_layers(const CnuityArgs &a, int *launches, cudaStream_t s);
 cudaError_t launch_cnuity_rest(const CnuityArgs &a, int *launches, cudaStream_t s);
 
+// Isopycnic smoothing of the layer-1 fluxes (mod_tsadvc.F90:1860-1897) into
+// us/vs (whole slices, 0 off the smoothed faces).
+cudaError_t launch_iso_smooth(const double *uk, const double *vk, const uint8_t *msk, long long slice, int ii, int jj,
+                              int nb, int ld1, int margin, double *us, double *vs, cudaStream_t s);
+
 // xctilr on nlev slices (mod_xc_sm.h:1337-1428).
 cudaError_t launch_xctilr(double *a, long long slice, int nlev, int ii, int jj, int nbdy, int ld1, int mh,
                           int nh, int nreg, cudaStream_t s);

@@ -9,25 +9,33 @@
 //
 // Memory: lane 0 of each warp keeps kNS blocks of kRB rows in flight.  A
 // block holds, per row, the old and centre levels of the pass's tracers,
-// uflx, vflx (FP32), dp (FP64), the per-cell factors (dt2*scp2i, scp2/dt2
-// with 0 marking land, iu, iv as FP32) and, with the FP64 thickness prep,
-// dt2*scp2i in FP64 -- one cp.async.bulk.tensor per array, one mbarrier per slot.
-// Out-of-range rows and columns arrive as zeros (TMA fill), so the kernel
-// has no bounds tests on loads.
+// uflx, vflx (FP32), dp (FP64) and the per-cell word (dt2*scp2i in FP64
+// with ip, iu, iv in its three lowest mantissa bits) -- one
+// cp.async.bulk.tensor per array, one mbarrier per slot.  The streams are
+// loaded with an L2 evict-first policy, so the per-cell words, which every
+// layer of a strip reads again, stay in L2.  Out-of-range rows and columns
+// arrive as zeros (TMA fill), so the kernel has no bounds tests on loads.
 //
-// Compute: the stage pipeline of mod_tsadvc.F90:645-997 runs in registers
-// as in hyc_mixed_col.cu -- at row J the lane forms the low-order fluxes of
-// row J (:686-720), the low-order solution and antidiffusive fluxes of row
-// J-1 (:778-855), the Zalesak ratios and limited fluxes of row J-2
-// (:863-946) and the update of row J-3 (:962-982).  With two columns per
-// lane, one shuffle moves a value across the lane boundary for both
-// columns, and adds, multiplies and FMAs run as packed FP32x2 operations.
-// The flux divergences use two-sum compensation.  The thickness factors
-// W = (fco+onemu)/(fcn+onemu), R = 1/(fcn+onemu), QF = fcn*scp2/dt2 of
-// mod_tsadvc.F90:1905-1942 are formed once per cell and layer, in FP64
-// (PREP64: the thickness update, the reciprocal by one Newton step from an
-// FP32 seed and W; the face-flux differences by two-sum in FP32) or in
-// compensated FP32.
+// Compute: the stage pipeline of mod_tsadvc.F90:645-997 runs in registers --
+// at row J the lane forms the low-order fluxes of row J (:686-720), the
+// low-order solution and antidiffusive fluxes of row J-1 (:778-855), the
+// Zalesak ratios and limited fluxes of row J-2 (:863-946) and the update of
+// row J-3 (:962-982).  With two columns per lane, one shuffle moves a value
+// across the lane boundary for both columns, and adds, multiplies and FMAs
+// run as packed FP32x2 operations.  The flux divergences use two-sum
+// compensation.
+//
+// Thickness factors of mod_tsadvc.F90:1905-1942, once per cell and layer
+// and shared by the pass's tracers:  W = (fco+onemu)/(fcn+onemu),
+// R = 1/(fcn+onemu), QF = fcn*scp2/dt2.  PREP64 (the precision form): the
+// continuity update fco+onemu = (dp+onemu) + div*dt2*scp2i (one FP64 FMA),
+// fcn+onemu (one FP64 add), the reciprocal R (hardware FP64 seed, one
+// Newton step: two FP64 FMAs, relative error < 2^-40) and W = (fco+onemu)*R
+// (one FP64 multiply) are FP64 -- five FP64-pipe operations per cell and
+// layer (MPDATA, which also needs W-1 without cancellation: seven).  The
+// conversions between FP32 and FP64 run on the integer pipes: on GB300 an
+// F2F conversion issues on the FP64 pipe, at about 1/60 of the FP32 rate.
+// Without PREP64 the factors are formed in compensated FP32.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -48,18 +56,18 @@ constexpr int kNS = 2;      // ring slots per warp
 constexpr int kWarps = 4;   // warps per CTA
 constexpr unsigned kFull = 0xffffffffu;
 
-template <int SCHEME, int NQ, bool PREP64>
+template <int SCHEME, int NQ>
 struct Ring {
   static constexpr int NC = SCHEME == kMPDATA ? 0 : NQ;  // centre-level rows (leapfrog schemes)
   static constexpr int FROW = kW * 4;  // one FP32 row
+  static constexpr int DROW = kW * 8;  // one FP64 row
   static constexpr int OFF_FO = 0;
   static constexpr int OFF_FC = OFF_FO + NQ * kRB * FROW;
   static constexpr int OFF_U = OFF_FC + NC * kRB * FROW;
   static constexpr int OFF_V = OFF_U + kRB * FROW;
-  static constexpr int OFF_DP = OFF_V + kRB * FROW;        // dp: double (PREP64) or float per cell
-  static constexpr int OFF_GE = OFF_DP + kRB * kW * (PREP64 ? 8 : 4);  // float4 per cell
-  static constexpr int OFF_SI = OFF_GE + kRB * kW * 16;    // double per cell (PREP64)
-  static constexpr int TX_BYTES = OFF_SI + (PREP64 ? kRB * kW * 8 : 0);
+  static constexpr int OFF_DP = OFF_V + kRB * FROW;   // dp, FP64
+  static constexpr int OFF_CG = OFF_DP + kRB * DROW;  // per-cell word, FP64
+  static constexpr int TX_BYTES = OFF_CG + kRB * DROW;
   static constexpr int SLOT = (TX_BYTES + 127) / 128 * 128;
   static constexpr int WARP = kNS * SLOT;
   static constexpr size_t SMEM = (size_t)kWarps * WARP + kWarps * kNS * 8 + 128;
@@ -92,6 +100,45 @@ __device__ __forceinline__ float rcp_approx(float x) {
   float r;
   asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
+}
+// hardware FP64 reciprocal seed (multi-function unit; about 9x the FP64 FMA rate here)
+__device__ __forceinline__ double rcp_seed64(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  return r;
+}
+// FP32 -> FP64 on the integer pipes: exact for normal values, +-0 for zeros
+// and denormals.  The exponent is rebased by 1023-127 and the mantissa
+// widened; the sign stays in bit 31 of the high word.
+__device__ __forceinline__ double f2d_i(float f) {
+  const unsigned b = __float_as_uint(f);
+  unsigned hi = ((unsigned)((int)b >> 3) & 0x8FFFFFFFu) + 0x38000000u;
+  unsigned lo = b << 29;
+  if ((b & 0x7F800000u) == 0u) {
+    hi = b & 0x80000000u;
+    lo = 0u;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+// FP64 -> FP32 on the integer pipes for positive values in the FP32 normal
+// range, rounded to nearest (ties away from zero): the top 32 bits after
+// dropping the sign and the two high exponent bits, exponent rebased by
+// 1023-127 (mod 2^32), plus the first dropped bit
+__device__ __forceinline__ float d2f_pos(double x) {
+  const unsigned lo = (unsigned)__double2loint(x), hi = (unsigned)__double2hiint(x);
+  return __uint_as_float(__funnelshift_l(lo, hi, 3) + 0x40000000u + ((lo >> 28) & 1u));
+}
+// as d2f_pos for either sign; magnitudes below the FP32 normal range give +-0
+__device__ __forceinline__ float d2f_i(double x) {
+  const unsigned lo = (unsigned)__double2loint(x), hi = (unsigned)__double2hiint(x);
+  const unsigned t = __funnelshift_l(lo, hi, 3) + 0x40000000u + ((lo >> 28) & 1u);
+  const unsigned m = ((hi >> 20) & 0x7FFu) > 0x380u ? (t & 0x7FFFFFFFu) : 0u;
+  return __uint_as_float(m | (hi & 0x80000000u));
+}
+// 1/h: hardware seed and one Newton step in FP64 (h >= onemu > 0)
+__device__ __forceinline__ double rcp64(double h) {
+  const double r = rcp_seed64(h);
+  return __fma_rn(r, __fma_rn(-h, r, 1.0), r);
 }
 // ((a - b) + (c - d)) with the rounding errors of the two differences added
 // back (two-sum), both columns at once
@@ -151,77 +198,35 @@ constexpr bool kLateStore = true;
 
 }  // namespace
 
-// PAIR: two warps share one ring and one item, each advancing one of the
-// pass's two tracers (one tracer of pipeline state per warp: fewer
-// registers, 3 CTAs and 12 warps per SM instead of 8, the inputs of a row
-// still read once).  The even warp takes items from the queue and hands
-// them to its partner through a shared-memory mailbox (mbarriers ibar /
-// tbar), issues the TMA blocks, and refills a slot only after both warps
-// have released it (mbarrier empty, two arrivals).  Every wait is bounded.
-template <int SCHEME, int NQ, bool PREP64, bool PAIR>
-struct Col2Geom {
-  static constexpr int NI = PAIR ? 2 : NQ;  // tracers in the ring per pass
-  using RG = Ring<SCHEME, NI, PREP64>;
-  static constexpr int NRING = PAIR ? kWarps / 2 : kWarps;
-  static constexpr int NBAR = PAIR ? 2 * kNS + 3 : kNS;  // full[kNS], empty[kNS], ibar, tbar, mailbox
-  static constexpr size_t SMEM = (size_t)NRING * RG::WARP + (size_t)NRING * NBAR * 8 + 128;
-};
-
-template <int SCHEME, int NQ, bool PREP64, bool PAIR = false>
-__global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
+template <int SCHEME, int NQ, bool PREP64>
+__global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     mix_col2_kernel(const MixBasin *__restrict__ basins, const int4 *__restrict__ items, int nitems, int *head,
                     int *err) {
-  static_assert(!PAIR || NQ == 1, "a warp of a pair advances one tracer");
-  using GE = Col2Geom<SCHEME, NQ, PREP64, PAIR>;
-  using RG = typename GE::RG;
-  constexpr int NI = GE::NI;
+  using RG = Ring<SCHEME, NQ>;
   constexpr bool MP = SCHEME == kMPDATA;
   constexpr bool F4 = SCHEME == kFCT4;
   using St = typename std::conditional<MP, StM, St2>::type;
   extern __shared__ unsigned char c2raw_[];
   unsigned char *sm = (unsigned char *)(((uintptr_t)c2raw_ + 127) & ~(uintptr_t)127);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int owner = PAIR ? (wid >> 1) : wid, sub = PAIR ? (wid & 1) : 0;
-  const bool lead = !PAIR || sub == 0;  // takes items and issues the copies
-  unsigned char *ring = sm + owner * RG::WARP;
-  uint64_t *bar = (uint64_t *)(sm + GE::NRING * RG::WARP) + owner * GE::NBAR;  // full[kNS]
-  uint64_t *empty = bar + kNS, *ibar = bar + 2 * kNS, *tbar = ibar + 1;
-  int *mailbox = (int *)(tbar + 1);
-  if (lead && lane == 0) {
+  unsigned char *ring = sm + wid * RG::WARP;
+  uint64_t *bar = (uint64_t *)(sm + kWarps * RG::WARP) + wid * kNS;  // full[kNS]
+  if (lane == 0) {
     for (int s = 0; s < kNS; s++) tma::bar_init(bar + s, 1);
-    if (PAIR) {
-      for (int s = 0; s < kNS; s++) tma::bar_init(empty + s, 2);
-      tma::bar_init(ibar, 1);
-      tma::bar_init(tbar, 1);
-    }
     tma::fence_bar_init();
   }
-  if (PAIR)
-    __syncthreads();  // the partner warps use the barriers their lead initialised
-  else
-    __syncwarp();
+  __syncwarp();
+  // L2 policies: the streams are read once per item (evict first), the
+  // per-cell words by every layer chunk of the strip (default)
+  const uint64_t pol_stream = tma::policy_evict_first();
   uint32_t tg = 0;  // blocks this warp has consumed (slot and phase of the next one)
-  uint32_t ni = 0;  // items handed over within the pair
   const float onemu = (float)kOnemu;
+  const float2 onemu2 = make_float2(onemu, onemu);
 
   for (;;) {
     int it = 0;
-    if (!PAIR) {
-      if (lane == 0) it = atomicAdd(head, 1);
-    } else if (lane == 0) {
-      if (lead) {
-        // the partner has read the previous item before the mailbox is reused
-        const bool okx = ni == 0 || tma::wait(tbar, (ni - 1) & 1u, err);
-        it = okx ? atomicAdd(head, 1) : nitems;
-        *(volatile int *)mailbox = it;
-        tma::arrive(ibar);
-      } else {
-        it = tma::wait(ibar, ni & 1u, err) ? *(volatile int *)mailbox : nitems;
-        tma::arrive(tbar);
-      }
-    }
+    if (lane == 0) it = atomicAdd(head, 1);
     it = __shfl_sync(kFull, it, 0);
-    ni++;
     if (it >= nitems) break;
     const int4 w = items[it];
     const MixBasin &B = basins[w.x];
@@ -231,7 +236,7 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
     const int s0 = 56 * w.y;  // strip start (padded column)
     const int j0 = 1 + w.z * B.seg, j1 = min(j0 + B.seg, jj + 1);
     const int nblk = (j1 - j0 + 6 + kRB - 1) / kRB;
-    const int nqp = (ntr + NI - 1) / NI;
+    const int nqp = (ntr + NQ - 1) / NQ;
     const int ka = w.w * B.kchunk, kb = min(kdm, ka + B.kchunk);  // this item's layers
     const int T = (kb - ka) * nqp * nblk;
     // this lane's columns: padded a0 = s0 + 2*lane (A) and a0 + 1 (B)
@@ -240,49 +245,36 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
     const bool outA = lane >= 2 && lane < 30 && iA >= 1 && iA <= ii;
     const bool outB = lane >= 2 && lane < 30 && iB >= 1 && iB <= ii;
 
-    auto issue = [&](int t) -> bool {  // lane 0 of the lead: block t of this item into its slot
+    auto issue = [&](int t) {  // lane 0: block t of this item into its slot
       const int kk = t / (nqp * nblk);
       const int rem = t - kk * nqp * nblk;
       const int k = ka + kk;
       const int qp = rem / nblk, blk = rem - qp * nblk;
       const int y = j0 - 3 + blk * kRB + nb - 1;
       const uint32_t g = tg + t;
-      // PAIR: both warps have released the slot's previous block
-      if (PAIR && g >= (uint32_t)kNS && !tma::wait(empty + (g % kNS), ((g / kNS) - 1) & 1u, err)) return false;
       unsigned char *slot = ring + (g % kNS) * RG::SLOT;
       uint64_t *b = bar + (g % kNS);
       tma::expect_tx(b, RG::TX_BYTES);
 #pragma unroll
-      for (int q = 0; q < NI; q++) {
-        const int qq = min(qp * NI + q, ntr - 1);
-        tma::load3(slot + RG::OFF_FO + q * kRB * RG::FROW, B.c2_old, b, s0, y, qq * kdm + k);
-        if (!MP) tma::load3(slot + RG::OFF_FC + q * kRB * RG::FROW, B.c2_cur, b, s0, y, qq * kdm + k);
+      for (int q = 0; q < NQ; q++) {
+        const int qq = min(qp * NQ + q, ntr - 1);
+        tma::load3h(slot + RG::OFF_FO + q * kRB * RG::FROW, B.c2_old, b, s0, y, qq * kdm + k, pol_stream);
+        if (!MP) tma::load3h(slot + RG::OFF_FC + q * kRB * RG::FROW, B.c2_cur, b, s0, y, qq * kdm + k, pol_stream);
       }
-      tma::load3(slot + RG::OFF_U, B.c2_u, b, s0, y, k);
-      tma::load3(slot + RG::OFF_V, B.c2_v, b, s0, y, k);
-      tma::load3(slot + RG::OFF_DP, PREP64 ? B.c2_dp : B.c2_dp32, b, s0, y, k);
-      tma::load2(slot + RG::OFF_GE, B.c2_ge, b, 4 * s0, y);
-      if (PREP64) tma::load2(slot + RG::OFF_SI, B.c2_si, b, s0, y);
-      return true;
+      tma::load3h(slot + RG::OFF_U, B.c2_u, b, s0, y, k, pol_stream);
+      tma::load3h(slot + RG::OFF_V, B.c2_v, b, s0, y, k, pol_stream);
+      tma::load3h(slot + RG::OFF_DP, B.c2_dp, b, s0, y, k, pol_stream);
+      tma::load2(slot + RG::OFF_CG, B.c2_cg, b, s0, y);
     };
-    int nissued = 0;  // lead lane 0: blocks of this item in flight
-    if (lead && lane == 0)
-      while (nissued < kNS && nissued < T && issue(nissued)) nissued++;
-    const bool short_issue = lead && nissued < kNS && nissued < T;  // meaningful on lane 0 only
-    if (__shfl_sync(kFull, short_issue ? 1 : 0, 0) != 0) {
-      // PAIR: the partner stopped releasing slots; let the copies in flight land, then stop
-      if (lead && lane == 0)
-        for (int d = 0; d < nissued; d++) tma::wait(bar + ((tg + d) % kNS), ((tg + d) / kNS) & 1u, nullptr);
-      return;
-    }
+    if (lane == 0)
+      for (int d = 0; d < kNS && d < T; d++) issue(d);
 
     int t = 0;
     bool ok = true;
     for (int k = ka; k < kb && ok; k++) {
       for (int qp = 0; qp < nqp && ok; qp++) {
-        // this warp's tracers of the pass: qp*NQ + q, or (PAIR) the partner's slot sub
-        const int qb = PAIR ? qp * 2 + sub : qp * NQ;
-        const int nq = PAIR ? (qb < ntr ? 1 : 0) : min(NQ, ntr - qp * NQ);
+        const int qb = qp * NQ;  // this pass's tracers: qb .. qb+nq-1
+        const int nq = min(NQ, ntr - qb);
         float *fn[NQ];
 #pragma unroll
         for (int q = 0; q < NQ; q++) fn[q] = fnew + ((long long)min(qb + (q < nq ? q : 0), ntr - 1) * kdm + k) * sl;
@@ -299,9 +291,8 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
         float2 IU1 = z2, IV1 = z2, IV2 = z2;  // FCT4: iu of row J-1, iv of rows J-1, J-2 (0/1)
         float2 L1 = z2, L2 = z2, L3 = z2;  // land flags (1 = land) of rows J-1, J-2, J-3
         float L2e = 0.f;                   // land flag east of column B, row J-2
-        using DT = typename std::conditional<PREP64, double, float>::type;
-        DT dA1 = 0, dB1 = 0;
-        double sA1 = 0.0, sB1 = 0.0;
+        double dA1 = 0.0, dB1 = 0.0;       // dp of row J-1
+        double sA1 = 0.0, sB1 = 0.0;       // dt2*scp2i of row J-1 (FP64 prep)
         for (int blk = 0; blk < nblk; blk++, t++) {
           const uint32_t g = tg + t;
           if (!__all_sync(kFull, tma::wait(bar + (g % kNS), (g / kNS) & 1u, err))) {
@@ -311,55 +302,55 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
             break;
           }
           const unsigned char *slot = ring + (g % kNS) * RG::SLOT;
-#pragma unroll(PREP64 ? 2 : kRB)  // measured: full unroll 1.8 % faster with the FP32 prep, 2.5 % slower with FP64
+#pragma unroll(PREP64 ? 2 : kRB)
           for (int rr = 0; rr < kRB; rr++) {
             const int J = j0 - 3 + blk * kRB + rr;
             // ---- inputs of row J
             const float2 u0 = ((const float2 *)(slot + RG::OFF_U + rr * RG::FROW))[lane];
             const float2 v0 = ((const float2 *)(slot + RG::OFF_V + rr * RG::FROW))[lane];
-            // dp as staged: FP64 for the FP64 prep, FP32 (rounded at put) for the FP32 one
-            using DT2 = typename std::conditional<PREP64, double2, float2>::type;
-            const DT2 d0 = ((const DT2 *)(slot + RG::OFF_DP + rr * kW * sizeof(DT2) / 2))[lane];
-            const float4 gA = ((const float4 *)(slot + RG::OFF_GE + rr * kW * 16))[2 * lane];
-            const float4 gB = ((const float4 *)(slot + RG::OFF_GE + rr * kW * 16))[2 * lane + 1];
+            const double2 d0 = ((const double2 *)(slot + RG::OFF_DP + rr * RG::DROW))[lane];
+            const double2 cg = ((const double2 *)(slot + RG::OFF_CG + rr * RG::DROW))[lane];
+            // per-cell word: dt2*scp2i with ip, iu, iv in the three lowest mantissa bits
+            const unsigned mA = (unsigned)__double2loint(cg.x), mB = (unsigned)__double2loint(cg.y);
+            const float2 ds0 = make_float2(d2f_pos(cg.x), d2f_pos(cg.y));  // FP32 dt2*scp2i (2.0 off the arrays)
+            const float2 giu = make_float2((mA & kIU) ? 1.f : 0.f, (mB & kIU) ? 1.f : 0.f);
+            const float2 giv = make_float2((mA & kIV) ? 1.f : 0.f, (mB & kIV) ? 1.f : 0.f);
+            // scp2/dt2 = 1/(dt2*scp2i) at sea cells (scp2i = 1/scp2, geopar.F90:320), 0 on land
+            const float2 qs0 = make_float2((mA & kIP) ? rcp_approx(ds0.x) : 0.f, (mB & kIP) ? rcp_approx(ds0.y) : 0.f);
             float2 f0[NQ], c0[NQ];
 #pragma unroll
             for (int q = 0; q < NQ; q++) {
-              const int qr = PAIR ? sub : q;  // ring row of this tracer
-              f0[q] = ((const float2 *)(slot + RG::OFF_FO + (qr * kRB + rr) * RG::FROW))[lane];
-              c0[q] = MP ? z2 : ((const float2 *)(slot + RG::OFF_FC + (qr * kRB + rr) * RG::FROW))[lane];
+              f0[q] = ((const float2 *)(slot + RG::OFF_FO + (q * kRB + rr) * RG::FROW))[lane];
+              c0[q] = MP ? z2 : ((const float2 *)(slot + RG::OFF_FC + (q * kRB + rr) * RG::FROW))[lane];
             }
 
             // ---- thickness factors of row J-1 (mod_tsadvc.F90:1905-1942)
             float2 W1, R1, QF1, Wm1, H1;  // Wm1 = W-1 and H1 = fco+fcn (MPDATA only)
             if (PREP64) {
               // continuity (:1931-1936): the face-flux differences and their sum by
-              // two-sum in FP32 (exact differences, the sum rounded once relative to
-              // the divergence), scaled by dt2*scp2i and added to dp in FP64
-              const double2 si0 = ((const double2 *)(slot + RG::OFF_SI + rr * kW * 8))[lane];
+              // two-sum in FP32, scaled by dt2*scp2i and added to dp in FP64
               const float2 dv = comp_div2(east(u1), u1, v0, v1);
-              const double fdvA = (double)dv.x * sA1, fdvB = (double)dv.y * sB1;
-              const double fcoA = kmax(dA1 + fdvA, 0.0), fcnA = kmax(dA1, 0.0);
-              const double fcoB = kmax(dB1 + fdvB, 0.0), fcnB = kmax(dB1, 0.0);
-              const double hA = fcnA + kOnemu, hB = fcnB + kOnemu;
-              // 1/h: FP32 seed, one Newton step in FP64 (relative error ~2^-44)
-              const float2 fcnf = pos2(make_float2((float)dA1, (float)dB1));
-              double rA = (double)rcp_approx(fcnf.x + onemu), rB = (double)rcp_approx(fcnf.y + onemu);
-              rA = __fma_rn(rA, __fma_rn(-hA, rA, 1.0), rA);
-              rB = __fma_rn(rB, __fma_rn(-hB, rB, 1.0), rB);
-              // W = (fco+onemu)/(fcn+onemu) = 1 + (fco-fcn)/(fcn+onemu)
-              W1 = make_float2((float)__fma_rn(fcoA - fcnA, rA, 1.0), (float)__fma_rn(fcoB - fcnB, rB, 1.0));
-              R1 = make_float2((float)rA, (float)rB);
-              QF1 = mul2(fcnf, QS1);
-              if (MP) {
-                Wm1 = make_float2((float)((fcoA - fcnA) * rA), (float)((fcoB - fcnB) * rB));
-                H1 = make_float2((float)(fcoA + fcnA), (float)(fcoB + fcnB));
+              const double bA = dA1 + kOnemu, bB = dB1 + kOnemu;       // dp + onemu
+              const double hA = ge0(dA1) ? bA : kOnemu, hB = ge0(dB1) ? bB : kOnemu;  // fcn + onemu
+              const double rA = rcp64(hA), rB = rcp64(hB);
+              const float2 hf = make_float2(d2f_pos(hA), d2f_pos(hB));
+              if (!MP) {
+                // fco + onemu = max(dp + div*dt2*scp2i, 0) + onemu
+                const double cA = kmax(__fma_rn(f2d_i(dv.x), sA1, bA), kOnemu);
+                const double cB = kmax(__fma_rn(f2d_i(dv.y), sB1, bB), kOnemu);
+                W1 = make_float2(d2f_pos(cA * rA), d2f_pos(cB * rB));
+              } else {
+                const double fA = f2d_i(dv.x) * sA1, fB = f2d_i(dv.y) * sB1;
+                const double cA = kmax(bA + fA, kOnemu), cB = kmax(bB + fB, kOnemu);
+                Wm1 = make_float2(d2f_i((cA - hA) * rA), d2f_i((cB - hB) * rB));
+                W1 = add2(Wm1, make_float2(1.f, 1.f));
+                H1 = add2(sub2(make_float2(d2f_pos(cA), d2f_pos(cB)), onemu2), sub2(hf, onemu2));
               }
-              sA1 = si0.x;
-              sB1 = si0.y;
+              R1 = make_float2(d2f_pos(rA), d2f_pos(rB));
+              QF1 = mul2(sub2(hf, onemu2), QS1);  // fcn*scp2/dt2
             } else {
               const float2 fdv = mul2(comp_div2(east(u1), u1, v0, v1), DS1);
-              const float2 d = make_float2((float)dA1, (float)dB1);
+              const float2 d = make_float2(d2f_i(dA1), d2f_i(dB1));
               const float2 fcn = pos2(d);
               const float2 r = make_float2(rcp_approx(fcn.x + onemu), rcp_approx(fcn.y + onemu));
               const float2 w1 = fma2(fdv, r, make_float2(1.f, 1.f));
@@ -379,14 +370,14 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
             // advective or antidiffusive flux, mod_tsadvc.F90:738-758), split for the
             // upwind choice: u*f_upwind = max(u,0)*f_west + min(u,0)*f (one of the two
             // products is zero, so the rounding is that of u*f)
-            const float2 u0m = mul2(u0, make_float2(gA.z, gB.z)), v0m = mul2(v0, make_float2(gA.w, gB.w));
+            const float2 u0m = mul2(u0, giu), v0m = mul2(v0, giv);
             const float2 un0 = neg2(u0m), vn0 = neg2(v0m);
             const float2 up0 = sub2(u0m, un0), vp0 = sub2(v0m, vn0);  // max(x,0) = x - min(x,0), exact
             const float2 half = make_float2(0.5f, 0.5f);
             const float2 u1h = mul2(u1m, half), v0h = mul2(v0m, half), v1h = mul2(v1m, half);
             const float2 F14 = make_float2(7.f / 12.f, 7.f / 12.f), F24 = make_float2(-1.f / 12.f, -1.f / 12.f);
-            // land flags (1 = land): scp2/dt2 is stored as 0 on land
-            const float2 L0 = make_float2(gA.y > 0.f ? 0.f : 1.f, gB.y > 0.f ? 0.f : 1.f);
+            // land flags (1 = land)
+            const float2 L0 = make_float2((mA & kIP) ? 0.f : 1.f, (mB & kIP) ? 0.f : 1.f);
             const bool ip1A = L1.x == 0.f, ip1B = L1.y == 0.f;
             const bool ip2B = L2.y == 0.f, ip2E = L2e == 0.f;  // column B and its east neighbour, row J-2
             const bool ip3A = L3.x == 0.f, ip3B = L3.y == 0.f;
@@ -421,14 +412,18 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
               const float iuwB = __shfl_up_sync(kFull, IU1.y, 1), iueA = __shfl_down_sync(kFull, IU1.x, 1);
               x4A = iuwB != 0.f && IU1.y != 0.f;
               x4B = IU1.x != 0.f && iueA != 0.f;
-              y4A = IV2.x != 0.f && gA.w != 0.f;
-              y4B = IV2.y != 0.f && gB.w != 0.f;
+              y4A = IV2.x != 0.f && giv.x != 0.f;
+              y4B = IV2.y != 0.f && giv.y != 0.f;
             }
             float2 res[NQ];
             auto store_row = [&](int q, float resA, float resB) {
               float *p = fn[q] + (long long)a0 + (long long)(jo + nb - 1) * ld1;
-              if (stA) p[0] = resA;
-              if (stB) p[1] = resB;
+              if (stA && stB) {
+                __stcs((float2 *)p, make_float2(resA, resB));  // a0 is even, ld1 a multiple of 4: 8-byte aligned
+              } else {
+                if (stA) __stcs(p, resA);
+                if (stB) __stcs(p + 1, resB);
+              }
               if (images) {
                 if (stA && iA <= images) p[ii] = resA;
                 if (stA && iA > ii - images) p[-ii] = resA;
@@ -627,36 +622,28 @@ __global__ void __launch_bounds__(kWarps * 32, (NQ == 1 || PAIR) ? 3 : 2)
             QF2 = QF1;
             DS3 = DS2;
             DS2 = DS1;
-            DS1 = make_float2(gA.x, gB.x);
-            QS1 = make_float2(gA.y, gB.y);
+            DS1 = ds0;
+            QS1 = qs0;
             L1 = L0;
             u1 = u0;
             u1m = u0m;
             if (MP || F4) v1m = v0m;
             if (MP) H2 = H1;
             if (F4) {
-              IU1 = make_float2(gA.z, gB.z);
+              IU1 = giu;
               IV2 = IV1;
-              IV1 = make_float2(gA.w, gB.w);
+              IV1 = giv;
             }
             v1 = v0;
             dA1 = d0.x;
             dB1 = d0.y;
-          }
-          __syncwarp();  // every lane is done with the slot before it is refilled
-          if (PAIR && lane == 0) tma::arrive(empty + (g % kNS));
-          if (lead) {
-            bool okw = true;
-            if (lane == 0 && t + kNS < T) okw = issue(t + kNS);
-            if (!__shfl_sync(kFull, okw, 0)) {
-              // the partner stopped: the copies already in flight land, then stop
-              for (int d = 1; d < kNS && t + d < T; d++)
-                tma::wait(bar + ((g + d) % kNS), ((g + d) / kNS) & 1u, nullptr);
-              ok = false;
-              t++;
-              break;
+            if (PREP64) {  // FP64 dt2*scp2i without the mask bits
+              sA1 = __hiloint2double(__double2hiint(cg.x), (int)(mA & ~7u));
+              sB1 = __hiloint2double(__double2hiint(cg.y), (int)(mB & ~7u));
             }
           }
+          __syncwarp();  // every lane is done with the slot before it is refilled
+          if (lane == 0 && t + kNS < T) issue(t + kNS);
         }
       }
     }
@@ -685,34 +672,20 @@ cudaError_t launch_wait_probe(int arrive, int *err, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// per-cell factors of the strip kernel: dt2*scp2i, scp2/dt2 (0 on land, so
-// the Zalesak ratios of land cells stay finite), iu and iv as 0/1
-__global__ void geo4_kernel(const double *scp2, const double *scp2i, const uint8_t *msk, double dt2, long long n,
-                            float4 *out) {
+// per-cell word of the strip kernel: dt2*scp2i (FP64) with ip, iu, iv in
+// its three lowest mantissa bits (a relative change below 2^-49)
+__global__ void cell_word_kernel(const double *scp2i, const uint8_t *msk, double dt2, long long n, double *out) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const uint8_t m = msk[t];
-    out[t] = make_float4((float)(dt2 * scp2i[t]), (m & kIP) ? (float)(scp2[t] / dt2) : 0.f, (m & kIU) ? 1.f : 0.f,
-                         (m & kIV) ? 1.f : 0.f);
+    const long long b = __double_as_longlong(dt2 * scp2i[t]);
+    out[t] = __longlong_as_double((b & ~7LL) | (long long)(msk[t] & (kIP | kIU | kIV)));
   }
 }
 
-cudaError_t launch_geo4(const double *scp2, const double *scp2i, const uint8_t *msk, double dt2, long long n,
-                        float4 *out, cudaStream_t s) {
+cudaError_t launch_cell_words(const double *scp2i, const uint8_t *msk, double dt2, long long n, double *out,
+                              cudaStream_t s) {
   int bx = (int)((n + 255) / 256);
   if (bx > 2048) bx = 2048;
-  geo4_kernel<<<bx, 256, 0, s>>>(scp2, scp2i, msk, dt2, n, out);
-  return cudaGetLastError();
-}
-
-__global__ void dtsi_kernel(const double *scp2i, double dt2, long long n, double *out) {
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-    out[t] = dt2 * scp2i[t];
-}
-
-cudaError_t launch_dtsi(const double *scp2i, double dt2, long long n, double *out, cudaStream_t s) {
-  int bx = (int)((n + 255) / 256);
-  if (bx > 2048) bx = 2048;
-  dtsi_kernel<<<bx, 256, 0, s>>>(scp2i, dt2, n, out);
+  cell_word_kernel<<<bx, 256, 0, s>>>(scp2i, msk, dt2, n, out);
   return cudaGetLastError();
 }
 
@@ -728,26 +701,11 @@ cudaError_t launch_mix_col2(int scheme, const MixBasin *basins, const int4 *item
     kern<<<nsm * per_sm, kWarps * 32, smem, s>>>(basins, items, nitems, head, err);
     return cudaGetLastError();
   };
-#define HYC_COL2(S, Q, P) pick(mix_col2_kernel<S, Q, P>, Ring<S, Q, P>::SMEM)
-#define HYC_PAIR(S, P) pick(mix_col2_kernel<S, 1, P, true>, Col2Geom<S, 1, P, true>::SMEM)
-  if (nq == 3) {  // warp pairs, one tracer per warp
-    if (scheme == kFCT2) return prep64 ? HYC_PAIR(kFCT2, true) : HYC_PAIR(kFCT2, false);
-    if (scheme == kMPDATA) return prep64 ? HYC_PAIR(kMPDATA, true) : HYC_PAIR(kMPDATA, false);
-    return cudaErrorInvalidValue;
-  }
-#undef HYC_PAIR
-  if (scheme == kFCT2) {
-    if (nq >= 2) return prep64 ? HYC_COL2(kFCT2, 2, true) : HYC_COL2(kFCT2, 2, false);
-    return prep64 ? HYC_COL2(kFCT2, 1, true) : HYC_COL2(kFCT2, 1, false);
-  }
-  if (scheme == kMPDATA) {
-    if (nq >= 2) return prep64 ? HYC_COL2(kMPDATA, 2, true) : HYC_COL2(kMPDATA, 2, false);
-    return prep64 ? HYC_COL2(kMPDATA, 1, true) : HYC_COL2(kMPDATA, 1, false);
-  }
-  if (scheme == kFCT4) {
-    if (nq >= 2) return prep64 ? HYC_COL2(kFCT4, 2, true) : HYC_COL2(kFCT4, 2, false);
-    return prep64 ? HYC_COL2(kFCT4, 1, true) : HYC_COL2(kFCT4, 1, false);
-  }
+#define HYC_COL2(S, Q) (prep64 ? pick(mix_col2_kernel<S, Q, true>, Ring<S, Q>::SMEM) \
+                               : pick(mix_col2_kernel<S, Q, false>, Ring<S, Q>::SMEM))
+  if (scheme == kFCT2) return nq >= 2 ? HYC_COL2(kFCT2, 2) : HYC_COL2(kFCT2, 1);
+  if (scheme == kMPDATA) return nq >= 2 ? HYC_COL2(kMPDATA, 2) : HYC_COL2(kMPDATA, 1);
+  if (scheme == kFCT4) return nq >= 2 ? HYC_COL2(kFCT4, 2) : HYC_COL2(kFCT4, 1);
 #undef HYC_COL2
   return cudaErrorInvalidValue;
 }

@@ -11,13 +11,20 @@
 //
 // Limits and sharing:
 //   * at most kNoallocMaxCells = 2^21 cells per slice ((idm+2*nbdy) *
-//     (jdm+2*nbdy)), i.e. 16 MiB of output slice plus 2 MiB of mask;
-//     larger slices are rejected with HYC_ERR_ARG;
+//     (jdm+2*nbdy)), i.e. 16 MiB of output slice plus 2 MiB of mask, and
+//     nbdy <= 64; larger slices are rejected with HYC_ERR_ARG;
+//   * the masks are checked as hyc_adv_init checks them: iu must be
+//     ip(i)*ip(i-1) and iv ip(j)*ip(j-1) wherever the west / south neighbour
+//     exists.  The check runs on the GPU beside the mask conversion and
+//     sets a flag word in the scratch; the call reads the flag back before
+//     it returns (so it returns after its GPU work) and answers
+//     HYC_ERR_MASK if it is set;
 //   * all calls on a device share the one array and it keeps the contents
-//     of the last call.  Nothing in it has to start at zero: every call
-//     rewrites the whole mask and writes every sea cell of the output slice
-//     before reading it.  Calls whose GPU work overlaps (different streams
-//     or host threads without ordering) race on the array; order them;
+//     of the last call.  The flag word must start at zero and is cleared
+//     at the start of every call; nothing else has to: every call rewrites
+//     the whole mask and writes every sea cell of the output slice before
+//     reading it.  Calls whose GPU work overlaps (different streams or host
+//     threads without ordering) race on the array; order them;
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress with that device current) and caches it; make
 //     that first call before any stream capture.
@@ -35,8 +42,10 @@
 namespace {
 
 constexpr long long kNoallocMaxCells = 1LL << 21;
+constexpr int kNoallocMaxNbdy = 64;
 constexpr long long kMaskOffsetBytes = kNoallocMaxCells * (long long)sizeof(double);
-constexpr long long kScratchBytes = kMaskOffsetBytes + kNoallocMaxCells;
+constexpr long long kFlagOffsetBytes = kMaskOffsetBytes + kNoallocMaxCells;  // one int: mask check
+constexpr long long kScratchBytes = kFlagOffsetBytes + 256;
 
 // The scratch.  In host code this name is a host-side stand-in, not a
 // device address: only the address from cudaGetSymbolAddress may be
@@ -47,11 +56,17 @@ constexpr int kMaxDev = 64;
 std::mutex g_mu;
 void *g_scratch_addr[kMaxDev] = {};
 
-// ip/iu/iv (int32, one slice) -> kernel mask byte ip | iu<<1 | iv<<2
-__global__ void noalloc_mask_kernel(const int32_t *ip, const int32_t *iu, const int32_t *iv, long long n,
-                                    uint8_t *msk) {
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-    msk[t] = (uint8_t)((ip[t] != 0 ? hyc::kIP : 0) | (iu[t] != 0 ? hyc::kIU : 0) | (iv[t] != 0 ? hyc::kIV : 0));
+// ip/iu/iv (int32, one slice of ld1 x ld2) -> kernel mask byte
+// ip | iu<<1 | iv<<2, and the bigrid consistency of iu/iv with ip (the
+// check of hyc_adv_init): *bad is set where it fails
+__global__ void noalloc_mask_kernel(const int32_t *ip, const int32_t *iu, const int32_t *iv, long long ld1,
+                                    long long n, uint8_t *msk, int *bad) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const bool p = ip[t] != 0, u = iu[t] != 0, v = iv[t] != 0;
+    const long long ia = t % ld1;
+    if ((ia > 0 && u != (p && ip[t - 1] != 0)) || (t >= ld1 && v != (p && ip[t - ld1] != 0))) atomicOr(bad, 1);
+    msk[t] = (uint8_t)((p ? hyc::kIP : 0) | (u ? hyc::kIU : 0) | (v ? hyc::kIV : 0));
+  }
 }
 
 // errors are reported through hyc_last_error(NULL, ...)
@@ -66,17 +81,19 @@ extern "C" int hyc_advem_noalloc(int32_t idm, int32_t jdm, int32_t nbdy, int32_t
                                  const double *fldc, const double *u, const double *v, const double *fco,
                                  const double *fcn, double posdef, const double *scal, const double *scali,
                                  double dt2, const int32_t *ip, const int32_t *iu, const int32_t *iv, void *stream) {
-  if (idm < 1 || jdm < 1 || nbdy < 3) return nerr(HYC_ERR_ARG, "hyc_advem_noalloc: bad sizes (need nbdy >= 3)");
+  if (idm < 1 || jdm < 1 || nbdy < 3 || nbdy > kNoallocMaxNbdy)
+    return nerr(HYC_ERR_ARG, "hyc_advem_noalloc: bad sizes (need idm, jdm >= 1 and 3 <= nbdy <= 64)");
   if (!(advtyp == 0 || advtyp == 1 || advtyp == 2 || advtyp == 4))
     return nerr(HYC_ERR_ADVTYP, "hyc_advem_noalloc: advtyp must be 0, 1, 2 or 4");
   const int mbdy = advtyp == 0 ? 2 : 5;
   if (nbdy < mbdy) return nerr(HYC_ERR_NBDY, "hyc_advem_noalloc: nbdy < mbdy_advtyp(advtyp)");
   if (!fld || !u || !v || !fco || !fcn || !scal || !scali || !ip || !iu || !iv || (advtyp >= 2 && !fldc))
     return nerr(HYC_ERR_ARG, "hyc_advem_noalloc: null array");
-  const int ld1 = idm + 2 * nbdy, ld2 = jdm + 2 * nbdy;
-  const long long cells = (long long)ld1 * ld2;
-  if (cells > kNoallocMaxCells)
+  const long long ld1l = (long long)idm + 2LL * nbdy, ld2l = (long long)jdm + 2LL * nbdy;
+  if (ld1l > kNoallocMaxCells || ld2l > kNoallocMaxCells || ld1l * ld2l > kNoallocMaxCells)
     return nerr(HYC_ERR_ARG, "hyc_advem_noalloc: slice larger than the 2^21-cell static scratch");
+  const int ld1 = (int)ld1l, ld2 = (int)ld2l;
+  const long long cells = ld1l * ld2l;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= kMaxDev) return nerr(HYC_ERR_CUDA, "hyc_advem_noalloc: no CUDA device");
@@ -93,11 +110,13 @@ extern "C" int hyc_advem_noalloc(int32_t idm, int32_t jdm, int32_t nbdy, int32_t
   }
   double *out = reinterpret_cast<double *>(base);
   uint8_t *msk = reinterpret_cast<uint8_t *>(base) + kMaskOffsetBytes;
+  int *bad = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(base) + kFlagOffsetBytes);
   cudaStream_t s = (cudaStream_t)stream;
 
+  if ((e = cudaMemsetAsync(bad, 0, sizeof(int), s)) != cudaSuccess) return nerr(HYC_ERR_CUDA, cudaGetErrorString(e));
   int bx = (int)((cells + 255) / 256);
   if (bx > 1024) bx = 1024;
-  noalloc_mask_kernel<<<bx, 256, 0, s>>>(ip, iu, iv, cells, msk);
+  noalloc_mask_kernel<<<bx, 256, 0, s>>>(ip, iu, iv, ld1l, cells, msk, bad);
   if ((e = cudaGetLastError()) != cudaSuccess) return nerr(HYC_ERR_CUDA, cudaGetErrorString(e));
 
   hyc::TileArgs a;
@@ -132,5 +151,13 @@ extern "C" int hyc_advem_noalloc(int32_t idm, int32_t jdm, int32_t nbdy, int32_t
   if ((e = hyc::launch_advect_tiles(advtyp, a, 1, shape, s)) != cudaSuccess)
     return nerr(HYC_ERR_CUDA, cudaGetErrorString(e));
   if ((e = hyc::launch_copy_back(a, 1, s)) != cudaSuccess) return nerr(HYC_ERR_CUDA, cudaGetErrorString(e));
+  // the mask check: the copy back writes fld only where the masks are sea,
+  // so with inconsistent masks fld holds a result the reference would not
+  // give; the caller learns it here
+  int flag = 0;
+  if ((e = cudaMemcpyAsync(&flag, bad, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return nerr(HYC_ERR_CUDA, cudaGetErrorString(e));
+  if (flag) return nerr(HYC_ERR_MASK, "hyc_advem_noalloc: iu/iv inconsistent with ip (bigrid masks expected)");
   return HYC_OK;
 }

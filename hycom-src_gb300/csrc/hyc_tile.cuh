@@ -94,7 +94,21 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
       int bb = t / RX, aa = t - bb * RX;
       double o = FCO[t] * FCN[t];  // onetamas*dp
       double fdv = 0.0;
-      if (aa < RX - 1 && bb < RY - 1) fdv = ((U[t + 1] - U[t]) + (V[t + RX] - V[t])) * dt2 * SCI[t];
+      if (aa < RX - 1 && bb < RY - 1) {
+        if (A.ufco) {
+          // the divergence of the smoothed layer-1 fluxes, read as the
+          // staged ones would be (0 outside the array)
+          const int i = ib0 + aa, j = jb0 + bb;
+          auto at = [&](const double *f, int ic, int jc) -> double {
+            const bool in = (ic >= 1 - nb) && (ic <= A.ii + nb) && (jc >= 1 - nb) && (jc <= A.jj + nb);
+            return in ? f[(long long)(ic + nb - 1) + (long long)(jc + nb - 1) * ld1] : 0.0;
+          };
+          fdv = ((at(A.ufco, i + 1, j) - at(A.ufco, i, j)) + (at(A.vfco, i, j + 1) - at(A.vfco, i, j))) * dt2 *
+                SCI[t];
+        } else {
+          fdv = ((U[t + 1] - U[t]) + (V[t + RX] - V[t])) * dt2 * SCI[t];
+        }
+      }
       FCO[t] = kmax(o + fdv, 0.0);
       FCN[t] = kmax(o, 0.0);
     }

@@ -540,10 +540,6 @@ class Ensemble(_StreamFollower):
     def enable_timers(self, on: bool = True):
         self._chk(lib().hyc_ens_enable_timers(self._h, int(bool(on))))
 
-    def set_tma(self, on: bool):
-        """Mixed form: TMA-staged, double-buffered kernel (True) or plain loads."""
-        self._chk(lib().hyc_ens_set_option(self._h, 2, int(bool(on))))
-
     def set_prep64(self, on: bool):
         """Mixed form: thickness prep in FP64 (True, default) or compensated FP32."""
         self._chk(lib().hyc_ens_set_option(self._h, 1, int(bool(on))))
@@ -553,14 +549,13 @@ class Ensemble(_StreamFollower):
         self._chk(lib().hyc_ens_set_posdef(self._h, b, q, float(posdef)))
 
     def set_strip_tracers(self, n: int):
-        """Two-column strip kernel: tracers advanced per pass (1 or 2), or 3:
-        two warps per staged block, one tracer each."""
+        """Mixed form: tracers advanced per pass of the strip kernel (1 or 2)."""
         self._chk(lib().hyc_ens_set_option(self._h, 3, int(n)))
 
     def option(self, name: str) -> int:
-        """Current value of an option: "prep64", "tma" or "strip_tracers"."""
+        """Current value of an option: "prep64" or "strip_tracers"."""
         v = C.c_int32()
-        self._chk(lib().hyc_ens_get_option(self._h, {"prep64": 1, "tma": 2, "strip_tracers": 3}[name], C.byref(v)))
+        self._chk(lib().hyc_ens_get_option(self._h, {"prep64": 1, "strip_tracers": 3}[name], C.byref(v)))
         return v.value
 
     def stats(self, reset: bool = False) -> dict:

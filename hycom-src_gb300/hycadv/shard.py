@@ -4,9 +4,9 @@ Basins of an ensemble share nothing during a step, so a multi-GPU run gives
 every rank a subset of the basins and needs no exchange in the data path:
 each rank advances its own basins; the only collectives are the barriers
 and the max-over-ranks of the timed region around a benchmark, and an
-optional gather of results for checking.  The reference's MPI halo
-exchange (mod_xc_mp.h) applies to a single basin split over ranks, which
-this library does not do: every configuration's basin fits one GPU.
+optional gather of results for checking.  A single basin split over
+ranks, with the reference's halo exchange (mod_xc_mp.h), is the other
+multi-rank path: hycadv.decomp.
 """
 from __future__ import annotations
 

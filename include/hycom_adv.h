@@ -349,11 +349,14 @@ int hyc_get_stats(hyc_ctx *ctx, hyc_stats *out, int32_t reset);
  * synchronise the whole device.  Same arguments and result as hyc_advem
  * with where = HYC_DEVICE, but without a context: the grid sizes and the
  * masks ip/iu/iv (int32, device, one slice each, the bigrid masks) are
- * passed in, and the work is queued on `stream` (a cudaStream_t, NULL for
- * the default stream); the call returns without waiting for it.
- * Scratch is a fixed array of 2^21 cells (18 MiB) inside the library that
- * every GPU loading the library holds until exit; slices with more than
- * 2^21 cells ((idm+2*nbdy)*(jdm+2*nbdy)) are rejected with HYC_ERR_ARG.
+ * passed in, and the work runs on `stream` (a cudaStream_t, NULL for the
+ * default stream).  The masks are checked on the GPU as hyc_adv_init
+ * checks them (iu = ip(i)*ip(i-1), iv = ip(j)*ip(j-1)); the call reads that
+ * check back, so it returns after its GPU work, with HYC_ERR_MASK if the
+ * masks are inconsistent.  Scratch is a fixed array of 2^21 cells
+ * (18 MiB) inside the library that every GPU loading the library holds
+ * until exit; slices with more than 2^21 cells ((idm+2*nbdy)*(jdm+2*nbdy))
+ * or nbdy > 64 are rejected with HYC_ERR_ARG.
  * All calls on a device share that array: calls whose GPU work overlaps
  * race and must be ordered by the caller.  The first call on a device
  * looks up the array's address; make it before any stream capture.
@@ -423,9 +426,9 @@ int hyc_ens_put_slices(hyc_ens *ens, int32_t basin, int32_t what, int32_t s0, in
 int hyc_ens_get_slices(hyc_ens *ens, int32_t basin, int32_t what, int32_t s0, int32_t ns, double *dst,
                        int32_t where);
 /* Tile shape of the step kernel; hyc_ens_tune picks one.  Mixed form:
- * tx = 56 is the two-column strip kernel (64-column strips streamed by TMA,
- * the default; ty = rows per segment, 32/64/128/256/512), tx = 26 the one-column
- * strip kernel (ty likewise), other shapes tx x ty cell tiles. */
+ * tx = 56, the strip kernel (64-column strips streamed by TMA, 56 columns
+ * updated), ty = rows per segment, 32/64/128/256/512.  FP64 form: 32 x 16
+ * or 16 x 16 cell tiles. */
 int hyc_ens_set_tile(hyc_ens *ens, int32_t tx, int32_t ty);
 /*
  * Autotuner: time every supported tile shape on this ensemble (the kernel
@@ -435,9 +438,8 @@ int hyc_ens_set_tile(hyc_ens *ens, int32_t tx, int32_t ty);
 int hyc_ens_tune(hyc_ens *ens, int32_t advtyp, double delt1, int32_t *tx, int32_t *ty, double *ms);
 /*
  * Advance every basin nsteps leapfrog steps.  advtyp: FP64 form 0 (PCM),
- * 1 (MPDATA), 2 (FCT2), 4 (FCT4); FP32-mixed form 2 (FCT2) with every
- * kernel, 1 (MPDATA) and 4 (FCT4) with the two-column strip kernel
- * (tx = 56).  PCM and MPDATA read only level t-1 (mod_tsadvc.F90:152, :495).
+ * 1 (MPDATA), 2 (FCT2), 4 (FCT4); FP32-mixed form 1 (MPDATA), 2 (FCT2)
+ * and 4 (FCT4).  PCM and MPDATA read only level t-1 (mod_tsadvc.F90:152, :495).
  * use_graph = 1: the nsteps launches are captured once into a CUDA graph
  * (per nsteps/advtyp/delt1/tile) and replayed.  Asynchronous.
  */
@@ -451,25 +453,20 @@ int hyc_ens_content(hyc_ens *ens, int32_t basin, int32_t tracer, int32_t what, d
 int hyc_ens_stats(hyc_ens *ens, hyc_stats *out, int32_t reset);
 /*
  * Options.  HYC_OPT_PREP64 (mixed form only; default 1): 1 = the per cell
- * and layer thickness prep (continuity fco, the division factors
- * (fco+onemu)/(fcn+onemu) and 1/(fcn+onemu)) runs in FP64; 0 = it runs in
- * FP32 with a compensated (two-sum) divergence and W = 1 + div/(fcn+onemu),
- * which rounds the same factors to FP32 within one ulp without using the
- * FP64 pipe (GB300 issues FP64 at ~1/72 of the FP32 rate).
+ * and layer thickness prep runs in FP64 -- the continuity update
+ * fco+onemu = (dp+onemu) + div*dt2*scp2i, fcn+onemu, the reciprocal
+ * 1/(fcn+onemu) (hardware seed and one Newton step, relative error below
+ * 2^-40) and W = (fco+onemu)/(fcn+onemu); the face-flux divergence is a
+ * compensated (two-sum) FP32 sum of the FP32 fluxes.  0 = the same factors
+ * in compensated FP32 (W = 1 + div/(fcn+onemu)), which leaves the FP64 pipe
+ * idle (GB300 issues FP64 at ~1/70 of the FP32 rate).  dp is read in FP64
+ * either way.
  */
 #define HYC_OPT_PREP64 1
-/* HYC_OPT_TMA (mixed form; default 1 when every basin has nbdy = 6): stage
- * tiles with the Tensor Memory Accelerator, double-buffered (1), or with
- * plain loads (0). */
-#define HYC_OPT_TMA 2
-/* HYC_OPT_STRIP_TRACERS (mixed form, two-column strip kernel; default 2):
- * tracers advanced per pass over a layer.  2: one warp advances two
- * tracers and shares the per-cell thickness factors between them; 1: one
- * tracer per pass, fewer registers, more warps per SM; 3: two warps share
- * a staged block and advance one tracer each (the inputs of a row are
- * read once, and 12 warps fit on an SM instead of 8; each warp forms the
- * thickness factors itself, which costs more than the extra warps gain:
- * measured 15 % slower than 2).  hyc_ens_tune tries 1 and 2. */
+/* HYC_OPT_STRIP_TRACERS (mixed form; default 2): tracers advanced per pass
+ * over a layer.  2: one warp advances two tracers and shares the per-cell
+ * thickness factors between them; 1: one tracer per pass, fewer registers,
+ * more warps per SM.  hyc_ens_tune tries both. */
 #define HYC_OPT_STRIP_TRACERS 3
 int hyc_ens_set_option(hyc_ens *ens, int32_t option, int32_t value);
 /*

@@ -1,6 +1,7 @@
 """Size-independent properties at the full size of the benchmark basin
-(4500x3298x41, periodic in x, T+S, FCT2, Courant 0.8, delt1 240 s), where
-the oracle would take minutes per step:
+(4500x3298x41, periodic in x, T+S, FCT2, Courant 0.8, delt1 240 s); the
+comparisons with the oracle at this size are in test_gpu_oracle_c1.py and
+test_gpu_oracle_c2c3.py:
 
 * FP64 ensemble step: tracer content conserved to 1e-13 and no value
   outside the inputs' range (FCT keeps new extrema out);
@@ -22,7 +23,11 @@ def c1(cuda):
 
     wl = dict(bench.WORKLOADS["c1"])
     b, masks, nreg, case = bench.make_workload(wl, cuda)
-    return wl, b, masks, nreg, case
+    yield wl, b, masks, nreg, case
+    import torch
+
+    del case
+    torch.cuda.empty_cache()
 
 
 def _spec(b, masks, nreg, kdm):

@@ -370,3 +370,53 @@ def test_za_read_into_device_memory(cuda, tmp_path):
     got = dev.cpu().numpy()
     assert np.array_equal(got[mask != 0], f[:10, :20].ravel())
     assert np.all(got[mask == 0] == -3.0)
+
+
+@pytest.mark.parametrize("advtyp", SCHEMES)
+@pytest.mark.parametrize("periodic", [False, True])
+def test_tsadvc_isopycnic_bit_for_bit(cuda, advtyp, periodic):
+    """Isopycnic mode (nhybrd = 0, mod_tsadvc.F90:1855-1897): layer 1
+    advects th3d and saln with the smoothed mixed-layer fluxes, its tracers
+    (and q2, q2l) with the layer's own fluxes and the thickness factors of
+    the smoothed ones; deeper layers advect saln and the tracers only."""
+    b = basin(83, 61, periodic, seed=131)
+    g = oracle_grid(b)
+    kdm = 3
+    c = np_case(b, g, kdm=kdm, ntracr=2, seed=131, courant=0.7, delt1=600.0)
+    c["delt1"] = 600.0
+    rng = np.random.default_rng(131)
+    c["q2"] = 0.01 + rng.random((2, kdm + 2, b.ld2, b.ld1)) * 0.1
+    c["q2l"] = 0.1 + rng.random((2, kdm + 2, b.ld2, b.ld1))
+    tf = np.array([0, 2], np.int32)
+    t = torchify(c, cuda)
+    ctx = make_ctx(b, g, kdm)
+    bind_all(ctx, t, extra=("q2", "q2l"))
+    kw = dict(isopyc=True, nhybrd=0, mxlmy=True)
+    temp0 = c["temp"].copy()
+    oracle_steps(g, c, range(1, 4), advtyp, trcflg=tf, q2=c["q2"], q2l=c["q2l"], **kw)
+    gpu_steps(ctx, t, range(1, 4), advtyp, ntracr=2, trcflg=tf, **kw)
+    compare(c, t, keys=("temp", "saln", "th3d", "tracer", "q2", "q2l"))
+    assert np.array_equal(c["temp"], temp0)  # temperature is not advected in isopycnic mode
+    # the smoothing changes layer 1: the same step with hybrid layers differs
+    c2 = np_case(b, g, kdm=kdm, ntracr=0, seed=131, courant=0.7, delt1=600.0)
+    c2["delt1"] = 600.0
+    c2["tracer"] = None
+    oracle_steps(g, c2, [1], advtyp, advflg=1)
+    t2 = np_case(b, g, kdm=kdm, ntracr=0, seed=131, courant=0.7, delt1=600.0)
+    t2["delt1"] = 600.0
+    t2["tracer"] = None
+    oracle_steps(g, t2, [1], advtyp, isopyc=True, nhybrd=0)
+    assert not np.array_equal(c2["th3d"][1, 0], t2["th3d"][1, 0])
+
+
+def test_tsadvc_isopycnic_rejects_fct2c(cuda):
+    b = basin(40, 30, False, seed=132)
+    g = oracle_grid(b)
+    c = np_case(b, g, kdm=2, ntracr=0, seed=132, courant=0.5, delt1=600.0)
+    t = torchify(c, cuda)
+    ctx = make_ctx(b, g, 2)
+    bind_all(ctx, t, extra=())
+    with pytest.raises(hycadv.HycError):
+        ctx.tsadvc(1, 2, delt1=600.0, advtyp=2, btrmas=True, isopyc=True, nhybrd=0)
+    with pytest.raises(hycadv.HycError):
+        ctx.tsadvc(1, 2, delt1=600.0, advtyp=2, isopyc=True, nhybrd=2)
