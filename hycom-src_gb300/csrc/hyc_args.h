@@ -34,6 +34,9 @@ struct TileArgs {
   // fco (the smoothed mixed-layer fluxes, mod_tsadvc.F90:1860-1897) when the
   // fields advected by uflx/vflx are not the ones smoothed; null otherwise
   const double *ufco, *vfco;
+  // advem's conservation rescale (lconserve): per (field, layer) factor
+  // 1 + offset applied by the copy back, index fi*kdm + k; null: none
+  const double *cfac;
   // advem mode (single slice)
   const double *fco, *fcn;
   double dt2;

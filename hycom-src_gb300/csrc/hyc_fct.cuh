@@ -91,7 +91,21 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
     if (A.mode == 0) {  // mod_tsadvc.F90:1931-1938
       const double o = HO[t] * FCN[t];
       double fdv = 0.0;
-      if (aa < RX - 1 && bb < RY - 1) fdv = ((U[t + 1] - U[t]) + (V[t + RX] - V[t])) * dt2 * SCI[t];
+      if (aa < RX - 1 && bb < RY - 1) {
+        if (A.ufco) {
+          // isopycnic layer 1: the divergence of the smoothed fluxes, read as
+          // the staged ones would be (0 outside the array)
+          const int i = ib0 + aa, j = jb0 + bb;
+          auto at = [&](const double *f, int ic, int jc) -> double {
+            const bool in = (ic >= 1 - nb) && (ic <= ii + nb) && (jc >= 1 - nb) && (jc <= jj + nb);
+            return in ? f[(long long)(ic + nb - 1) + (long long)(jc + nb - 1) * ld1] : 0.0;
+          };
+          fdv = ((at(A.ufco, i + 1, j) - at(A.ufco, i, j)) + (at(A.vfco, i, j + 1) - at(A.vfco, i, j))) * dt2 *
+                SCI[t];
+        } else {
+          fdv = ((U[t + 1] - U[t]) + (V[t + RX] - V[t])) * dt2 * SCI[t];
+        }
+      }
       fco = kmax(o + fdv, 0.0);
       fcn = kmax(o, 0.0);
     } else {

@@ -121,8 +121,94 @@ __global__ void copy_back_kernel(const TileArgs A) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     int j = (int)(t / A.ii), i = (int)(t - (long long)j * A.ii);
     long long o = (long long)(i + A.nbdy) + (long long)(j + A.nbdy) * A.ld1;
-    if (A.msk[o] & kIP) dst[o] = src[o];  // advem updates sea points only
+    if (A.msk[o] & kIP) dst[o] = A.cfac ? src[o] * A.cfac[fi * A.kdm + k] : src[o];  // sea points only
   }
+}
+
+// ---------------------------------------------------------------------------
+// advem's explicit conservation (mod_tsadvc.F90:168-203, lconserve): for
+// every (field, layer) of a tile launch, the contents before and after,
+// sum(fld_old*fco*scal) and sum(fld_new*fcn*scal) over interior sea points,
+// each summed in xcsum's order (mod_xc_sm.h:900-963: a row in strips of
+// 2*nbdy+1 columns, each strip from 0 in column order, the strips in order,
+// then the rows in order), then the factor 1 + (old-new)/new that the copy
+// back applies.  fco/fcn are formed as the tile kernel forms them (tsadvc
+// mode) or taken as given (advem mode).
+// rows: [(fi*kdm + k)*2 + (0 old, 1 new)][jj]
+// grid: (ceil(jj/8), nlayers, nfld), 8 warps per block, one row per warp
+// ---------------------------------------------------------------------------
+__global__ void conserve_rows_kernel(const TileArgs A, double *rows) {
+  const int k = blockIdx.y, fi = blockIdx.z;
+  const FieldDesc fd = A.f[fi];
+  if (k + 1 > fd.kmax || k + 1 < fd.kmin) return;
+  const int lane = threadIdx.x & 31, jr = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (jr >= A.jj) return;  // whole warps
+  const long long sl = A.slice, ld = A.ld1;
+  const int nb = A.nbdy, w = 2 * nb + 1, nstrip = (A.ii + w - 1) / w;
+  const double *fo = fd.nbase + (long long)(k + fd.k_off) * sl;  // level n before the copy back
+  const double *fnw = A.out + ((long long)fi * A.kdm + k) * sl;
+  const double *uk = A.mode == 0 ? (A.ufco ? A.ufco : A.uflx + k * sl) : nullptr;
+  const double *vk = A.mode == 0 ? (A.vfco ? A.vfco : A.vflx + k * sl) : nullptr;
+  const long long row = (long long)(jr + nb) * ld;
+  double so = 0.0, sn = 0.0;  // row sums (lane 0)
+  for (int r0 = 0; r0 < nstrip; r0 += 32) {
+    const int st = r0 + lane;
+    double po = 0.0, pn = 0.0;  // strip sums
+    if (st < nstrip) {
+      const int i1 = st * w, i2 = min(A.ii, i1 + w);
+      for (int i = i1; i < i2; i++) {
+        const long long c = row + i + nb;
+        if (!(A.msk[c] & kIP)) continue;
+        double fco, fcn;
+        if (A.mode == 0) {
+          const double o = (A.oneta_n ? A.oneta_n[c] : 1.0) * A.dpn[k * sl + c];
+          const double fdv = ((uk[c + 1] - uk[c]) + (vk[c + ld] - vk[c])) * A.dt2 * A.scali[c];
+          fco = kmax(o + fdv, 0.0);
+          fcn = kmax(o, 0.0);
+        } else {
+          fco = A.fco[c];
+          fcn = A.fcn[c];
+        }
+        po = po + fo[c] * fco * A.scal[c];
+        pn = pn + fnw[c] * fcn * A.scal[c];
+      }
+    }
+    const int nr = min(32, nstrip - r0);
+    for (int l = 0; l < nr; l++) {
+      const double a = __shfl_sync(0xffffffffu, po, l), b = __shfl_sync(0xffffffffu, pn, l);
+      so = so + a;
+      sn = sn + b;
+    }
+  }
+  if (lane == 0) {
+    double *rp = rows + ((long long)fi * A.kdm + k) * 2 * A.jj;
+    rp[jr] = so;
+    rp[A.jj + jr] = sn;
+  }
+}
+
+// one thread per (field, layer): the rows in order, then 1 + offset (:176-181)
+__global__ void conserve_factor_kernel(const TileArgs A, int nlayers, const double *rows, double *fac) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.nfld * nlayers) return;
+  const int fi = t / nlayers, k = t - fi * nlayers;
+  const double *rp = rows + ((long long)fi * A.kdm + k) * 2 * A.jj;
+  double sumold = rp[0], sumnew = rp[A.jj];
+  for (int j = 1; j < A.jj; j++) {
+    sumold = sumold + rp[j];
+    sumnew = sumnew + rp[A.jj + j];
+  }
+  const double offset = sumnew != 0.0 ? (sumold - sumnew) / sumnew : 0.0;
+  fac[fi * A.kdm + k] = 1.0 + offset;
+}
+
+size_t conserve_rows_elems(int nfld, int kdm, int jj) { return (size_t)nfld * kdm * 2 * jj; }
+
+cudaError_t launch_conserve(const TileArgs &a, int nlayers, double *rows, double *fac, cudaStream_t s) {
+  dim3 grid((a.jj + 7) / 8, nlayers, a.nfld);
+  conserve_rows_kernel<<<grid, 256, 0, s>>>(a, rows);
+  conserve_factor_kernel<<<(a.nfld * nlayers + 127) / 128, 128, 0, s>>>(a, nlayers, rows, fac);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_copy_back(const TileArgs &a, int nlayers, cudaStream_t s) {

@@ -66,6 +66,9 @@ struct hyc_ctx {
   Field fields[HYC_NFIELDS];
   double *d_scratch = nullptr;  // advem output slices (fields x layers)
   double *d_iso = nullptr;      // smoothed layer-1 fluxes of isopycnic mode (2 slices)
+  bool lconserve = false;       // advem's explicit conservation rescale (hyc_set_conserve)
+  double *d_cons = nullptr;     // its row sums and factors
+  size_t cons_elems = 0;
   size_t scratch_elems = 0;
   unsigned char *d_fct2c = nullptr;  // advem_fct2c work arrays (per (field, layer) pair)
   size_t fct2c_bytes = 0;
@@ -166,6 +169,24 @@ void fct2c_bind(hyc::Fct2cArgs &f, const hyc_ctx *c, int npair) {
   f.lcalc = c->d_fct2c + (size_t)npair * sl * 13 * sizeof(double);
 }
 
+// the lconserve rescale of one tile launch: a.cfac is set for its copy back
+int conserve(hyc_ctx *c, hyc::TileArgs &a, int nlayers) {
+  const size_t rows = hyc::conserve_rows_elems(a.nfld, a.kdm, a.jj), need = rows + (size_t)a.nfld * a.kdm;
+  if (c->cons_elems < need) {
+    cudaFree(c->d_cons);
+    c->d_cons = nullptr;
+    c->cons_elems = 0;
+    cudaError_t e = cudaMalloc(&c->d_cons, need * sizeof(double));
+    if (e != cudaSuccess) return fail(c, HYC_ERR_NOMEM, "lconserve work: %s", cudaGetErrorString(e));
+    c->cons_elems = need;
+  }
+  cudaError_t e = hyc::launch_conserve(a, nlayers, c->d_cons, c->d_cons + rows, c->stream);
+  if (e != cudaSuccess) return fail(c, HYC_ERR_CUDA, "lconserve: %s", cudaGetErrorString(e));
+  c->stats.launches += 2;
+  a.cfac = c->d_cons + rows;
+  return HYC_OK;
+}
+
 int ensure_scratch(hyc_ctx *c, size_t elems) {
   if (c->scratch_elems >= elems) return HYC_OK;
   if (c->d_scratch) cudaFree(c->d_scratch);
@@ -245,6 +266,12 @@ void fold_timings(hyc_ctx *c) {
 void hyc::set_library_error(const char *msg) { g_lib_error = msg ? msg : ""; }
 
 extern "C" {
+
+int hyc_set_conserve(hyc_ctx *c, int32_t on) {
+  if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
+  c->lconserve = on != 0;
+  return HYC_OK;
+}
 
 int hyc_enable_timers(hyc_ctx *c, int32_t on) {
   if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
@@ -432,6 +459,7 @@ int hyc_adv_finalize(hyc_ctx *c) {
     cudaFree(c->d_cnkeys);
     cudaFree(c->d_scratch);
     cudaFree(c->d_iso);
+    cudaFree(c->d_cons);
     cudaFree(c->d_fct2c);
     cudaFree(c->d_tmp);
     cudaFree(c->d_keys);
@@ -554,6 +582,8 @@ int hyc_advem(hyc_ctx *c, int32_t advtyp, double *fld, const double *fldc, const
     dscali = c->d_tmp + 7 * sl;
   }
   if (advtyp == 2 && btrmas) {  // advem_fct2c, mod_tsadvc.F90:154-155
+    if (c->lconserve)  // advem_fct2c forms no fldao/fldan (mod_tsadvc.F90:999-1368)
+      return fail(c, HYC_ERR_UNSUPPORTED, "lconserve with advem_fct2c (btrmas) is not supported");
     if (c->nreg < 0)
       return fail(c, HYC_ERR_UNSUPPORTED, "advem_fct2c refreshes halos in mid-scheme: not with external halos");
     int rc = ensure_fct2c(c, hyc::fct2c_work_bytes(sl));
@@ -624,6 +654,7 @@ int hyc_advem(hyc_ctx *c, int32_t advtyp, double *fld, const double *fldc, const
     Timed t(c, HYC_T_ADVECT);
     CK(hyc::launch_advect_tiles(advtyp, a, 1, c->shape, c->stream), "advem kernel");
   }
+  if (c->lconserve && (rc = conserve(c, a, 1))) return rc;
   CK(hyc::launch_copy_back(a, 1, c->stream), "advem copy");
   c->stats.launches += 2;
   if (where == HYC_HOST)
@@ -643,6 +674,8 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
     return fail(c, HYC_ERR_ARG, "isopycnic mode is nhybrd = 0 (no hybrid layers)");
   if (p->isopyc && at == 2 && p->btrmas)
     return fail(c, HYC_ERR_UNSUPPORTED, "isopycnic flux smoothing with advem_fct2c (btrmas) is not supported");
+  if (c->lconserve && at == 2 && p->btrmas)  // advem_fct2c forms no fldao/fldan (mod_tsadvc.F90:999-1368)
+    return fail(c, HYC_ERR_UNSUPPORTED, "lconserve with advem_fct2c (btrmas) is not supported");
   if (p->ntracr < 0 || (p->ntracr > 0 && !p->trcflg)) return fail(c, HYC_ERR_ARG, "ntracr/trcflg");
   const int kk = c->kdm;
   const long long sl = c->slice;
@@ -822,11 +855,14 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
       {
         Timed t(c, HYC_T_ADVECT);
         CK(hyc::launch_advect_tiles(at, a, nlay, c->shape, s), "advect kernel");
+        int rc2;
+        if (c->lconserve && (rc2 = conserve(c, a, nlay))) return rc2;
       }
       {
         Timed t(c, HYC_T_COPY);
         CK(hyc::launch_copy_back(a, nlay, s), "copy back");
       }
+      a.cfac = nullptr;
       c->stats.launches += 2;
     }
     return HYC_OK;

@@ -23,8 +23,14 @@ size_t advect_tiles_smem(TileShape shape);
 bool advect_tile_shape_ok(TileShape shape);
 
 // Copy the interior of out[(fi*kdm+k)] back into field level n for every
-// (field, layer) the launch processed.
+// (field, layer) the launch processed (times a.cfac[fi*kdm+k] when set).
 cudaError_t launch_copy_back(const TileArgs &a, int nlayers, cudaStream_t s);
+
+// advem's conservation rescale (lconserve): the factors a.cfac for the
+// pairs of a tile launch, from the old level n and the new values in
+// a.out; rows holds conserve_rows_elems(nfld, kdm, jj) doubles
+size_t conserve_rows_elems(int nfld, int kdm, int jj);
+cudaError_t launch_conserve(const TileArgs &a, int nlayers, double *rows, double *fac, cudaStream_t s);
 
 struct Fct2cArgs;
 // advem_fct2c: work bytes per (field, layer) pair; the stages of one call

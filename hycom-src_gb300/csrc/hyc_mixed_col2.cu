@@ -11,10 +11,9 @@
 // block holds, per row, the old and centre levels of the pass's tracers,
 // uflx, vflx (FP32), dp (FP64) and the per-cell word (dt2*scp2i in FP64
 // with ip, iu, iv in its three lowest mantissa bits) -- one
-// cp.async.bulk.tensor per array, one mbarrier per slot.  The streams are
-// loaded with an L2 evict-first policy, so the per-cell words, which every
-// layer of a strip reads again, stay in L2.  Out-of-range rows and columns
-// arrive as zeros (TMA fill), so the kernel has no bounds tests on loads.
+// cp.async.bulk.tensor per array, one mbarrier per slot.  Out-of-range rows
+// and columns arrive as zeros (TMA fill), so the kernel has no bounds tests
+// on loads.
 //
 // Compute: the stage pipeline of mod_tsadvc.F90:645-997 runs in registers --
 // at row J the lane forms the low-order fluxes of row J (:686-720), the
@@ -216,9 +215,6 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     tma::fence_bar_init();
   }
   __syncwarp();
-  // L2 policies: the streams are read once per item (evict first), the
-  // per-cell words by every layer chunk of the strip (default)
-  const uint64_t pol_stream = tma::policy_evict_first();
   uint32_t tg = 0;  // blocks this warp has consumed (slot and phase of the next one)
   const float onemu = (float)kOnemu;
   const float2 onemu2 = make_float2(onemu, onemu);
@@ -258,12 +254,12 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
 #pragma unroll
       for (int q = 0; q < NQ; q++) {
         const int qq = min(qp * NQ + q, ntr - 1);
-        tma::load3h(slot + RG::OFF_FO + q * kRB * RG::FROW, B.c2_old, b, s0, y, qq * kdm + k, pol_stream);
-        if (!MP) tma::load3h(slot + RG::OFF_FC + q * kRB * RG::FROW, B.c2_cur, b, s0, y, qq * kdm + k, pol_stream);
+        tma::load3(slot + RG::OFF_FO + q * kRB * RG::FROW, B.c2_old, b, s0, y, qq * kdm + k);
+        if (!MP) tma::load3(slot + RG::OFF_FC + q * kRB * RG::FROW, B.c2_cur, b, s0, y, qq * kdm + k);
       }
-      tma::load3h(slot + RG::OFF_U, B.c2_u, b, s0, y, k, pol_stream);
-      tma::load3h(slot + RG::OFF_V, B.c2_v, b, s0, y, k, pol_stream);
-      tma::load3h(slot + RG::OFF_DP, B.c2_dp, b, s0, y, k, pol_stream);
+      tma::load3(slot + RG::OFF_U, B.c2_u, b, s0, y, k);
+      tma::load3(slot + RG::OFF_V, B.c2_v, b, s0, y, k);
+      tma::load3(slot + RG::OFF_DP, B.c2_dp, b, s0, y, k);
       tma::load2(slot + RG::OFF_CG, B.c2_cg, b, s0, y);
     };
     if (lane == 0)

@@ -66,20 +66,5 @@ __device__ __forceinline__ void load2(void *dst, const CUtensorMap *map, uint64_
       : "memory");
 }
 
-// L2 eviction-priority policy for the cache-hinted loads below
-__device__ __forceinline__ uint64_t policy_evict_first() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ void load3h(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y, int z,
-                                       uint64_t policy) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
-      " [%0], [%1, {%2, %3, %4}], [%5], %6;" ::"r"(sa(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(z), "r"(sa(bar)), "l"(policy)
-      : "memory");
-}
-
 }  // namespace tma
 }  // namespace hyc

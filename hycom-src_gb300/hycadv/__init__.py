@@ -44,7 +44,7 @@ FIELDS = {"temp": 0, "saln": 1, "th3d": 2, "tracer": 3, "uflx": 4, "vflx": 5, "d
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "hyc_set_stream", "hyc_bind_field",
            "hyc_sync_field", "hyc_synchronize", "hyc_tsadvc", "hyc_advem", "hyc_xctilr", "hyc_mass_sum",
-           "hyc_version", "hyc_enable_timers", "hyc_get_stats", "hyc_advem_noalloc", "hyc_ens_create",
+           "hyc_version", "hyc_enable_timers", "hyc_set_conserve", "hyc_get_stats", "hyc_advem_noalloc", "hyc_ens_create",
            "hyc_ens_destroy", "hyc_ens_set_stream", "hyc_ens_put", "hyc_ens_get",
            "hyc_ens_put_slices", "hyc_ens_get_slices", "hyc_ens_set_tile",
            "hyc_ens_tune", "hyc_ens_step", "hyc_ens_content", "hyc_ens_stats", "hyc_ens_enable_timers",
@@ -121,6 +121,7 @@ def lib() -> C.CDLL:
         L.hyc_tsdff.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(TsadvcParams), C.c_double, C.c_double,
                                 C.c_double]
         L.hyc_enable_timers.argtypes = [vp, C.c_int32]
+        L.hyc_set_conserve.argtypes = [vp, C.c_int32]
         L.hyc_get_stats.argtypes = [vp, C.POINTER(Stats), C.c_int32]
         L.hyc_ens_create.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(BasinSpec), C.c_int32, C.c_int32]
         L.hyc_ens_destroy.argtypes = [vp]
@@ -419,6 +420,10 @@ class Context(_StreamFollower):
 
     def enable_timers(self, on: bool = True):
         _check(lib().hyc_enable_timers(self._h, int(bool(on))), self._h)
+
+    def set_conserve(self, on: bool = True):
+        """advem's explicit conservation rescale (mod_tsadvc.F90:32, :168-203)."""
+        _check(lib().hyc_set_conserve(self._h, int(bool(on))), self._h)
 
     def stats(self, reset: bool = False) -> dict:
         """Kernel launches and device-time per timer slot (ms, calls)."""

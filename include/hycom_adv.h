@@ -336,6 +336,17 @@ typedef struct hyc_stats {
   double ms[HYC_NTIMERS];      /* accumulated device milliseconds       */
 } hyc_stats;
 
+/*
+ * advem's explicit conservation switch (mod_tsadvc.F90:32, lconserve,
+ * .false. as shipped; the rescale at :168-203).  on = 1: after every
+ * advem of hyc_tsadvc and hyc_advem, the tracer contents before and after,
+ * sum(fld_old*fco*scp2) and sum(fld_new*fcn*scp2) over the interior sea
+ * points, are summed in xcsum's order (mod_xc_sm.h:900-963) and the new
+ * values at sea points are multiplied by 1 + (old-new)/new, bit for bit as
+ * the reference does.  Not available with advem_fct2c (btrmas with FCT2),
+ * whose scheme forms no such contents (HYC_ERR_UNSUPPORTED).
+ */
+int hyc_set_conserve(hyc_ctx *ctx, int32_t on);
 int hyc_enable_timers(hyc_ctx *ctx, int32_t on);
 /* Wait for the stream, fold finished timings in, copy out; reset=1 zeroes. */
 int hyc_get_stats(hyc_ctx *ctx, hyc_stats *out, int32_t reset);

@@ -74,6 +74,7 @@ typedef struct hyo_grid {
      face a sea cell touches, as geopar.F90:833 leaves them */
   double *uflux2, *vflux2;
   int nthreads; /* 0 = OpenMP default */
+  int lconserve; /* advem's explicit conservation rescale, mod_tsadvc.F90:32 (.false. as shipped) */
 } hyo_grid;
 
 #define P(g, i, j) ((size_t)((i) + (g)->nbdy - 1) + (size_t)((j) + (g)->nbdy - 1) * (size_t)(g)->ld1)
@@ -107,6 +108,7 @@ static double *nan_array(size_t n) {
 }
 
 void hyo_set_threads(hyo_grid *g, int n) { g->nthreads = n; }
+void hyo_set_conserve(hyo_grid *g, int on) { g->lconserve = on != 0; }
 
 static int nthr(const hyo_grid *g) {
 #ifdef _OPENMP
@@ -1191,8 +1193,11 @@ static void advem_fct2c(hyo_grid *g, double *fld, const double *fldc, const doub
     }
 }
 
+double hyo_xcsum(const hyo_grid *g, const double *a, const int32_t *mask);
+
 /* ------------------------------------------------------------------ */
-/* advem: mod_tsadvc.F90:69-205 (lconserve=.false., :32)                */
+/* advem: mod_tsadvc.F90:69-205; with lconserve (:32, .false. as       */
+/* shipped) the rescale of :168-203 follows the scheme                 */
 /* ------------------------------------------------------------------ */
 int hyo_advem(hyo_grid *g, int advtyp, double *fld, const double *fldc, const double *u, const double *v,
               const double *fco, const double *fcn, double posdef, const double *scal, const double *scali,
@@ -1209,6 +1214,16 @@ int hyo_advem(hyo_grid *g, int advtyp, double *fld, const double *fldc, const do
     advem_fct4(g, fld, fldc, u, v, fco, fcn, scal, scali, dt2);
   else
     return HYO_ERR_ADVTYP;
+  if (g->lconserve) { /* :168-188; ipa = ip without ice shelf or tripole (geopar.F90:427-437) */
+    const double sumold = hyo_xcsum(g, g->fldao, g->ip);
+    const double sumnew = hyo_xcsum(g, g->fldan, g->ip);
+    const double offset = sumnew != 0.0 ? (sumold - sumnew) / sumnew : 0.0;
+    for (int j = 1; j <= g->jj; j++)
+      for (int i = 1; i <= g->ii; i++) {
+        const size_t c = P(g, i, j);
+        if (g->ip[c] != 0) fld[c] = fld[c] * (1.0 + offset);
+      }
+  }
   return HYO_OK;
 }
 

@@ -44,6 +44,7 @@ def lib():
         L.hyo_grid_masks.argtypes = [C.c_void_p] + [ip] * 7
         L.hyo_grid_work.argtypes = [C.c_void_p, C.c_char_p, dp]
         L.hyo_set_threads.argtypes = [C.c_void_p, C.c_int]
+        L.hyo_set_conserve.argtypes = [C.c_void_p, C.c_int]
         L.hyo_max_threads.restype = C.c_int
         L.hyo_xctilr.argtypes = [C.c_void_p, dp, C.c_int, C.c_int, C.c_int]
         L.hyo_advem.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp, dp, C.c_double, dp, dp, C.c_double, C.c_int]
@@ -149,6 +150,10 @@ class Grid:
 
     def set_threads(self, n: int):
         lib().hyo_set_threads(self._h, int(n))
+
+    def set_conserve(self, on: bool):
+        """advem's explicit conservation rescale (mod_tsadvc.F90:32, :168-203)."""
+        lib().hyo_set_conserve(self._h, int(bool(on)))
 
     def xctilr(self, a: np.ndarray, mh: int, nh: int):
         nlev = int(np.prod(a.shape[:-2])) if a.ndim > 2 else 1

@@ -396,7 +396,8 @@ def test_tsadvc_isopycnic_bit_for_bit(cuda, advtyp, periodic):
     oracle_steps(g, c, range(1, 4), advtyp, trcflg=tf, q2=c["q2"], q2l=c["q2l"], **kw)
     gpu_steps(ctx, t, range(1, 4), advtyp, ntracr=2, trcflg=tf, **kw)
     compare(c, t, keys=("temp", "saln", "th3d", "tracer", "q2", "q2l"))
-    assert np.array_equal(c["temp"], temp0)  # temperature is not advected in isopycnic mode
+    # temperature is not advected in isopycnic mode (its halo is refreshed)
+    assert np.array_equal(c["temp"][..., b.J, b.I], temp0[..., b.J, b.I])
     # the smoothing changes layer 1: the same step with hybrid layers differs
     c2 = np_case(b, g, kdm=kdm, ntracr=0, seed=131, courant=0.7, delt1=600.0)
     c2["delt1"] = 600.0
@@ -420,3 +421,52 @@ def test_tsadvc_isopycnic_rejects_fct2c(cuda):
         ctx.tsadvc(1, 2, delt1=600.0, advtyp=2, btrmas=True, isopyc=True, nhybrd=0)
     with pytest.raises(hycadv.HycError):
         ctx.tsadvc(1, 2, delt1=600.0, advtyp=2, isopyc=True, nhybrd=2)
+
+
+@pytest.mark.parametrize("advtyp", SCHEMES)
+def test_tsadvc_lconserve_bit_for_bit(cuda, advtyp):
+    """advem's explicit conservation rescale (lconserve, mod_tsadvc.F90:168-203):
+    xcsum-ordered content sums before and after each advem, new values at
+    sea points scaled by 1 + (old-new)/new; equal to the oracle bit for bit,
+    and different from the run without it."""
+    b = basin(70, 52, True, seed=141)
+    g = oracle_grid(b)
+    g.set_conserve(True)
+    c = np_case(b, g, kdm=3, ntracr=1, seed=141, courant=0.7, delt1=600.0)
+    c["delt1"] = 600.0
+    tf = np.array([0], np.int32)
+    plain = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in c.items()}
+    t = torchify(c, cuda)
+    ctx = make_ctx(b, g, 3)
+    ctx.set_conserve(True)
+    bind_all(ctx, t)
+    oracle_steps(g, c, range(1, 4), advtyp, trcflg=tf)
+    gpu_steps(ctx, t, range(1, 4), advtyp, ntracr=1, trcflg=tf)
+    compare(c, t)
+    g.set_conserve(False)
+    oracle_steps(g, plain, range(1, 4), advtyp, trcflg=tf)
+    assert not np.array_equal(plain["saln"], c["saln"])
+
+
+def test_advem_lconserve_slice(cuda):
+    """hyc_advem on one slice with the rescale, host pointers, FCT2."""
+    b = basin(64, 48, False, seed=142)
+    g = oracle_grid(b)
+    g.set_conserve(True)
+    c = np_case(b, g, kdm=1, ntracr=0, seed=142, courant=0.7, delt1=600.0)
+    ctx = make_ctx(b, g, 1)
+    ctx.set_conserve(True)
+    fld = c["temp"][1, 0].copy()
+    fldc = c["temp"][0, 0].copy()
+    u, v = c["uflx"][0].copy(), c["vflx"][0].copy()
+    for a in (fld, fldc, u, v):
+        g.xctilr(a, 5, 5)
+    fco = np.maximum(c["dp"][1, 0] * 1.02, 0.0)
+    fcn = c["dp"][1, 0].copy()
+    ref = fld.copy()
+    g.advem(2, ref, fldc, u, v, fco, fcn, 0.0, c["scp2"], c["scp2i"], 600.0)
+    got = fld.copy()
+    ctx.advem(2, got, fldc, u, v, fco, fcn, 0.0, c["scp2"], c["scp2i"], 600.0)
+    assert same(got, ref)
+    with pytest.raises(hycadv.HycError):  # advem_fct2c forms no content arrays
+        ctx.advem(2, got, fldc, u, v, fco, fcn, 0.0, c["scp2"], c["scp2i"], 600.0, btrmas=True)

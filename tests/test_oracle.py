@@ -261,3 +261,40 @@ def test_oracle_rejects_bad_advtyp(closed):
     a = np.zeros((b.ld2, b.ld1))
     with pytest.raises(O.OracleError):
         g.advem(3, a, a, a, a, a, a, 0.0, a, a, 1.0)
+
+
+def test_oracle_lconserve_restores_content():
+    """With advem's rescale (lconserve) the content sum(fld*fcn*scp2) after a
+    step equals the sum(fld*fco*scp2) before it to round-off (the FCT2 step
+    alone conserves only to its own round-off plus the coastal-quirk
+    imbalance); the rescale is a sea-point scaling by one factor."""
+    import numpy as np
+
+    from helpers import basin, np_case, oracle_grid
+
+    b = basin(60, 45, False, seed=143)
+    g = oracle_grid(b)
+    c = np_case(b, g, kdm=1, ntracr=0, seed=143, courant=0.7, delt1=600.0)
+    fld = c["saln"][1, 0].copy()
+    fldc = c["saln"][0, 0].copy()
+    u, v = c["uflx"][0].copy(), c["vflx"][0].copy()
+    for a in (fld, fldc, u, v):
+        g.xctilr(a, 5, 5)
+    dpn = c["dp"][1, 0]
+    fd = np.zeros_like(dpn)
+    fd[:-1, :-1] = ((u[:-1, 1:] - u[:-1, :-1]) + (v[1:, :-1] - v[:-1, :-1])) * 600.0 * c["scp2i"][:-1, :-1]
+    fco = np.maximum(dpn + fd, 0.0)
+    fcn = np.maximum(dpn, 0.0)
+    ip = g.masks["ip"]
+    before = g.xcsum(fld * fco * c["scp2"], ip)
+    plain = fld.copy()
+    g.advem(2, plain, fldc, u, v, fco, fcn, 0.0, c["scp2"], c["scp2i"], 600.0)
+    g.set_conserve(True)
+    fixed = fld.copy()
+    g.advem(2, fixed, fldc, u, v, fco, fcn, 0.0, c["scp2"], c["scp2i"], 600.0)
+    after = g.xcsum(fixed * fcn * c["scp2"], ip)
+    assert abs(after - before) <= 1e-14 * abs(before)
+    sea = ip != 0
+    ratio = fixed[sea] / plain[sea]
+    assert np.allclose(ratio, ratio[0], rtol=0, atol=1e-15)
+    assert np.array_equal(fixed[~sea], plain[~sea])
