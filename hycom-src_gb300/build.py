@@ -36,6 +36,7 @@ UNITS = {
     "hyc_ens_util.cu": ["-lineinfo"],
     "hyc_ens_host.cpp": [],
     "hyc_za.cpp": [],
+    "hyc_tmap.cpp": [],
 }
 
 

@@ -37,6 +37,15 @@ struct TileArgs {
   // advem's conservation rescale (lconserve): per (field, layer) factor
   // 1 + offset applied by the copy back, index fi*kdm + k; null: none
   const double *cfac;
+  // TMA staging of the tile region (null: plain loads): CUtensorMap array
+  // in device memory, FP64, box (TX+8) x (TY+6):
+  //   [0] uflx, [1] vflx (slice k of the layer; advem: the one slice),
+  //   [2] dp(:,:,:,n) (advem: fcn), [3] onetamas(m) (advem: fco; tm_has3 = 0
+  //   when absent), [4] scal, [5] scali, then [6 + 2*fi] level n and
+  //   [7 + 2*fi] level m of field fi (slice k + k_off)
+  const void *tmaps;
+  int tm_has3;
+  int *err;  // set when a bounded TMA wait gave up (may be null)
   // advem mode (single slice)
   const double *fco, *fcn;
   double dt2;
@@ -125,12 +134,25 @@ struct CnuityArgs {
   long long *keys;                  // 2*kdm dpkmin keys, or null
 };
 
+// Region of the generic tile kernel: RW x RY cells (TX x TY output cells and
+// a 3-cell ring), rows stored RX apart.  RX = TX + 8 (an even count of
+// doubles: TMA boxes of 16-byte rows starting on an even column, the region
+// at offset 0 or 1 in each array's slot) when the arrays then fit in shared
+// memory, else TX + 6 and plain loads only.
 template <int TX, int TY>
 struct TileGeom {
-  static constexpr int RX = TX + 6, RY = TY + 6, N = RX * RY;
   // per-layer arrays: U V FCO FCN HN RH SCAL SCALI ; per-field: FLD FLDC FX FY FLO FXL FNL RP RM QX QN
-  static constexpr int NLAYER = 8, NFIELD = 11;
-  static constexpr size_t smem_bytes = (size_t)(NLAYER + NFIELD) * N * sizeof(double) + ((N + 15) / 16) * 16;
+  static constexpr int NLAYER = 8, NFIELD = 11, NARR = NLAYER + NFIELD;
+  static constexpr int RW = TX + 6, RY = TY + 6;
+  static constexpr int slot(int rx) { return (rx * RY + 1 + 15) / 16 * 16; }
+  static constexpr size_t bytes(int rx) {
+    return 128 + (size_t)NARR * slot(rx) * sizeof(double) + (size_t)((rx * RY + 15) / 16) * 16;
+  }
+  static constexpr bool TMA = bytes(TX + 8) <= 227 * 1024;
+  static constexpr int RX = TMA ? TX + 8 : TX + 6;
+  static constexpr int NR = RX * RY, N = slot(RX);
+  static constexpr unsigned BOX = NR * 8;  // bytes of one TMA box
+  static constexpr size_t smem_bytes = bytes(RX);
 };
 
 }  // namespace hyc

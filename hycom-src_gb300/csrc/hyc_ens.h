@@ -26,7 +26,7 @@ struct MixBasin {
   float posdef[kMaxFields];  // MPDATA offset of each tracer (mod_tsadvc.F90:1755-1763)
   // TMA maps (box 64 x 4 rows, device memory): levels t-1 and t (3-D, ld1 x
   // ld2 x ntr*kdm, FP32), uflx, vflx (FP32), dp (FP64) and the per-cell
-  // words (2-D, FP64)
+  // words (one slice, FP64)
   const CUtensorMap *c2_old, *c2_cur, *c2_u, *c2_v, *c2_dp, *c2_cg;
 };
 

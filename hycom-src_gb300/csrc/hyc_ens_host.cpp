@@ -16,6 +16,7 @@
 #include "hyc_args.h"
 #include "hyc_ens.h"
 #include "hyc_internal.h"
+#include "hyc_tmap.h"
 
 using hyc::MixBasin;
 using hyc::TileArgs;
@@ -50,6 +51,8 @@ struct hyc_ens {
   int maxntr = 1;        // largest tracer count
   int strip_nq = 2;      // strip kernel: tracers per pass (1 or 2)
   CUtensorMap *d_cmaps = nullptr;  // [nbasin][kMaps]: strip kernel maps (levels 0-2, u, v, dp, cell words)
+  CUtensorMap *d_fmaps = nullptr;  // FP64 form: the FCT tile kernel's maps, 3 rotations x basins
+  size_t fmaps_cap = 0;
   int *d_err = nullptr;            // device error flag (bounded waits that gave up)
   // device tables, one per rotation
   MixBasin *d_mix[3] = {nullptr, nullptr, nullptr};
@@ -164,6 +167,7 @@ void free_all(hyc_ens *e) {
   if (e->copy_stream) cudaStreamDestroy(e->copy_stream);
   if (e->in_stream) cudaStreamDestroy(e->in_stream);
   cudaFree(e->d_cmaps);
+  cudaFree(e->d_fmaps);
   cudaFree(e->d_err);
   if (e->gexec) cudaGraphExecDestroy(e->gexec);
   for (auto &p : e->pending) {
@@ -172,62 +176,21 @@ void free_all(hyc_ens *e) {
   }
 }
 
-// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-  }
-  return fn;
-}
-
-// 3-D tiled map over nz slices of (ld1 x ld2) elements, box (bx, by, 1)
-bool encode3t(CUtensorMap *m, void *base, CUtensorMapDataType dt, size_t es, int ld1, int ld2, long long nz, int bx,
-              int by) {
-  EncodeTiledFn fn = encode_fn();
-  if (!fn) return false;
-  cuuint64_t dims[3] = {(cuuint64_t)ld1, (cuuint64_t)ld2, (cuuint64_t)nz};
-  cuuint64_t strides[2] = {(cuuint64_t)ld1 * es, (cuuint64_t)ld1 * ld2 * es};
-  cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
-  cuuint32_t estr[3] = {1, 1, 1};
-  return fn(m, dt, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-// 2-D tiled map over one (w x ld2) slice, box (bx, by)
-bool encode2t(CUtensorMap *m, void *base, CUtensorMapDataType dt, size_t es, int w, int ld2, int bx, int by) {
-  EncodeTiledFn fn = encode_fn();
-  if (!fn) return false;
-  cuuint64_t dims[2] = {(cuuint64_t)w, (cuuint64_t)ld2};
-  cuuint64_t strides[1] = {(cuuint64_t)w * es};
-  cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
-  cuuint32_t estr[2] = {1, 1};
-  return fn(m, dt, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 // maps of the two-column strip kernel; they depend only on the allocations
 int encode_strip_maps(hyc_ens *e) {
   const int bx = hyc::kCol2Box, by = hyc::kCol2Rows;
-  const CUtensorMapDataType F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32, F64 = CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
   std::vector<CUtensorMap> h(e->b.size() * kMaps);
   for (size_t i = 0; i < e->b.size(); i++) {
     EBasin &b = e->b[i];
     CUtensorMap *m = &h[i * kMaps];
     bool ok = true;
-    for (int l = 0; l < 3; l++) ok &= encode3t(m + l, b.lev[l], F32, 4, b.ld1, b.ld2, (long long)b.ntr * b.kdm, bx, by);
-    ok &= encode3t(m + 3, b.uflx, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
-    ok &= encode3t(m + 4, b.vflx, F32, 4, b.ld1, b.ld2, b.kdm, bx, by);
-    ok &= encode3t(m + 5, b.dp, F64, 8, b.ld1, b.ld2, b.kdm, bx, by);
-    ok &= encode2t(m + 6, b.cell, F64, 8, b.ld1, b.ld2, bx, by);
+    // widths are the pitch: the padding columns are zeros, as out of range
+    for (int l = 0; l < 3; l++)
+      ok &= hyc::tmap_encode3(m + l, b.lev[l], 4, b.ld1, b.ld2, b.ld1, b.slice, (long long)b.ntr * b.kdm, bx, by);
+    ok &= hyc::tmap_encode3(m + 3, b.uflx, 4, b.ld1, b.ld2, b.ld1, b.slice, b.kdm, bx, by);
+    ok &= hyc::tmap_encode3(m + 4, b.vflx, 4, b.ld1, b.ld2, b.ld1, b.slice, b.kdm, bx, by);
+    ok &= hyc::tmap_encode3(m + 5, b.dp, 8, b.ld1, b.ld2, b.ld1, b.slice, b.kdm, bx, by);
+    ok &= hyc::tmap_encode3(m + 6, b.cell, 8, b.ld1, b.ld2, b.ld1, b.slice, 1, bx, by);
     if (!ok) return efail(e, HYC_ERR_CUDA, "cuTensorMapEncodeTiled failed for the strip maps (basin %zu)", i);
   }
   ECK(cudaMemcpy(e->d_cmaps, h.data(), h.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "strip maps copy");
@@ -321,6 +284,54 @@ int build_tables(hyc_ens *e, double dt2) {
         a.out = (double *)b.lev[ln];
         a.kdm = b.kdm;
         a.images = b.nreg == 1 ? std::min(5, b.nbdy) : 0;
+      }
+      // TMA maps of the FCT tile kernel (box tx+8 x ty+6): uflx, vflx, dp,
+      // (no onetamas), scp2, scp2i, then levels t-1 and t of each tracer
+      if (r == 0) {
+        size_t need = 0;
+        for (const auto &b : e->b) need += 3 * (6 + 2 * (size_t)b.ntr);
+        if (e->fmaps_cap < need) {
+          cudaFree(e->d_fmaps);
+          e->d_fmaps = nullptr;
+          e->fmaps_cap = 0;
+          ECK(cudaMalloc(&e->d_fmaps, need * sizeof(CUtensorMap)), "fp64 tensor maps");
+          e->fmaps_cap = need;
+        }
+      }
+      {
+        std::vector<CUtensorMap> h;
+        size_t base = 0;  // the rotations' maps one after another
+        for (int rr = 0; rr < r; rr++)
+          for (const auto &b : e->b) base += 6 + 2 * (size_t)b.ntr;
+        const int bx = e->shape.tx + 8, by = e->shape.ty + 6;
+        size_t at = base;
+        for (int i = 0; i < nb; i++) {
+          const EBasin &b = e->b[i];
+          const long long w = b.idm + 2LL * b.nbdy, hh = b.jdm + 2LL * b.nbdy;
+          std::vector<CUtensorMap> m(6 + 2 * (size_t)b.ntr);
+          bool ok = hyc::tmap_available();
+          auto enc = [&](CUtensorMap *p, const void *ptr, long long nz) {
+            ok = ok && hyc::tmap_encode3(p, ptr, 8, w, hh, b.ld1, b.slice, nz, bx, by);
+          };
+          enc(&m[0], b.uflx, b.kdm);
+          enc(&m[1], b.vflx, b.kdm);
+          enc(&m[2], b.dp, b.kdm);
+          enc(&m[4], b.scp2, 1);
+          enc(&m[5], b.scp2i, 1);
+          for (int q = 0; q < b.ntr; q++) {
+            enc(&m[6 + 2 * q], t[i].f[q].nbase, b.kdm);
+            enc(&m[7 + 2 * q], t[i].f[q].mbase, b.kdm);
+          }
+          if (ok) {
+            t[i].tmaps = e->d_fmaps + at;
+            t[i].tm_has3 = 0;
+          }
+          t[i].err = e->d_err;
+          h.insert(h.end(), m.begin(), m.end());
+          at += m.size();
+        }
+        ECK(cudaMemcpy(e->d_fmaps + base, h.data(), h.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice),
+            "fp64 tensor maps copy");
       }
       ECK(cudaMemcpy(e->d_targs[r], t.data(), nb * sizeof(TileArgs), cudaMemcpyHostToDevice), "fp64 table");
       e->h_targs[r] = t;
@@ -531,7 +542,7 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
   if (cudaMalloc(&e->d_err, sizeof(int)) != cudaSuccess || cudaMemset(e->d_err, 0, sizeof(int)) != cudaSuccess)
     return bail(efail(nullptr, HYC_ERR_NOMEM, "error flag"));
   if (precision == HYC_PREC_MIXED) {  // the strip kernel streams its rows by TMA
-    if (!encode_fn())
+    if (!hyc::tmap_available())
       return bail(efail(nullptr, HYC_ERR_UNSUPPORTED, "the mixed form needs cuTensorMapEncodeTiled (driver)"));
     if (cudaMalloc(&e->d_cmaps, nbasin * kMaps * sizeof(CUtensorMap)) != cudaSuccess)
       return bail(efail(nullptr, HYC_ERR_NOMEM, "strip maps"));

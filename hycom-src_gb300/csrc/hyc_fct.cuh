@@ -10,18 +10,33 @@
 //   * fco+onemu is formed once per cell (the reference forms it per field);
 //   * the stage loops have compile-time bounds and are unrolled, so a
 //     thread's cells interleave (more independent FP64 work in flight).
-// Only sea cells of the interior are written to the output slice.
+// The region is staged by TMA (cp.async.bulk.tensor, one box per array and
+// one mbarrier, every wait bounded) when the launch carries tensor maps,
+// else by plain loads.  Only sea cells of the interior are written to the
+// output slice.
 #pragma once
+#include <cuda.h>
+
 #include "hyc_args.h"
 #include "hyc_device.cuh"
+#include "hyc_tma.cuh"
 
 namespace hyc {
 
+// The region is RW x RY cells (the TX x TY output cells and a 3-cell ring).
+// Its rows are stored RX = TX + 8 doubles apart, an even count, so that a
+// TMA box row is a multiple of 16 bytes and the box can start on the even
+// padded column at or before the region's first one (x coordinates of a
+// box must be even for 8-byte elements); the region then sits at offset
+// off = 0 or 1 in each array's slot.
 template <int TX, int TY>
 struct FctGeom {
-  static constexpr int RX = TX + 6, RY = TY + 6, N = RX * RY;
+  static constexpr int RW = TX + 6, RX = TX + 8, RY = TY + 6;
+  static constexpr int NR = RX * RY;                     // cells of a staged box
+  static constexpr int N = (NR + 1 + 15) / 16 * 16;      // one array's slot (128-byte multiple)
   static constexpr int NARR = 15;  // U V FCN HO HN RH SCL SCI | FLD FLDC FX FY FLO RP RM
-  static constexpr size_t smem_bytes = (size_t)NARR * N * sizeof(double) + ((N + 15) / 16) * 16;
+  static constexpr unsigned BOX = NR * 8;                // bytes of one TMA box
+  static constexpr size_t smem_bytes = 128 + (size_t)NARR * N * sizeof(double) + ((NR + 15) / 16) * 16;
 };
 
 // Compile-time rectangle [A0,A1) x [B0,B1) of a region of width RX, spread
@@ -43,29 +58,67 @@ __device__ __forceinline__ void rect(F &&f) {
 }
 
 // One tile (tile index, 0-based layer k) of one basin; sm is the CTA's
-// dynamic shared memory (FctGeom<TX,TY>::smem_bytes).
+// dynamic shared memory (FctGeom<TX,TY>::smem_bytes), bar its mbarrier and
+// ph the count of the mbarrier's completed phases (uniform over the CTA).
+// False when a TMA wait gave up (A.err is set; the CTA stops).
 template <int SCHEME, int TX, int TY>
-__device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile, const int k, double *sm) {
+__device__ __forceinline__ bool fct_tile_body(const TileArgs &A, const int tile, const int k, double *sm,
+                                              uint64_t *bar, uint32_t &ph) {
   using G = FctGeom<TX, TY>;
-  constexpr int RX = G::RX, RY = G::RY, N = G::N;
+  constexpr int RX = G::RX, RW = G::RW, RY = G::RY, N = G::N, NR = G::NR;
   constexpr int NOUT_IT = (TX * TY + 255) / 256;
-  double *U = sm, *V = U + N, *FCN = V + N, *HO = FCN + N, *HN = HO + N, *RH = HN + N, *SCL = RH + N,
-         *SCI = SCL + N;
-  double *FLD = SCI + N, *FLDC = FLD + N, *FX = FLDC + N, *FY = FX + N, *FLO = FY + N, *RP = FLO + N,
-         *RM = RP + N;
-  uint8_t *MSK = reinterpret_cast<uint8_t *>(RM + N);
-
   const int tyi = tile / A.ntx, txi = tile - tyi * A.ntx;
   const int ib0 = 1 + txi * TX - 3, jb0 = 1 + tyi * TY - 3;  // region origin (Fortran index)
   const int nb = A.nbdy, ld1 = A.ld1, ii = A.ii, jj = A.jj;
+  const int x0 = ib0 + nb - 1, y0 = jb0 + nb - 1;  // padded column / row of the region origin
+  const int off = x0 & 1;                           // TMA boxes start at the even column x0 - off
+  double *sal = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(sm) + 127) & ~uintptr_t(127));
+  double *U = sal + off, *V = U + N, *FCN = V + N, *HO = FCN + N, *HN = HO + N, *RH = HN + N, *SCL = RH + N,
+         *SCI = SCL + N;
+  double *FLD = SCI + N, *FLDC = FLD + N, *FX = FLDC + N, *FY = FX + N, *FLO = FY + N, *RP = FLO + N,
+         *RM = RP + N;
+  uint8_t *MSK = reinterpret_cast<uint8_t *>(sal + G::NARR * N);
+  const CUtensorMap *tm = reinterpret_cast<const CUtensorMap *>(A.tmaps);
   const long long sl = A.slice;
   const double dt2 = A.dt2;
+  // all threads wait for the mbarrier's next phase; if any gave up, let the
+  // copies in flight land (bounded) and report failure
+  auto landed = [&]() -> bool {
+    const bool ok = tma::wait(bar, ph & 1u, A.err);
+    ph++;
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) tma::wait(bar, (ph - 1) & 1u, nullptr);
+      return false;
+    }
+    return true;
+  };
 
   // ---- per-layer inputs ------------------------------------------------------
-  {
+  if (tm) {
+    __syncthreads();  // the previous item's readers of these slots are done
+    if (threadIdx.x == 0) {
+      tma::fence_proxy_async();
+      const int zk = A.mode == 0 ? k : 0;
+      tma::expect_tx(bar, (A.tm_has3 ? 6u : 5u) * G::BOX);
+      tma::load3(U - off, tm + 0, bar, x0 - off, y0, zk);
+      tma::load3(V - off, tm + 1, bar, x0 - off, y0, zk);
+      tma::load3(FCN - off, tm + 2, bar, x0 - off, y0, zk);
+      if (A.tm_has3) tma::load3(HO - off, tm + 3, bar, x0 - off, y0, 0);
+      tma::load3(SCL - off, tm + 4, bar, x0 - off, y0, 0);
+      tma::load3(SCI - off, tm + 5, bar, x0 - off, y0, 0);
+    }
+    for (int t = threadIdx.x; t < NR; t += 256) {  // masks (bytes) by plain loads meanwhile
+      const int bb = t / RX, aa = t - bb * RX;
+      const int i = ib0 + aa, j = jb0 + bb;
+      const bool in = (i >= 1 - nb) && (i <= ii + nb) && (j >= 1 - nb) && (j <= jj + nb);
+      MSK[t] = in ? A.msk[(long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1] : 0;
+      if (!A.tm_has3) HO[t] = 1.0;  // tsadvc without btrmas: onetamas = 1
+    }
+    if (!landed()) return false;
+  } else {
     const double *uk = A.mode == 0 ? A.uflx + k * sl : A.uflx;
     const double *vk = A.mode == 0 ? A.vflx + k * sl : A.vflx;
-    for (int t = threadIdx.x; t < N; t += 256) {
+    for (int t = threadIdx.x; t < NR; t += 256) {
       const int bb = t / RX, aa = t - bb * RX;
       const int i = ib0 + aa, j = jb0 + bb;
       const bool in = (i >= 1 - nb) && (i <= ii + nb) && (j >= 1 - nb) && (j <= jj + nb);
@@ -85,7 +138,7 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
     }
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < N; t += 256) {
+  for (int t = threadIdx.x; t < NR; t += 256) {
     const int bb = t / RX, aa = t - bb * RX;
     double fco, fcn;
     if (A.mode == 0) {  // mod_tsadvc.F90:1931-1938
@@ -127,26 +180,40 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
     const double *fn = fd.nbase + (long long)(k + fd.k_off) * sl;
     const double *fm = fd.mbase + (long long)(k + fd.k_off) * sl;
     double *out = A.out + ((long long)fi * A.kdm + k) * sl;
-    for (int t = threadIdx.x; t < N; t += 256) {
-      const int bb = t / RX, aa = t - bb * RX;
-      const int i = ib0 + aa, j = jb0 + bb;
-      const bool in = (i >= 1 - nb) && (i <= ii + nb) && (j >= 1 - nb) && (j <= jj + nb);
-      const long long o = in ? (long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1 : 0;
-      FLD[t] = in ? fn[o] : 0.0;
-      FLDC[t] = in ? fm[o] : 0.0;
-      FX[t] = 0.0;
-      FY[t] = 0.0;
+    if (tm) {  // the previous field's readers passed the barrier that ends its loop
+      if (threadIdx.x == 0) {
+        tma::fence_proxy_async();
+        tma::expect_tx(bar, 2u * G::BOX);
+        tma::load3(FLD - off, tm + 6 + 2 * fi, bar, x0 - off, y0, k + fd.k_off);
+        tma::load3(FLDC - off, tm + 7 + 2 * fi, bar, x0 - off, y0, k + fd.k_off);
+      }
+      for (int t = threadIdx.x; t < NR; t += 256) {
+        FX[t] = 0.0;
+        FY[t] = 0.0;
+      }
+      if (!landed()) return false;
+    } else {
+      for (int t = threadIdx.x; t < NR; t += 256) {
+        const int bb = t / RX, aa = t - bb * RX;
+        const int i = ib0 + aa, j = jb0 + bb;
+        const bool in = (i >= 1 - nb) && (i <= ii + nb) && (j >= 1 - nb) && (j <= jj + nb);
+        const long long o = in ? (long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1 : 0;
+        FLD[t] = in ? fn[o] : 0.0;
+        FLDC[t] = in ? fm[o] : 0.0;
+        FX[t] = 0.0;
+        FY[t] = 0.0;
+      }
+      __syncthreads();
     }
-    __syncthreads();
 
     // S1: upwind fluxes, :686-720 (zero on faces that are not sea-sea)
-    rect<RX, 1, RX, 1, RY - 1>([&](int a, int b, int e, int) {
+    rect<RX, 1, RW, 1, RY - 1>([&](int a, int b, int e, int) {
       if (MSK[e] & kIU) {
         const double uu = U[e];
         FX[e] = uu * (ge0(uu) ? FLD[e - 1] : FLD[e]);
       }
     });
-    rect<RX, 1, RX - 1, 1, RY>([&](int a, int b, int e, int) {
+    rect<RX, 1, RW - 1, 1, RY>([&](int a, int b, int e, int) {
       if (MSK[e] & kIV) {
         const double vv = V[e];
         FY[e] = vv * (ge0(vv) ? FLD[e - RX] : FLD[e]);
@@ -155,7 +222,7 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
     __syncthreads();
 
     // S2: low-order solution on [1,RX-1)^2, :778-791
-    rect<RX, 1, RX - 1, 1, RY - 1>([&](int a, int b, int e, int) {
+    rect<RX, 1, RW - 1, 1, RY - 1>([&](int a, int b, int e, int) {
       const uint8_t m = MSK[e];
       if (!(m & kIP)) return;
       const double c = FLD[e];
@@ -172,7 +239,7 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
     __syncthreads();
 
     // S3: antidiffusive fluxes, :817-855 (FCT4: :1528-1580)
-    rect<RX, 2, RX - 1, 2, RY - 2>([&](int a, int b, int e, int) {
+    rect<RX, 2, RW - 1, 2, RY - 2>([&](int a, int b, int e, int) {
       if (!(MSK[e] & kIU)) return;
       const double uu = U[e];
       double fhx;
@@ -184,7 +251,7 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
       }
       FX[e] = fhx - FX[e];
     });
-    rect<RX, 2, RX - 2, 2, RY - 1>([&](int a, int b, int e, int) {
+    rect<RX, 2, RW - 2, 2, RY - 1>([&](int a, int b, int e, int) {
       if (!(MSK[e] & kIV)) return;
       const double vv = V[e];
       double fhy;
@@ -199,7 +266,7 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
     __syncthreads();
 
     // fmxlo/fmnlo (:792-793) in place over fld/fldc, now dead
-    rect<RX, 1, RX - 1, 1, RY - 1>([&](int a, int b, int e, int) {
+    rect<RX, 1, RW - 1, 1, RY - 1>([&](int a, int b, int e, int) {
       if (!(MSK[e] & kIP)) return;
       const double c = FLD[e], cc = FLDC[e], lo = FLO[e];
       FLD[e] = kmax(kmax(c, cc), lo);
@@ -240,19 +307,19 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
       RP[e] = rp;
       RM[e] = rm;
     };
-    rect<RX, 3, RX - 3, 3, RY - 3>([&](int a, int b, int e, int it) {
+    rect<RX, 3, RW - 3, 3, RY - 3>([&](int a, int b, int e, int it) {
       if (MSK[e] & kIP) zalesak(e, qx[it], qn[it]);
     });
-    {  // the ring [2,RX-2)^2 minus the output cells: ratios only
-      constexpr int NR = 2 * (RX - 4) + 2 * (RY - 6);
-      static_assert(NR <= 256, "ring larger than the CTA");
+    {  // the ring [2,RW-2) x [2,RY-2) minus the output cells: ratios only
+      constexpr int NRING = 2 * (RW - 4) + 2 * (RY - 6);
+      static_assert(NRING <= 256, "ring larger than the CTA");
       const int t = threadIdx.x;
-      if (t < NR) {
+      if (t < NRING) {
         int a, b;
-        if (t < RX - 4) { a = 2 + t; b = 2; }
-        else if (t < 2 * (RX - 4)) { a = 2 + t - (RX - 4); b = RY - 3; }
-        else if (t < 2 * (RX - 4) + (RY - 6)) { a = 2; b = 3 + t - 2 * (RX - 4); }
-        else { a = RX - 3; b = 3 + t - 2 * (RX - 4) - (RY - 6); }
+        if (t < RW - 4) { a = 2 + t; b = 2; }
+        else if (t < 2 * (RW - 4)) { a = 2 + t - (RW - 4); b = RY - 3; }
+        else if (t < 2 * (RW - 4) + (RY - 6)) { a = 2; b = 3 + t - 2 * (RW - 4); }
+        else { a = RW - 3; b = 3 + t - 2 * (RW - 4) - (RY - 6); }
         const int e = b * RX + a;
         double dx, dn;
         if (MSK[e] & kIP) zalesak(e, dx, dn);
@@ -261,13 +328,13 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
     __syncthreads();
 
     // S5: limit, :922-946
-    rect<RX, 3, RX - 2, 3, RY - 3>([&](int a, int b, int e, int) {
+    rect<RX, 3, RW - 2, 3, RY - 3>([&](int a, int b, int e, int) {
       if (!(MSK[e] & kIU)) return;
       const double f = FX[e];
       const double fact = lt0(f) ? kmin(RP[e - 1], RM[e]) : kmin(RP[e], RM[e - 1]);
       FX[e] = fact * f;
     });
-    rect<RX, 3, RX - 3, 3, RY - 2>([&](int a, int b, int e, int) {
+    rect<RX, 3, RW - 3, 3, RY - 2>([&](int a, int b, int e, int) {
       if (!(MSK[e] & kIV)) return;
       const double f = FY[e];
       const double fact = lt0(f) ? kmin(RP[e - RX], RM[e]) : kmin(RP[e], RM[e - RX]);
@@ -276,7 +343,7 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
     __syncthreads();
 
     // S6: corrected update of the output cells, :962-982
-    rect<RX, 3, RX - 3, 3, RY - 3>([&](int a, int b, int e, int it) {
+    rect<RX, 3, RW - 3, 3, RY - 3>([&](int a, int b, int e, int it) {
       const int i = ib0 + a, j = jb0 + b;
       if (i > ii || j > jj || !(MSK[e] & kIP)) return;
       const double fdv = ((FX[e + 1] - FX[e]) + (FY[e + RX] - FY[e])) * dt2 * SCI[e];
@@ -290,12 +357,20 @@ __device__ __forceinline__ void fct_tile_body(const TileArgs &A, const int tile,
     });
     __syncthreads();
   }
+  return true;
 }
 
 template <int SCHEME, int TX, int TY>
 __global__ void __launch_bounds__(256, 2) fct_tile_kernel(const TileArgs A) {
   extern __shared__ __align__(16) double sm[];
-  fct_tile_body<SCHEME, TX, TY>(A, blockIdx.x, blockIdx.y, sm);
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tma::bar_init(&bar, 1);
+    tma::fence_bar_init();
+  }
+  __syncthreads();
+  uint32_t ph = 0;
+  fct_tile_body<SCHEME, TX, TY>(A, blockIdx.x, blockIdx.y, sm, &bar, ph);
 }
 
 // Persistent form for an ensemble of basins: CTAs take work items
@@ -307,7 +382,13 @@ __global__ void __launch_bounds__(256, 2)
   __shared__ int cur;
   __shared__ int cur_basin;
   __shared__ __align__(16) TileArgs sa;  // the item's basin, staged once (read many times below)
-  if (threadIdx.x == 0) cur_basin = -1;
+  __shared__ uint64_t bar;
+  uint32_t ph = 0;
+  if (threadIdx.x == 0) {
+    cur_basin = -1;
+    tma::bar_init(&bar, 1);
+    tma::fence_bar_init();
+  }
   for (;;) {
     if (threadIdx.x == 0) cur = atomicAdd(head, 1);
     __syncthreads();
@@ -323,7 +404,7 @@ __global__ void __launch_bounds__(256, 2)
       if (threadIdx.x == 0) cur_basin = w.x;
     }
     __syncthreads();
-    fct_tile_body<SCHEME, TX, TY>(sa, w.y, w.z, sm);
+    if (!fct_tile_body<SCHEME, TX, TY>(sa, w.y, w.z, sm, &bar, ph)) break;
   }
 }
 

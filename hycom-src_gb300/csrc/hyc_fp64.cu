@@ -61,6 +61,14 @@ bool advect_tile_shape_ok(TileShape t) {
          (t.tx == 16 && t.ty == 16);
 }
 
+bool advect_tiles_tma(int scheme, TileShape t) {
+  if (!advect_tile_shape_ok(t)) return false;
+  if (scheme == kFCT2 || scheme == kFCT4) return true;  // fct_tile_kernel: every shape
+  if (t.tx == 32 && t.ty == 16) return TileGeom<32, 16>::TMA;
+  if (t.tx == 32 && t.ty == 32) return TileGeom<32, 32>::TMA;
+  return TileGeom<16, 16>::TMA;
+}
+
 size_t advect_tiles_smem(TileShape t) {
   if (t.tx == 32 && t.ty == 16) return TileGeom<32, 16>::smem_bytes;
   if (t.tx == 32 && t.ty == 32) return TileGeom<32, 32>::smem_bytes;

@@ -15,6 +15,8 @@
 
 #include <cstddef>
 
+#include "hyc_tmap.h"
+
 // The parameter blocks are passed by reference from Fortran as bind(c)
 // derived types (ten int32 flags then delt1 and the trcflg pointer; four
 // int32 then delt1 and ra2fac; an int64, eight int64 counts, eight doubles):
@@ -67,6 +69,9 @@ struct hyc_ctx {
   double *d_scratch = nullptr;  // advem output slices (fields x layers)
   double *d_iso = nullptr;      // smoothed layer-1 fluxes of isopycnic mode (2 slices)
   bool lconserve = false;       // advem's explicit conservation rescale (hyc_set_conserve)
+  CUtensorMap *d_tmaps = nullptr;  // TMA maps of the FCT tile launches of one call
+  size_t tmaps_cap = 0;
+  int *d_err = nullptr;            // a TMA wait of a tile kernel gave up
   double *d_cons = nullptr;     // its row sums and factors
   size_t cons_elems = 0;
   size_t scratch_elems = 0;
@@ -167,6 +172,60 @@ void fct2c_bind(hyc::Fct2cArgs &f, const hyc_ctx *c, int npair) {
   f.npair = npair;
   f.work = (double *)c->d_fct2c;
   f.lcalc = c->d_fct2c + (size_t)npair * sl * 13 * sizeof(double);
+}
+
+// TMA maps of the FCT tile kernel for the launches of one call (box TX+8 x
+// TY+6, FP64; see TileArgs::tmaps): host list, then one copy to the device.
+// use = false when the arrays break a TMA rule (pitch or base alignment):
+// those launches stage with plain loads.
+struct TileMaps {
+  std::vector<CUtensorMap> h;
+  bool use = true;
+};
+
+// append the maps of launch a; returns its first index, or -1 (plain loads)
+long tile_maps_add(const hyc_ctx *c, const hyc::TileArgs &a, int kk, bool flux1, TileMaps &tmv) {
+  if (!tmv.use || !hyc::tmap_available()) return -1;
+  const int bx = c->shape.tx + 8, by = c->shape.ty + 6;
+  const long long w = c->idm + 2LL * c->nbdy, h = c->jdm + 2LL * c->nbdy, ld = c->ld1, sl = c->slice;
+  std::vector<CUtensorMap> m(6 + 2 * (size_t)a.nfld);
+  bool ok = true;
+  auto enc = [&](CUtensorMap *p, const double *base, long long nz) {
+    ok = ok && hyc::tmap_encode3(p, base, 8, w, h, ld, sl, nz, bx, by);
+  };
+  const long long nzf = a.mode == 0 ? (flux1 ? 1 : kk) : 1;
+  enc(&m[0], a.uflx, nzf);
+  enc(&m[1], a.vflx, nzf);
+  enc(&m[2], a.mode == 0 ? a.dpn : a.fcn, a.mode == 0 ? kk : 1);
+  const double *m3 = a.mode == 0 ? a.oneta_n : a.fco;
+  if (m3) enc(&m[3], m3, 1);
+  enc(&m[4], a.scal, 1);
+  enc(&m[5], a.scali, 1);
+  for (int fi = 0; fi < a.nfld; fi++) {
+    const long long nz = kk + 2LL * a.f[fi].k_off;  // q2/q2l: 0..kk+1
+    enc(&m[6 + 2 * fi], a.f[fi].nbase, nz);
+    enc(&m[7 + 2 * fi], a.f[fi].mbase, nz);
+  }
+  if (!ok) return -1;
+  const long at = (long)tmv.h.size();
+  tmv.h.insert(tmv.h.end(), m.begin(), m.end());
+  return at;
+}
+
+// copy the call's maps to the device; the launches then point into it
+int tile_maps_upload(hyc_ctx *c, const TileMaps &tmv) {
+  if (tmv.h.empty()) return HYC_OK;
+  if (c->tmaps_cap < tmv.h.size()) {
+    CK(cudaStreamSynchronize(c->stream), "maps sync");  // earlier launches may read the old buffer
+    cudaFree(c->d_tmaps);
+    c->d_tmaps = nullptr;
+    c->tmaps_cap = 0;
+    CK(cudaMalloc(&c->d_tmaps, tmv.h.size() * sizeof(CUtensorMap)), "malloc tensor maps");
+    c->tmaps_cap = tmv.h.size();
+  }
+  CK(cudaMemcpyAsync(c->d_tmaps, tmv.h.data(), tmv.h.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, c->stream),
+     "tensor maps");
+  return HYC_OK;
 }
 
 // the lconserve rescale of one tile launch: a.cfac is set for its copy back
@@ -279,10 +338,22 @@ int hyc_enable_timers(hyc_ctx *c, int32_t on) {
   return HYC_OK;
 }
 
+// after a stream synchronisation: a tile kernel's bounded TMA wait gave up
+int tma_flag(hyc_ctx *c) {
+  int flag = 0;
+  CK(cudaMemcpy(&flag, c->d_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+  if (flag) {
+    cudaMemset(c->d_err, 0, sizeof(int));
+    return fail(c, HYC_ERR_CUDA, "a tile kernel gave up waiting for its TMA loads");
+  }
+  return HYC_OK;
+}
+
 int hyc_get_stats(hyc_ctx *c, hyc_stats *out, int32_t reset) {
   if (!c || !out) return fail(c, HYC_ERR_ARG, "hyc_get_stats: null argument");
   DeviceGuard g(c->device);
   CK(cudaStreamSynchronize(c->stream), "stats sync");
+  if (int rc = tma_flag(c)) return rc;
   fold_timings(c);
   *out = c->stats;
   if (reset) c->stats = hyc_stats{};
@@ -431,6 +502,8 @@ int hyc_adv_init(hyc_ctx **out, int32_t idm, int32_t jdm, int32_t kdm, int32_t n
   if ((e = cudaMalloc(&c->d_scp2, c->slice * 8)) != cudaSuccess) return bail(e, "malloc scp2");
   if ((e = cudaMalloc(&c->d_scp2i, c->slice * 8)) != cudaSuccess) return bail(e, "malloc scp2i");
   if ((e = cudaMalloc(&c->d_keys, 2 * kdm * sizeof(long long))) != cudaSuccess) return bail(e, "malloc keys");
+  if ((e = cudaMalloc(&c->d_err, sizeof(int))) != cudaSuccess || (e = cudaMemset(c->d_err, 0, sizeof(int))) != cudaSuccess)
+    return bail(e, "error flag");
   if ((e = cudaMallocHost(&c->h_keys, 2 * kdm * sizeof(long long))) != cudaSuccess) return bail(e, "host keys");
   if ((e = cudaMalloc(&c->d_sum, (2 * hyc::mass_sum_partials() + 2) * sizeof(double))) != cudaSuccess)
     return bail(e, "malloc sum");
@@ -459,6 +532,8 @@ int hyc_adv_finalize(hyc_ctx *c) {
     cudaFree(c->d_cnkeys);
     cudaFree(c->d_scratch);
     cudaFree(c->d_iso);
+    cudaFree(c->d_tmaps);
+    cudaFree(c->d_err);
     cudaFree(c->d_cons);
     cudaFree(c->d_fct2c);
     cudaFree(c->d_tmp);
@@ -493,7 +568,7 @@ int hyc_synchronize(hyc_ctx *c) {
   if (!c) return fail(nullptr, HYC_ERR_ARG, "null ctx");
   DeviceGuard g(c->device);
   CK(cudaStreamSynchronize(c->stream), "synchronize");
-  return HYC_OK;
+  return tma_flag(c);
 }
 
 int hyc_bind_field(hyc_ctx *c, int32_t field, void *ptr, int64_t nelem, int32_t where) {
@@ -650,6 +725,16 @@ int hyc_advem(hyc_ctx *c, int32_t advtyp, double *fld, const double *fldc, const
   a.f[0].posdef = posdef;
   a.out = c->d_scratch;
   a.kdm = 1;
+  a.err = c->d_err;
+  if (hyc::advect_tiles_tma(advtyp, c->shape)) {  // the tile kernel stages by TMA
+    TileMaps tmv;
+    const long m0 = tile_maps_add(c, a, 1, true, tmv);
+    if (m0 >= 0) {
+      if ((rc = tile_maps_upload(c, tmv))) return rc;
+      a.tmaps = c->d_tmaps + m0;
+      a.tm_has3 = 1;  // fco
+    }
+  }
   {
     Timed t(c, HYC_T_ADVECT);
     CK(hyc::launch_advect_tiles(advtyp, a, 1, c->shape, c->stream), "advem kernel");
@@ -846,46 +931,67 @@ int hyc_tsadvc(hyc_ctx *c, int32_t m, int32_t n, const hyc_tsadvc_params *p, dou
   const int nchunk0 = (int)most < chunk ? (int)most : chunk;
   if (most > 0 && (rc = ensure_scratch(c, (size_t)nchunk0 * kk * sl))) return rc;
   a.out = c->d_scratch;
-  // one group of fields over layers 1..nlay: tile kernel into the scratch, then back into level n
-  auto run = [&](const std::vector<FieldDesc> &grp, int nlay) -> int {
-    for (size_t f0 = 0; f0 < grp.size(); f0 += chunk) {
-      int nf = (int)(grp.size() - f0) < chunk ? (int)(grp.size() - f0) : chunk;
-      a.nfld = nf;
-      for (int q = 0; q < nf; q++) a.f[q] = grp[f0 + q];
-      {
-        Timed t(c, HYC_T_ADVECT);
-        CK(hyc::launch_advect_tiles(at, a, nlay, c->shape, s), "advect kernel");
-        int rc2;
-        if (c->lconserve && (rc2 = conserve(c, a, nlay))) return rc2;
-      }
-      {
-        Timed t(c, HYC_T_COPY);
-        CK(hyc::launch_copy_back(a, nlay, s), "copy back");
-      }
-      a.cfac = nullptr;
-      c->stats.launches += 2;
-    }
-    return HYC_OK;
+  a.err = c->d_err;
+  // the tile launches of this call: each group of fields over layers
+  // 1..nlay in chunks of kMaxFields, with the TMA maps of the FCT kernel
+  struct Launch {
+    TileArgs a;
+    int nlay;
+    long map0;  // first TMA map, -1: plain loads
   };
+  std::vector<Launch> launches;
+  TileMaps tmv;
+  const bool fct = hyc::advect_tiles_tma(at, c->shape);  // the tile kernel stages by TMA
+  auto plan = [&](const std::vector<FieldDesc> &grp, int nlay, bool flux1) {
+    for (size_t f0 = 0; f0 < grp.size(); f0 += chunk) {
+      Launch L{a, nlay, -1};
+      L.a.nfld = (int)(grp.size() - f0) < chunk ? (int)(grp.size() - f0) : chunk;
+      for (int q = 0; q < L.a.nfld; q++) L.a.f[q] = grp[f0 + q];
+      if (fct) L.map0 = tile_maps_add(c, L.a, kk, flux1, tmv);
+      launches.push_back(L);
+    }
+  };
+  double *us = nullptr, *vs = nullptr;
   if (p->isopyc && (!iso1.empty() || !isot.empty())) {  // layer 1, :1860-1897
     if (!c->d_iso) CK(cudaMalloc(&c->d_iso, 2 * sl * sizeof(double)), "malloc isopycnic fluxes");
-    double *us = c->d_iso, *vs = c->d_iso + sl;
-    CK(hyc::launch_iso_smooth(F[HYC_F_UFLX].dev, F[HYC_F_VFLX].dev, c->d_msk, sl, c->idm, c->jdm, c->nbdy, c->ld1,
-                              kMbdy[at] - 1, us, vs, s),
-       "isopycnic smoothing");
-    c->stats.launches += 1;
+    us = c->d_iso;
+    vs = c->d_iso + sl;
     a.uflx = us;  // layer 1 of the launch reads uflx + 0*slice
     a.vflx = vs;
-    if ((rc = run(iso1, 1))) return rc;
+    plan(iso1, 1, true);
     a.uflx = F[HYC_F_UFLX].dev;
     a.vflx = F[HYC_F_VFLX].dev;
     a.ufco = us;
     a.vfco = vs;
-    if ((rc = run(isot, 1))) return rc;
+    plan(isot, 1, false);
     a.ufco = nullptr;
     a.vfco = nullptr;
   }
-  if ((rc = run(fl, kk))) return rc;
+  plan(fl, kk, false);
+  if ((rc = tile_maps_upload(c, tmv))) return rc;
+  if (us) {
+    CK(hyc::launch_iso_smooth(F[HYC_F_UFLX].dev, F[HYC_F_VFLX].dev, c->d_msk, sl, c->idm, c->jdm, c->nbdy, c->ld1,
+                              kMbdy[at] - 1, us, vs, s),
+       "isopycnic smoothing");
+    c->stats.launches += 1;
+  }
+  for (Launch &L : launches) {
+    if (L.map0 >= 0) {
+      L.a.tmaps = c->d_tmaps + L.map0;
+      L.a.tm_has3 = L.a.oneta_n != nullptr;
+    }
+    {
+      Timed t(c, HYC_T_ADVECT);
+      CK(hyc::launch_advect_tiles(at, L.a, L.nlay, c->shape, s), "advect kernel");
+      int rc2;
+      if (c->lconserve && (rc2 = conserve(c, L.a, L.nlay))) return rc2;
+    }
+    {
+      Timed t(c, HYC_T_COPY);
+      CK(hyc::launch_copy_back(L.a, L.nlay, s), "copy back");
+    }
+    c->stats.launches += 2;
+  }
 
   // salinity range diagnostic, mod_tsadvc.F90:2065-2084
   if (xmin && xmax && (p->nstep % 3 == 0 || p->diagno)) {

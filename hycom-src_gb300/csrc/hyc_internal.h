@@ -20,6 +20,9 @@ struct TileShape {
 cudaError_t launch_advect_tiles(int scheme, const TileArgs &a, int nlayers, TileShape shape,
                                 cudaStream_t s);
 size_t advect_tiles_smem(TileShape shape);
+// the tile kernel of this scheme and shape stages its region by TMA when
+// the launch carries tensor maps (box (tx+8) x (ty+6), see TileArgs::tmaps)
+bool advect_tiles_tma(int scheme, TileShape shape);
 bool advect_tile_shape_ok(TileShape shape);
 
 // Copy the interior of out[(fi*kdm+k)] back into field level n for every

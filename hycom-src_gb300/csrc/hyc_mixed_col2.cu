@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
       tma::load3(slot + RG::OFF_U, B.c2_u, b, s0, y, k);
       tma::load3(slot + RG::OFF_V, B.c2_v, b, s0, y, k);
       tma::load3(slot + RG::OFF_DP, B.c2_dp, b, s0, y, k);
-      tma::load2(slot + RG::OFF_CG, B.c2_cg, b, s0, y);
+      tma::load3(slot + RG::OFF_CG, B.c2_cg, b, s0, y, 0);
     };
     if (lane == 0)
       for (int d = 0; d < kNS && d < T; d++) issue(d);

@@ -25,9 +25,16 @@
 // (this file is compiled with -fmad=false); the only rewritten operation is
 // division by the layer thickness, which uses div_rcp (bit-identical to
 // IEEE division).
+//
+// The region is staged by TMA (one box per array, one mbarrier, bounded
+// waits) when the launch carries tensor maps and the shape allows it
+// (TileGeom::TMA), else by plain loads.
 #pragma once
+#include <cuda.h>
+
 #include "hyc_args.h"
 #include "hyc_device.cuh"
+#include "hyc_tma.cuh"
 
 namespace hyc {
 
@@ -46,13 +53,9 @@ __device__ __forceinline__ void for_rect(int a0, int a1, int b0, int b1, F f) {
 template <int SCHEME, int TX, int TY>
 __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
   using G = TileGeom<TX, TY>;
-  constexpr int RX = G::RX, RY = G::RY, N = G::N;
+  constexpr int RX = G::RX, RW = G::RW, RY = G::RY, N = G::N, NR = G::NR;
   extern __shared__ __align__(16) double sm[];
-  double *U = sm, *V = U + N, *FCO = V + N, *FCN = FCO + N, *HN = FCN + N, *RH = HN + N, *SCL = RH + N,
-         *SCI = SCL + N;
-  double *FLD = SCI + N, *FLDC = FLD + N, *FX = FLDC + N, *FY = FX + N, *FLO = FY + N, *FXL = FLO + N,
-         *FNL = FXL + N, *RP = FNL + N, *RM = RP + N, *QX = RM + N, *QN = QX + N;
-  uint8_t *MSK = reinterpret_cast<uint8_t *>(QN + N);
+  __shared__ uint64_t bar;
 
   const int tile = blockIdx.x;
   const int k = blockIdx.y;  // 0-based layer
@@ -60,13 +63,59 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
   const int i0 = 1 + txi * TX, j0 = 1 + tyi * TY;  // first output cell (Fortran index)
   const int ib0 = i0 - 3, jb0 = j0 - 3;            // region origin
   const int nb = A.nbdy, ld1 = A.ld1;
+  const int x0 = ib0 + nb - 1, y0 = jb0 + nb - 1;  // padded column / row of the region origin
+  const int off = x0 & 1;                           // TMA boxes start at the even column x0 - off
+  double *sal = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(sm) + 127) & ~uintptr_t(127));
+  double *U = sal + off, *V = U + N, *FCO = V + N, *FCN = FCO + N, *HN = FCN + N, *RH = HN + N, *SCL = RH + N,
+         *SCI = SCL + N;
+  double *FLD = SCI + N, *FLDC = FLD + N, *FX = FLDC + N, *FY = FX + N, *FLO = FY + N, *FXL = FLO + N,
+         *FNL = FXL + N, *RP = FNL + N, *RM = RP + N, *QX = RM + N, *QN = QX + N;
+  uint8_t *MSK = reinterpret_cast<uint8_t *>(sal + G::NARR * N);
+  const CUtensorMap *tm = G::TMA ? reinterpret_cast<const CUtensorMap *>(A.tmaps) : nullptr;
   const long long sl = A.slice;
   const double dt2 = A.dt2;
+  uint32_t ph = 0;  // completed phases of bar
+  if (tm && threadIdx.x == 0) {
+    tma::bar_init(&bar, 1);
+    tma::fence_bar_init();
+  }
+  // all threads wait for the mbarrier's next phase; if any gave up, the
+  // copies in flight land (bounded) and the CTA stops
+  auto landed = [&]() -> bool {
+    const bool ok = tma::wait(&bar, ph & 1u, A.err);
+    ph++;
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) tma::wait(&bar, (ph - 1) & 1u, nullptr);
+      return false;
+    }
+    return true;
+  };
 
   // ---- stage per-layer inputs -------------------------------------------------
   const double *uk = A.mode == 0 ? A.uflx + k * sl : A.uflx;
   const double *vk = A.mode == 0 ? A.vflx + k * sl : A.vflx;
-  for (int t = threadIdx.x; t < N; t += blockDim.x) {
+  if (tm) {
+    __syncthreads();  // the mbarrier is initialised
+    if (threadIdx.x == 0) {
+      const int zk = A.mode == 0 ? k : 0;
+      tma::expect_tx(&bar, (A.tm_has3 ? 6u : 5u) * G::BOX);
+      tma::load3(U - off, tm + 0, &bar, x0 - off, y0, zk);
+      tma::load3(V - off, tm + 1, &bar, x0 - off, y0, zk);
+      tma::load3(FCN - off, tm + 2, &bar, x0 - off, y0, zk);
+      if (A.tm_has3) tma::load3(FCO - off, tm + 3, &bar, x0 - off, y0, 0);
+      tma::load3(SCL - off, tm + 4, &bar, x0 - off, y0, 0);
+      tma::load3(SCI - off, tm + 5, &bar, x0 - off, y0, 0);
+    }
+    for (int t = threadIdx.x; t < NR; t += blockDim.x) {  // masks (bytes) by plain loads meanwhile
+      int bb = t / RX, aa = t - bb * RX;
+      int i = ib0 + aa, j = jb0 + bb;
+      bool in = (i >= 1 - nb) && (i <= A.ii + nb) && (j >= 1 - nb) && (j <= A.jj + nb);
+      MSK[t] = in ? A.msk[(long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1] : 0;
+      if (!A.tm_has3) FCO[t] = 1.0;  // tsadvc without btrmas: onetamas = 1
+    }
+    if (!landed()) return;
+  }
+  for (int t = threadIdx.x; t < (tm ? 0 : NR); t += blockDim.x) {
     int bb = t / RX, aa = t - bb * RX;
     int i = ib0 + aa, j = jb0 + bb;
     bool in = (i >= 1 - nb) && (i <= A.ii + nb) && (j >= 1 - nb) && (j <= A.jj + nb);
@@ -90,7 +139,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
     // only its own FCO/FCN and the fluxes on its faces):
     //   util1 = max(onetamas*dp + flxdiv, 0), util2 = max(onetamas*dp, 0)
     // valid on [0,RX-1) x [0,RY-1) (the face at a+1, b+1 is needed).
-    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+    for (int t = threadIdx.x; t < NR; t += blockDim.x) {
       int bb = t / RX, aa = t - bb * RX;
       double o = FCO[t] * FCN[t];  // onetamas*dp
       double fdv = 0.0;
@@ -114,7 +163,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
     }
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < N; t += blockDim.x) {
+  for (int t = threadIdx.x; t < NR; t += blockDim.x) {
     double hn = FCN[t] + kOnemu;
     HN[t] = hn;
     RH[t] = __drcp_rn(hn);
@@ -128,21 +177,33 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
     const double *fn = fd.nbase + (long long)(k + fd.k_off) * sl;
     const double *fm = fd.mbase + (long long)(k + fd.k_off) * sl;
     const double posdef = fd.posdef;
-    for (int t = threadIdx.x; t < N; t += blockDim.x) {
-      int bb = t / RX, aa = t - bb * RX;
-      int i = ib0 + aa, j = jb0 + bb;
-      bool in = (i >= 1 - nb) && (i <= A.ii + nb) && (j >= 1 - nb) && (j <= A.jj + nb);
-      long long o = in ? (long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1 : 0;
-      FLD[t] = in ? fn[o] : 0.0;
-      if (SCHEME != kPCM && SCHEME != kMPDATA) FLDC[t] = in ? fm[o] : 0.0;
+    constexpr bool CENTRE = SCHEME != kPCM && SCHEME != kMPDATA;
+    if (tm) {  // the previous field's readers passed the barrier that ends its loop
+      if (threadIdx.x == 0) {
+        tma::fence_proxy_async();
+        tma::expect_tx(&bar, (CENTRE ? 2u : 1u) * G::BOX);
+        tma::load3(FLD - off, tm + 6 + 2 * fi, &bar, x0 - off, y0, k + fd.k_off);
+        if (CENTRE) tma::load3(FLDC - off, tm + 7 + 2 * fi, &bar, x0 - off, y0, k + fd.k_off);
+      }
+    }
+    for (int t = threadIdx.x; t < NR; t += blockDim.x) {
+      if (!tm) {
+        int bb = t / RX, aa = t - bb * RX;
+        int i = ib0 + aa, j = jb0 + bb;
+        bool in = (i >= 1 - nb) && (i <= A.ii + nb) && (j >= 1 - nb) && (j <= A.jj + nb);
+        long long o = in ? (long long)(i + nb - 1) + (long long)(j + nb - 1) * ld1 : 0;
+        FLD[t] = in ? fn[o] : 0.0;
+        if (CENTRE) FLDC[t] = in ? fm[o] : 0.0;
+      }
       FX[t] = 0.0;
       FY[t] = 0.0;
     }
+    if (tm && !landed()) return;
     __syncthreads();
 
     // S1: low-order (upwind) face fluxes on x-faces [1,RX-1] x rows [1,RY-1)
     // and y-faces cols [1,RX-1) x [1,RY-1]; MPDATA adds posdef and tx1/ty1.
-    for_rect<RX>(1, RX, 1, RY - 1, [&](int a, int b, int e) {
+    for_rect<RX>(1, RW, 1, RY - 1, [&](int a, int b, int e) {
       if (MSK[e] & kIU) {
         double uu = U[e];
         double q = ge0(uu) ? FLD[e - 1] : FLD[e];
@@ -156,7 +217,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
         FXL[e] = 0.0;
       }
     });
-    for_rect<RX>(1, RX - 1, 1, RY, [&](int a, int b, int e) {
+    for_rect<RX>(1, RW - 1, 1, RY, [&](int a, int b, int e) {
       if (MSK[e] & kIV) {
         double vv = V[e];
         double q = ge0(vv) ? FLD[e - RX] : FLD[e];
@@ -174,7 +235,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
 
     if (SCHEME == kPCM) {
       // mod_tsadvc.F90:610-630 on the output cells
-      for_rect<RX>(3, RX - 3, 3, RY - 3, [&](int a, int b, int e) {
+      for_rect<RX>(3, RW - 3, 3, RY - 3, [&](int a, int b, int e) {
         int i = ib0 + a, j = jb0 + b;
         if (i > A.ii || j > A.jj) return;
         double c = FLD[e];
@@ -199,7 +260,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
 
     // S2: on cells [1,RX-1) x [1,RY-1): 5-point extrema over sea neighbours
     // (ipim1/ipip1/ipjm1/ipjp1, bigrid.F90:316-333) and the low-order update.
-    for_rect<RX>(1, RX - 1, 1, RY - 1, [&](int a, int b, int e) {
+    for_rect<RX>(1, RW - 1, 1, RY - 1, [&](int a, int b, int e) {
       if (!(MSK[e] & kIP)) return;
       double c = FLD[e];
       double w = (MSK[e - 1] & kIP) ? FLD[e - 1] : c;
@@ -230,7 +291,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
 
     // S3: antidiffusive fluxes on x-faces [2,RX-2] x rows [2,RY-2) and
     // y-faces cols [2,RX-2) x [2,RY-2].
-    for_rect<RX>(2, RX - 1, 2, RY - 2, [&](int a, int b, int e) {
+    for_rect<RX>(2, RW - 1, 2, RY - 2, [&](int a, int b, int e) {
       uint8_t m = MSK[e];
       if (!(m & kIU)) return;
       double uu = U[e];
@@ -247,7 +308,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
         FX[e] = fhx - FX[e];
       }
     });
-    for_rect<RX>(2, RX - 2, 2, RY - 1, [&](int a, int b, int e) {
+    for_rect<RX>(2, RW - 2, 2, RY - 1, [&](int a, int b, int e) {
       uint8_t m = MSK[e];
       if (!(m & kIV)) return;
       double vv = V[e];
@@ -267,7 +328,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
     __syncthreads();
 
     // S4: limiter ratios on cells [2,RX-2) x [2,RY-2)
-    for_rect<RX>(2, RX - 2, 2, RY - 2, [&](int a, int b, int e) {
+    for_rect<RX>(2, RW - 2, 2, RY - 2, [&](int a, int b, int e) {
       uint8_t m = MSK[e];
       if (!(m & kIP)) return;
       if (SCHEME == kMPDATA) {  // :411-419
@@ -318,7 +379,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
     __syncthreads();
 
     // S5: limit fluxes on x-faces [3,RX-3] x rows [3,RY-3) and y-faces
-    for_rect<RX>(3, RX - 2, 3, RY - 3, [&](int a, int b, int e) {
+    for_rect<RX>(3, RW - 2, 3, RY - 3, [&](int a, int b, int e) {
       if (!(MSK[e] & kIU)) return;
       double f = FX[e];
       if (SCHEME == kMPDATA) {  // :440-441
@@ -328,7 +389,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
         FX[e] = fact * f;
       }
     });
-    for_rect<RX>(3, RX - 3, 3, RY - 2, [&](int a, int b, int e) {
+    for_rect<RX>(3, RW - 3, 3, RY - 2, [&](int a, int b, int e) {
       if (!(MSK[e] & kIV)) return;
       double f = FY[e];
       if (SCHEME == kMPDATA) {
@@ -341,7 +402,7 @@ __global__ void __launch_bounds__(256, 1) advect_tile_kernel(const TileArgs A) {
     __syncthreads();
 
     // S6: corrected update on the output cells, :962-982 (MPDATA :465-486)
-    for_rect<RX>(3, RX - 3, 3, RY - 3, [&](int a, int b, int e) {
+    for_rect<RX>(3, RW - 3, 3, RY - 3, [&](int a, int b, int e) {
       int i = ib0 + a, j = jb0 + b;
       if (i > A.ii || j > A.jj) return;
       double res = FLD[e];

@@ -18,6 +18,9 @@ __device__ __forceinline__ void bar_init(uint64_t *bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(bar)), "r"(count) : "memory");
 }
 __device__ __forceinline__ void fence_bar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// orders this thread's earlier generic-proxy accesses of shared memory (and,
+// after a CTA barrier, the CTA's) before its later TMA writes
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sa(bar)), "r"(bytes) : "memory");
 }
@@ -58,13 +61,5 @@ __device__ __forceinline__ void load3(void *dst, const CUtensorMap *map, uint64_
       "l"(map), "r"(x), "r"(y), "r"(z), "r"(sa(bar))
       : "memory");
 }
-__device__ __forceinline__ void load2(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          sa(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(sa(bar))
-      : "memory");
-}
-
 }  // namespace tma
 }  // namespace hyc

@@ -336,9 +336,9 @@ def test_error_paths(cuda):
     with pytest.raises(hycadv.HycError) as e:
         ctx.tsadvc(1, 2, delt1=100.0, advtyp=2, btrmas=True)
     assert e.value.code in (-6, -8)
-    with pytest.raises(hycadv.HycError) as e:
+    with pytest.raises(hycadv.HycError) as e:  # isopycnic mode has no hybrid layers (nhybrd = 0)
         ctx.tsadvc(1, 2, delt1=100.0, isopyc=True)
-    assert e.value.code == -8
+    assert e.value.code == -1
     with pytest.raises(hycadv.HycError) as e:
         ctx.tsadvc(0, 2, delt1=100.0)
     assert e.value.code == -1
