@@ -322,10 +322,12 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
 
             // ---- thickness factors of row J-1 (mod_tsadvc.F90:1905-1942)
             float2 W1, R1, QF1, Wm1, H1;  // Wm1 = W-1 and H1 = fco+fcn (MPDATA only)
+            float2 dv;                    // FP64 prep: the divergence of the face fluxes of row J-1
+            bool unA = false, unB = false;  // FP64 prep, MPDATA: fco = dp + div*dt2*scp2i (no clip)
             if (PREP64) {
               // continuity (:1931-1936): the face-flux differences and their sum by
               // two-sum in FP32, scaled by dt2*scp2i and added to dp in FP64
-              const float2 dv = comp_div2(east(u1), u1, v0, v1);
+              dv = comp_div2(east(u1), u1, v0, v1);
               const double bA = dA1 + kOnemu, bB = dB1 + kOnemu;       // dp + onemu
               const double hA = ge0(dA1) ? bA : kOnemu, hB = ge0(dB1) ? bB : kOnemu;  // fcn + onemu
               const double rA = rcp64(hA), rB = rcp64(hB);
@@ -338,6 +340,8 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               } else {
                 const double fA = f2d_i(dv.x) * sA1, fB = f2d_i(dv.y) * sB1;
                 const double cA = kmax(bA + fA, kOnemu), cB = kmax(bB + fB, kOnemu);
+                unA = ge0(dA1) && !klt(bA + fA, kOnemu);
+                unB = ge0(dB1) && !klt(bB + fB, kOnemu);
                 Wm1 = make_float2(d2f_i((cA - hA) * rA), d2f_i((cB - hB) * rB));
                 W1 = add2(Wm1, make_float2(1.f, 1.f));
                 H1 = add2(sub2(make_float2(d2f_pos(cA), d2f_pos(cB)), onemu2), sub2(hf, onemu2));
@@ -391,8 +395,16 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
             //       (:377-387);  ua0, va0  .5|u|, .5|v| of row J (:255, :264)
             float2 du1, Z1, uD1, vD1, ua0, va0;
             if (MP) {
-              du1 = mul2(comp_div2(east(u1m), u1m, v0m, v1m), DS1);
+              const float2 dvm = comp_div2(east(u1m), u1m, v0m, v1m);  // of the masked mass fluxes
+              du1 = mul2(dvm, DS1);
               Z1 = fma2(du1, nR1, Wm1);
+              if (PREP64) {
+                // unclipped, W-1 - du*R = (div - div_masked)*dt2*scp2i*R: formed from the
+                // difference of the two divergences, which is exactly 0 wherever no
+                // closed face carries a flux, instead of from W-1 (FP64) and du*R (FP32)
+                const float2 zd = mul2(mul2(sub2(dv, dvm), DS1), R1);
+                Z1 = sel(unA, unB, zd, Z1);
+              }
               const float2 Hw = west(H1);
               uD1 = make_float2(u1m.x * rcp_approx((H1.x + Hw.x) + onemu), u1m.y * rcp_approx((H1.y + Hw.y) + onemu));
               vD1 = make_float2(v1m.x * rcp_approx((H1.x + H2.x) + onemu), v1m.y * rcp_approx((H1.y + H2.y) + onemu));
