@@ -815,8 +815,8 @@ def ensemble_workload(args, wl, workload, dev, dist, forms, fp64_steps=None):
         members = [dict(nx=wl["nx"], ny=wl["ny"], kdm=args.layers or wl["kdm"], ntr=wl["ntr"], seed=wl["seed"])]
         nbasin_all = ws
         steps = args.steps
-    if forms[0] != "fp64":
-        raise SystemExit("--ens-forms must start with fp64 (the reference the others are compared with)")
+    if "fp64" in forms and forms[0] != "fp64":
+        raise SystemExit("--ens-forms: fp64 (the reference the others are compared with) must come first")
     t_start = time.perf_counter()
     geos = [member_geometry(m, wl) for m in members]
     specs = [g[2] for g in geos]
@@ -855,7 +855,7 @@ def ensemble_workload(args, wl, workload, dev, dist, forms, fp64_steps=None):
                 acc["cons"] = max(acc["cons"], abs(c_new - c_old[i][q]) / abs(c_old[i][q]))
                 if form == "fp64":
                     refs[(i, q)] = new.clone()
-                else:
+                elif (i, q) in refs:
                     ref = refs[(i, q)]
                     scale = float(ref.abs().max())
                     d = new - ref
@@ -911,7 +911,8 @@ def ensemble_workload(args, wl, workload, dev, dist, forms, fp64_steps=None):
         torch.cuda.empty_cache()
     refs.clear()
     for f in forms[1:]:
-        res[f]["speedup_vs_fp64"] = res[f]["value"] / res["fp64"]["value"]
+        if "fp64" in res:
+            res[f]["speedup_vs_fp64"] = res[f]["value"] / res["fp64"]["value"]
     if workload == "c3":
         desc = (f"c3: {nbasin_all} closed basins, nx 120-1500, ny 90-1100, kdm 22/32/41, 2-6 tracers (T, S, "
                 f"passive), FCT2, max Courant {wl['courant']}, delt1 {wl['delt1']} s, {steps}-step CUDA graph"
