@@ -363,13 +363,16 @@ RA2FAC = 0.125  # Robert-Asselin weight of the full form (blkdat ra2fac)
 ONETA0 = 0.1    # minimum 1+eta (blkdat oneta0)
 
 
-def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, advtyp=None, full=False):
+def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, advtyp=None, full=False,
+                    btrmas=False):
     """FP64 plain form through the reference-layout C ABI (hyc_tsadvc on
     resident fields), timed over K steps after W warm-up steps.  With full,
     every step is the tracer part of a HYCOM step: asselin_save, tsadvc, its
     diffusion block (hyc_tsdff, temdf2 = TEMDF2, on a uniform grid: aspux =
     aspvy = 1, scuy = scvx = sqrt(scp2)) and asselin_filter (ra2fac =
-    RA2FAC; dpo = the initial dp, pbot = 4e7 Pa, pbavg = 0, so oneta = 1)."""
+    RA2FAC; dpo = the initial dp, pbot = 4e7 Pa, pbavg = 0, so oneta = 1).
+    With btrmas, tsadvc runs with the barotropic mass flux (onetamas = 1 +
+    a seeded 1 % perturbation), so FCT2 is advem_fct2c."""
     advtyp = args.advtyp if advtyp is None else advtyp
     import numpy as np
     import torch
@@ -399,12 +402,18 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
         dx = np.sqrt(np.asarray(sc, dtype=np.float64))
         one = np.ones_like(dx)
         ctx.set_diffusion_grid(one, one, dx, dx)
+    if btrmas:
+        sh2 = tuple(case.dp.shape[-2:])
+        g = torch.Generator(device=dev).manual_seed(wl["seed"] + 77)
+        oneta = 1.0 + 0.01 * torch.rand((2,) + sh2, dtype=torch.float64, device=dev, generator=g)
+        ctx.bind("oneta", oneta)
+        keep.append(oneta)
 
     def step(s):
         m, n = ((s + 1) % 2) + 1, (s % 2) + 1
         if full:
             ctx.asselin_save(m, n, oneta0=ONETA0)
-        ctx.tsadvc(m, n, delt1=wl["delt1"], advtyp=advtyp, nstep=s)
+        ctx.tsadvc(m, n, delt1=wl["delt1"], advtyp=advtyp, nstep=s, btrmas=btrmas)
         if full:
             ctx.tsdff(m, n, delt1=wl["delt1"], temdf2=TEMDF2)
             ctx.asselin_filter(m, n, ra2fac=RA2FAC, oneta0=ONETA0)
@@ -440,7 +449,8 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
     bpu = bytes_per_update(8, 8, 8, 2, kdm)
     peak, peak_kind = peak_hbm()
     res = {"value": ws * ups_step * args.steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / args.steps,
-           "scheme": SCHEME_NAMES[advtyp] + (" + Laplacian diffusion + Robert-Asselin filter" if full else ""),
+           "scheme": SCHEME_NAMES[advtyp] + (" + Laplacian diffusion + Robert-Asselin filter" if full else "")
+           + (" with btrmas (advem_fct2c)" if btrmas else ""),
            "gpu_launches": int(st["launches"]), "clocks": clk.summary(),
            "timers_ms": {k: v for k, v in st.items() if k != "launches"}}
     if adv_calls > 0:
@@ -448,9 +458,12 @@ def run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, l
         achieved = ups_step * bpu / avg_s / 1e9
         res["roofline"] = {"bound": "fp64-alu (hbm fraction shown)", "achieved": achieved, "peak": peak,
                            "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                           "kernel": "advect_tile_kernel", "algorithmic_bytes_per_update": bpu,
+                           "kernel": ("fct2c_* stage kernels" if btrmas and advtyp == 2 else
+                                      "fct_tile_kernel" if advtyp in (2, 4) else "advect_tile_kernel"),
+                           "algorithmic_bytes_per_update": bpu,
                            "avg_launch_ms": adv_ms / adv_calls, "share_of_step": adv_ms / max(st["tsadvc"][0], 1e-9),
-                           "traffic": profile_traffic(f"{SCHEME_NAMES[advtyp].lower()}_fp64_{args.workload}")}
+                           "traffic": None if btrmas else
+                           profile_traffic(f"{SCHEME_NAMES[advtyp].lower()}_fp64_{args.workload}")}
     df_ms, df_calls = st["tsdff"]
     if df_calls > 0:
         # diffusion alone: T and S updated per cell and layer; algorithmic
@@ -1150,7 +1163,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.ref_layers <= 0:
-        args.ref_layers = args.layers or WORKLOADS[args.workload]["kdm"]
+        args.ref_layers = args.layers or WORKLOADS[args.workload].get("kdm", 41)
     args.tile = tuple(int(x) for x in args.tile.split(",")) if args.tile else None
     wl = dict(WORKLOADS[args.workload])
     if args.layers > 0:
@@ -1197,6 +1210,9 @@ def main():
     for f, adv in (("tsadvc-fct4", 4), ("tsadvc-mpdata", 1), ("tsadvc-pcm", 0)):
         if f in others:
             schemes[f] = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local, adv)
+    if "tsadvc-btrmas" in others:
+        schemes["tsadvc-btrmas"] = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local,
+                                                   2, btrmas=True)
     if "tsadvc-full" in others:
         schemes["tsadvc-full"] = run_tsadvc_fp64(args, wl, b, masks, nreg, sc, si, case, dev, stream, dist, local,
                                                  2, full=True)
