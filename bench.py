@@ -239,13 +239,16 @@ ENS_FORMS = {  # form -> (precision, FP64 thickness prep, advtyp)
     "mixed-fct4": ("mixed", True, 4),
     "fp64-mpdata": ("fp64", True, 1),
     "mixed-mpdata": ("mixed", True, 1),
+    "mixed-diff": ("mixed", True, 2),  # with tsadvc's lateral diffusion fused into the step kernel
 }
+DIFF_FORMS = {"mixed-diff"}
 FP64_REF = {2: "fp64", 4: "fp64-fct4", 1: "fp64-mpdata"}  # the FP64 form each mixed form is checked against
 # the ncu capture (profiles/) whose DRAM traffic a form's strip kernel launch is quoted with
 TRAFFIC_KEY = {"mixed": "col2_mixed", "mixed-fp32prep": "col2_mixed_fp32prep", "mixed-fct4": "col2_mixed_fct4",
-               "mixed-mpdata": "col2_mixed_mpdata", "fp64": "fct2_fp64_ens"}
+               "mixed-mpdata": "col2_mixed_mpdata", "fp64": "fct2_fp64_ens", "mixed-diff": "col2_mixed_diff"}
 KERNEL_OF_FORM = {"mixed": "mix_col2_kernel<FCT2,2,PREP64>", "mixed-fp32prep": "mix_col2_kernel<FCT2,2,FP32 prep>",
-                  "mixed-fct4": "mix_col2_kernel<FCT4,2,PREP64>", "mixed-mpdata": "mix_col2_kernel<MPDATA,2,PREP64>"}
+                  "mixed-fct4": "mix_col2_kernel<FCT4,2,PREP64>", "mixed-mpdata": "mix_col2_kernel<MPDATA,2,PREP64>",
+                  "mixed-diff": "mix_col2_kernel<FCT2,2,PREP64,DIFF>"}
 
 
 def make_ensemble(spec, form, stream):
@@ -257,6 +260,14 @@ def make_ensemble(spec, form, stream):
         ens.set_posdef(0, 0, 256.0)  # temperature (mod_tsadvc.F90:1761)
     if prec == "mixed":
         ens.set_prep64(prep64)
+    if form in DIFF_FORMS:
+        # the diffusion block of tsadvc (temdf2 = TEMDF2) on a uniform grid:
+        # aspux = aspvy = 1, scuy = scvx = sqrt(scp2)
+        import numpy as np
+
+        dx = np.sqrt(np.asarray(spec["scp2"], dtype=np.float64))
+        one = np.ones_like(dx)
+        ens.set_diffusion(0, TEMDF2, one, one, dx, dx)
     ens.set_stream(stream)  # graphs are recorded on the library's own stream and replayed here
     return ens
 
@@ -343,6 +354,15 @@ def run_ensemble_forms(args, wl, b, masks, spec, case, dev, stream, dist, local,
         del ens
         torch.cuda.empty_cache()
     for form in first:
+        if form in DIFF_FORMS:
+            # checked against the oracle's tsadvc + tsdff by the GPU tests; here the
+            # size of the diffusion against the same step without it
+            if "mixed" in first:
+                out[form]["diffusion_change_one_step"] = {
+                    name: float((first[form][q] - first["mixed"][q]).abs().max() / first["mixed"][q].abs().max())
+                    for q, name in enumerate(("temp", "saln"))}
+                out[form]["time_vs_mixed"] = out[form]["ms_per_step"] / out["mixed"]["ms_per_step"]
+            continue
         rf = FP64_REF[ENS_FORMS[form][2]]
         if form == rf or rf not in first:
             continue
@@ -1144,8 +1164,8 @@ def main():
                     help="headline form (ensemble API): mixed = the precision form (FP32 fluxes, limiter and "
                          "update; FP64 thickness prep and dp), mixed-fp32prep = the same with the thickness "
                          "factors in compensated FP32, fp64 = the FP64 form")
-    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-full,cnuity,fp64,mixed-fp32prep,"
-                                       "fp64-fct4,mixed-fct4,fp64-mpdata,mixed-mpdata,c3",
+    ap.add_argument("--forms", default="tsadvc,tsadvc-fct4,tsadvc-mpdata,tsadvc-full,tsadvc-btrmas,cnuity,fp64,"
+                                       "mixed-fp32prep,fp64-fct4,mixed-fct4,fp64-mpdata,mixed-mpdata,mixed-diff,c3",
                     help="forms measured beside the headline (tsadvc[-fct4|-mpdata|-pcm] = FP64 plain through "
                          "hyc_tsadvc, FCT2 unless named; tsadvc-full = asselin_save + tsadvc + its "
                          "diffusion + asselin_filter; cnuity = the continuity equation; fp64[-fct4|-mpdata], "

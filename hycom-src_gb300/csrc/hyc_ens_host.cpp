@@ -32,6 +32,8 @@ struct EBasin {
   double *dp = nullptr;
   void *lev[3] = {nullptr, nullptr, nullptr};  // tracer state, physical levels
   double *cell = nullptr;                       // strip kernel per-cell words (mixed form)
+  float2 *gd = nullptr;                         // diffusion grid table of the strip kernel (mixed form)
+  double temdf2 = 0.0;                          // lateral diffusion after each step (0: none)
   long long work = 0;                           // cells*layers*tracers, for queue ordering
   std::vector<double> posdef;                   // MPDATA offset per tracer (0 unless set)
 };
@@ -50,6 +52,7 @@ struct hyc_ens {
   bool prep64 = true;  // FP32-mixed: thickness prep in FP64 (else compensated FP32)
   int maxntr = 1;        // largest tracer count
   int strip_nq = 2;      // strip kernel: tracers per pass (1 or 2)
+  bool diff = false;     // some basin diffuses its tracers after each step (mixed form)
   CUtensorMap *d_cmaps = nullptr;  // [nbasin][kMaps]: strip kernel maps (levels 0-2, u, v, dp, cell words)
   CUtensorMap *d_fmaps = nullptr;  // FP64 form: the FCT tile kernel's maps, 3 rotations x basins
   size_t fmaps_cap = 0;
@@ -133,7 +136,7 @@ size_t esz(const hyc_ens *e) { return e->prec == HYC_PREC_MIXED ? 4 : 8; }
 
 // tx == 56 selects the two-column strip kernel (ty = rows per segment)
 bool is_col2(hyc::TileShape t) { return t.tx == hyc::kCol2Strip; }
-constexpr int kMaps = 7;  // strip kernel maps per basin
+constexpr int kMaps = 8;  // strip kernel maps per basin
 
 void free_all(hyc_ens *e) {
   for (auto &b : e->b) {
@@ -144,6 +147,7 @@ void free_all(hyc_ens *e) {
     cudaFree(b.vflx);
     cudaFree(b.dp);
     cudaFree(b.cell);
+    cudaFree(b.gd);
     for (auto &l : b.lev) cudaFree(l);
   }
   for (int r = 0; r < 3; r++) {
@@ -191,6 +195,7 @@ int encode_strip_maps(hyc_ens *e) {
     ok &= hyc::tmap_encode3(m + 4, b.vflx, 4, b.ld1, b.ld2, b.ld1, b.slice, b.kdm, bx, by);
     ok &= hyc::tmap_encode3(m + 5, b.dp, 8, b.ld1, b.ld2, b.ld1, b.slice, b.kdm, bx, by);
     ok &= hyc::tmap_encode3(m + 6, b.cell, 8, b.ld1, b.ld2, b.ld1, b.slice, 1, bx, by);
+    if (b.gd) ok &= hyc::tmap_encode3(m + 7, b.gd, 8, b.ld1, b.ld2, b.ld1, b.slice, 1, bx, by);
     if (!ok) return efail(e, HYC_ERR_CUDA, "cuTensorMapEncodeTiled failed for the strip maps (basin %zu)", i);
   }
   ECK(cudaMemcpy(e->d_cmaps, h.data(), h.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice), "strip maps copy");
@@ -248,6 +253,7 @@ int build_tables(hyc_ens *e, double dt2) {
         m.c2_v = c + 4;
         m.c2_dp = c + 5;
         m.c2_cg = c + 6;
+        m.c2_gd = c + 7;
       }
       ECK(cudaMemcpy(e->d_mix[r], t.data(), nb * sizeof(MixBasin), cudaMemcpyHostToDevice), "mix table");
     } else {
@@ -415,7 +421,7 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
   cudaError_t c;
   if (e->prec == HYC_PREC_MIXED)
     c = hyc::launch_mix_col2(advtyp, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm,
-                             std::min(e->strip_nq, e->maxntr), e->prep64, e->d_err, st);
+                             std::min(e->strip_nq, e->maxntr), e->prep64, e->diff, e->d_err, st);
   else if (e->prec != HYC_PREC_MIXED && (advtyp == 0 || advtyp == 1)) {
     // FP64 PCM/MPDATA: the plain form's tile kernel per basin, then the periodic halo
     c = cudaSuccess;
@@ -825,6 +831,69 @@ int hyc_ens_set_posdef(hyc_ens *e, int32_t basin, int32_t tracer, double posdef)
   return HYC_OK;
 }
 
+int hyc_ens_set_diffusion(hyc_ens *e, int32_t basin, double temdf2, const double *aspux, const double *aspvy,
+                          const double *scuy, const double *scvx, int32_t where) {
+  if (!e || basin < 0 || basin >= (int)e->b.size()) return efail(e, HYC_ERR_ARG, "hyc_ens_set_diffusion: bad basin");
+  if (e->prec != HYC_PREC_MIXED)
+    return efail(e, HYC_ERR_UNSUPPORTED, "hyc_ens_set_diffusion: the FP32-mixed form only (FP64: hyc_tsdff)");
+  if (!(temdf2 >= 0.0)) return efail(e, HYC_ERR_ARG, "hyc_ens_set_diffusion: temdf2 < 0");
+  if (temdf2 > 0.0 && (!aspux || !aspvy || !scuy || !scvx))
+    return efail(e, HYC_ERR_ARG, "hyc_ens_set_diffusion: null grid array");
+  if (where != HYC_HOST && where != HYC_DEVICE) return efail(e, HYC_ERR_ARG, "hyc_ens_set_diffusion: bad where");
+  Dev g(e->device);
+  ECK(cudaStreamSynchronize(e->stream), "diffusion sync");  // steps in flight read the tables
+  // every basin gets a table once one diffuses (zeros: no diffusion)
+  if (temdf2 > 0.0 && !e->diff) {
+    for (auto &b : e->b)
+      if (!b.gd) {
+        if (cudaMalloc(&b.gd, b.slice * sizeof(float2)) != cudaSuccess)
+          return efail(e, HYC_ERR_NOMEM, "hyc_ens_set_diffusion: table allocation");
+        ECK(cudaMemset(b.gd, 0, b.slice * sizeof(float2)), "diffusion table");
+      }
+  }
+  EBasin &b = e->b[basin];
+  if (b.gd) {
+    if (temdf2 > 0.0) {
+      const size_t rsl = (size_t)b.ld1r * b.ld2;
+      const double *src[4] = {aspux, aspvy, scuy, scvx};
+      double *tmp = nullptr;
+      if (where == HYC_HOST) {
+        if (cudaMalloc(&tmp, 4 * rsl * sizeof(double)) != cudaSuccess)
+          return efail(e, HYC_ERR_NOMEM, "hyc_ens_set_diffusion: staging");
+        for (int a = 0; a < 4; a++) {
+          cudaError_t c = cudaMemcpy(tmp + a * rsl, src[a], rsl * sizeof(double), cudaMemcpyHostToDevice);
+          if (c != cudaSuccess) {
+            cudaFree(tmp);
+            return efail(e, HYC_ERR_CUDA, "hyc_ens_set_diffusion: copy: %s", cudaGetErrorString(c));
+          }
+          src[a] = tmp + a * rsl;
+        }
+      }
+      cudaError_t c = hyc::launch_diff_table(src[0], src[1], src[2], src[3], b.msk, temdf2, b.ld1r, b.ld1, b.ld2,
+                                             b.gd, e->stream);
+      if (c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
+      cudaFree(tmp);
+      if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "hyc_ens_set_diffusion: %s", cudaGetErrorString(c));
+    } else {
+      ECK(cudaMemset(b.gd, 0, b.slice * sizeof(float2)), "diffusion table");
+    }
+  }
+  b.temdf2 = temdf2;
+  bool any = false;
+  for (const auto &x : e->b) any |= x.temdf2 > 0.0;
+  if (any != e->diff || temdf2 > 0.0) {
+    e->diff = any;
+    int rc = encode_strip_maps(e);
+    if (rc) return rc;
+    e->tbl_dt2 = -1.0;
+    if (e->gexec) {
+      cudaGraphExecDestroy(e->gexec);
+      e->gexec = nullptr;
+    }
+  }
+  return HYC_OK;
+}
+
 int hyc_ens_get_option(hyc_ens *e, int32_t option, int32_t *value) {
   if (!e || !value) return efail(e, HYC_ERR_ARG, "null argument");
   switch (option) {
@@ -869,6 +938,8 @@ int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32
   if (nsteps < 1) return efail(e, HYC_ERR_ARG, "nsteps < 1");
   if (!scheme_ok(e, advtyp))
     return efail(e, HYC_ERR_UNSUPPORTED, "ensemble advtyp %d not available for this precision", advtyp);
+  if (e->diff && !e->prep64)
+    return efail(e, HYC_ERR_UNSUPPORTED, "the diffusion epilogue needs the FP64 thickness prep (HYC_OPT_PREP64)");
   Dev g(e->device);
   int rc;
   if ((rc = build_items(e)) ||
@@ -934,6 +1005,8 @@ int hyc_ens_step(hyc_ens *e, int32_t advtyp, double delt1, int32_t nsteps, int32
 
 int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t *ty, double *ms_out) {
   if (!e) return efail(nullptr, HYC_ERR_ARG, "null ensemble");
+  if (e->diff && !e->prep64)
+    return efail(e, HYC_ERR_UNSUPPORTED, "the diffusion epilogue needs the FP64 thickness prep (HYC_OPT_PREP64)");
   Dev g(e->device);
   static const hyc::TileShape cands[] = {{32, 16}, {16, 16}, {56, 32}, {56, 64}, {56, 128}, {56, 256}, {56, 512}};
   hyc::TileShape best = e->shape;

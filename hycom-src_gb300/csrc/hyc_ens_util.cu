@@ -11,6 +11,43 @@
 namespace hyc {
 
 // ---------------------------------------------------------------------------
+// grid table of the strip kernel's diffusion epilogue: row r holds, per
+// cell, temdf2*aspux*scuy of row r-4 (0 where iu = 0) and temdf2*aspvy*scvx
+// of row r-3 (0 where iv = 0), as in tsdff_2x (mod_tsadvc.F90:2274-2287),
+// rounded to FP32; rows before the grid and the padding columns are 0
+// ---------------------------------------------------------------------------
+__global__ void diff_table_kernel(const double *aspux, const double *aspvy, const double *scuy, const double *scvx,
+                                  const uint8_t *msk, double temdf2, int ld1r, int ld1, int ld2, float2 *out) {
+  const long long n = (long long)ld1 * ld2;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(t / ld1), i = (int)(t - (long long)r * ld1);
+    float au = 0.f, av = 0.f;
+    if (i < ld1r) {
+      const int ru = r - 4, rv = r - 3;
+      if (ru >= 0 && (msk[i + (long long)ru * ld1] & kIU)) {
+        const long long o = i + (long long)ru * ld1r;
+        au = (float)(temdf2 * aspux[o] * scuy[o]);
+      }
+      if (rv >= 0 && (msk[i + (long long)rv * ld1] & kIV)) {
+        const long long o = i + (long long)rv * ld1r;
+        av = (float)(temdf2 * aspvy[o] * scvx[o]);
+      }
+    }
+    out[t] = make_float2(au, av);
+  }
+}
+
+cudaError_t launch_diff_table(const double *aspux, const double *aspvy, const double *scuy, const double *scvx,
+                              const uint8_t *msk, double temdf2, int ld1r, int ld1, int ld2, float2 *out,
+                              cudaStream_t s) {
+  const long long n = (long long)ld1 * ld2;
+  int bx = (int)((n + 255) / 256);
+  if (bx > 2048) bx = 2048;
+  diff_table_kernel<<<bx, 256, 0, s>>>(aspux, aspvy, scuy, scvx, msk, temdf2, ld1r, ld1, ld2, out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // format conversion between the reference layout (FP64, pitch ld1) and the
 // ensemble layout (FP32 or FP64, pitch ld1p), nslices slices
 // ---------------------------------------------------------------------------

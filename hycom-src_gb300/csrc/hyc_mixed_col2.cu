@@ -55,7 +55,7 @@ constexpr int kNS = 2;      // ring slots per warp
 constexpr int kWarps = 4;   // warps per CTA
 constexpr unsigned kFull = 0xffffffffu;
 
-template <int SCHEME, int NQ>
+template <int SCHEME, int NQ, bool DIFF>
 struct Ring {
   static constexpr int NC = SCHEME == kMPDATA ? 0 : NQ;  // centre-level rows (leapfrog schemes)
   static constexpr int FROW = kW * 4;  // one FP32 row
@@ -66,7 +66,9 @@ struct Ring {
   static constexpr int OFF_V = OFF_U + kRB * FROW;
   static constexpr int OFF_DP = OFF_V + kRB * FROW;   // dp, FP64
   static constexpr int OFF_CG = OFF_DP + kRB * DROW;  // per-cell word, FP64
-  static constexpr int TX_BYTES = OFF_CG + kRB * DROW;
+  static constexpr int OFF_D3 = OFF_CG + kRB * DROW;  // DIFF: dp three rows south, FP64
+  static constexpr int OFF_GD = OFF_D3 + (DIFF ? kRB * DROW : 0);  // DIFF: diffusion face factors (FP32 pairs)
+  static constexpr int TX_BYTES = OFF_GD + (DIFF ? kRB * DROW : 0);
   static constexpr int SLOT = (TX_BYTES + 127) / 128 * 128;
   static constexpr int WARP = kNS * SLOT;
   static constexpr size_t SMEM = (size_t)kWarps * WARP + kWarps * kNS * 8 + 128;
@@ -134,6 +136,12 @@ __device__ __forceinline__ float d2f_i(double x) {
   const unsigned m = ((hi >> 20) & 0x7FFu) > 0x380u ? (t & 0x7FFFFFFFu) : 0u;
   return __uint_as_float(m | (hi & 0x80000000u));
 }
+// max(x, onemu) by one signed comparison of the bit patterns: for positive
+// operands their integer order is the numeric order, and a negative x
+// (sign bit set) compares below onemu
+__device__ __forceinline__ double max_onemu(double x) {
+  return __double_as_longlong(x) < __double_as_longlong(kOnemu) ? kOnemu : x;
+}
 // 1/h: hardware seed and one Newton step in FP64 (h >= onemu > 0)
 __device__ __forceinline__ double rcp64(double h) {
   const double r = rcp_seed64(h);
@@ -155,16 +163,26 @@ __device__ __forceinline__ float2 sel(bool pa, bool pb, float2 a, float2 b) {
   return make_float2(pa ? a.x : b.x, pb ? a.y : b.y);
 }
 __device__ __forceinline__ float2 min2(float2 a, float2 b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
+// harmonc of mod_tsadvc.F90:1770-1771 on the clipped thicknesses, both
+// columns: 2ab/max(a+b, 2*eps_har)
+__device__ __forceinline__ float2 harmonic2(float2 a, float2 b) {
+  const float2 t = add2(a, b);
+  const float2 r = make_float2(rcp_approx(fmaxf(t.x, 2.0e-20f)), rcp_approx(fmaxf(t.y, 2.0e-20f)));
+  return mul2(mul2(mul2(a, make_float2(2.f, 2.f)), b), r);
+}
 __device__ __forceinline__ float2 pos2(float2 a) { return make_float2(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f)); }
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(fminf(a.x, 0.f), fminf(a.y, 0.f)); }
 
 
 // pipeline registers of one tracer, both columns.  Land neighbours drop
-// out of the 5-point extrema by carrying masked copies of the fields:
-// -BIG (for maxima) or +BIG (for minima) where ip = 0.
+// out of the 5-point extrema of the field by carrying a copy of it that is
+// NaN where ip = 0: max.f32 and min.f32 return the other operand when one
+// is NaN, so one copy serves the maxima and the minima (the centre operand
+// is the unmasked field, so no extremum is NaN).  The extrema of fmxlo and
+// fmnlo carry -BIG (maxima) or +BIG (minima) masked copies.
 struct St2 {
   float2 f1;                 // fld at J-1
-  float2 fA1, fB1, fA2, fB2;  // fld at J-1, J-2 masked for maxima (A) / minima (B)
+  float2 fN1, fN2;           // fld at J-1, J-2, NaN at land cells
   float2 c1, c2, c3;         // fldc at J-1 (J-2, J-3: FCT4's y stencil)
   float2 fx1, fy1;           // low-order x (west face) / y (south face) fluxes of row J-1
   float2 lo2, lo3;           // fldlo at J-2, J-3
@@ -179,7 +197,7 @@ struct St2 {
 // posdef offset enters through the mass-flux divergence only)
 struct StM {
   float2 f1;                  // fld at J-1
-  float2 fA1, fB1, fA2, fB2;  // fld at J-1, J-2 masked for maxima (A) / minima (B)
+  float2 fN1, fN2;            // fld at J-1, J-2, NaN at land cells
   float2 fx1, fy1;            // low-order x (west face) / y (south face) fluxes of row J-1, f part
   float2 tx1, ty1;            // .5|u|(f-f_w) of row J-1 (x), .5|v|(f-f_s) of the south face of J-1
   float2 fg2;                 // flxdiv (with posdef) of row J-2
@@ -197,11 +215,14 @@ constexpr bool kLateStore = true;
 
 }  // namespace
 
-template <int SCHEME, int NQ, bool PREP64>
+template <int SCHEME, int NQ, bool PREP64, bool DIFF>
 __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     mix_col2_kernel(const MixBasin *__restrict__ basins, const int4 *__restrict__ items, int nitems, int *head,
                     int *err) {
-  using RG = Ring<SCHEME, NQ>;
+  using RG = Ring<SCHEME, NQ, DIFF>;
+  // rows fed before the first stored row: the scheme reaches 3 rows; the
+  // diffusion epilogue stores row J-4 and needs the new values of J-5..J-3
+  constexpr int kLead = DIFF ? 4 : 3;
   constexpr bool MP = SCHEME == kMPDATA;
   constexpr bool F4 = SCHEME == kFCT4;
   using St = typename std::conditional<MP, StM, St2>::type;
@@ -231,7 +252,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     const long long sl = B.slice;
     const int s0 = 56 * w.y;  // strip start (padded column)
     const int j0 = 1 + w.z * B.seg, j1 = min(j0 + B.seg, jj + 1);
-    const int nblk = (j1 - j0 + 6 + kRB - 1) / kRB;
+    const int nblk = (j1 - j0 + 2 * kLead + kRB - 1) / kRB;
     const int nqp = (ntr + NQ - 1) / NQ;
     const int ka = w.w * B.kchunk, kb = min(kdm, ka + B.kchunk);  // this item's layers
     const int T = (kb - ka) * nqp * nblk;
@@ -246,7 +267,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
       const int rem = t - kk * nqp * nblk;
       const int k = ka + kk;
       const int qp = rem / nblk, blk = rem - qp * nblk;
-      const int y = j0 - 3 + blk * kRB + nb - 1;
+      const int y = j0 - kLead + blk * kRB + nb - 1;
       const uint32_t g = tg + t;
       unsigned char *slot = ring + (g % kNS) * RG::SLOT;
       uint64_t *b = bar + (g % kNS);
@@ -261,6 +282,10 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
       tma::load3(slot + RG::OFF_V, B.c2_v, b, s0, y, k);
       tma::load3(slot + RG::OFF_DP, B.c2_dp, b, s0, y, k);
       tma::load3(slot + RG::OFF_CG, B.c2_cg, b, s0, y, 0);
+      if (DIFF) {
+        tma::load3(slot + RG::OFF_D3, B.c2_dp, b, s0, y - 3, k);  // rows before the grid start read as 0
+        tma::load3(slot + RG::OFF_GD, B.c2_gd, b, s0, y, 0);
+      }
     };
     if (lane == 0)
       for (int d = 0; d < kNS && d < T; d++) issue(d);
@@ -289,6 +314,12 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
         float L2e = 0.f;                   // land flag east of column B, row J-2
         double dA1 = 0.0, dB1 = 0.0;       // dp of row J-1
         double sA1 = 0.0, sB1 = 0.0;       // dt2*scp2i of row J-1 (FP64 prep)
+        // DIFF: new values of row J-4 and the diffusive flux through its south face, per tracer;
+        // max(dp,0), dt2*scp2i and the land flags of row J-4
+        float2 D1[NQ], VF1[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; q++) D1[q] = VF1[q] = z2;
+        float2 h4 = z2, DS4 = z2, L4 = z2;
         for (int blk = 0; blk < nblk; blk++, t++) {
           const uint32_t g = tg + t;
           if (!__all_sync(kFull, tma::wait(bar + (g % kNS), (g / kNS) & 1u, err))) {
@@ -300,7 +331,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
           const unsigned char *slot = ring + (g % kNS) * RG::SLOT;
 #pragma unroll(PREP64 ? 2 : kRB)
           for (int rr = 0; rr < kRB; rr++) {
-            const int J = j0 - 3 + blk * kRB + rr;
+            const int J = j0 - kLead + blk * kRB + rr;
             // ---- inputs of row J
             const float2 u0 = ((const float2 *)(slot + RG::OFF_U + rr * RG::FROW))[lane];
             const float2 v0 = ((const float2 *)(slot + RG::OFF_V + rr * RG::FROW))[lane];
@@ -329,13 +360,14 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               // two-sum in FP32, scaled by dt2*scp2i and added to dp in FP64
               dv = comp_div2(east(u1), u1, v0, v1);
               const double bA = dA1 + kOnemu, bB = dB1 + kOnemu;       // dp + onemu
-              const double hA = ge0(dA1) ? bA : kOnemu, hB = ge0(dB1) ? bB : kOnemu;  // fcn + onemu
+              // fcn + onemu = max(dp, 0) + onemu (dp = -0 gives onemu either way)
+              const double hA = __double2hiint(dA1) >= 0 ? bA : kOnemu, hB = __double2hiint(dB1) >= 0 ? bB : kOnemu;
               const double rA = rcp64(hA), rB = rcp64(hB);
               const float2 hf = make_float2(d2f_pos(hA), d2f_pos(hB));
               if (!MP) {
                 // fco + onemu = max(dp + div*dt2*scp2i, 0) + onemu
-                const double cA = kmax(__fma_rn(f2d_i(dv.x), sA1, bA), kOnemu);
-                const double cB = kmax(__fma_rn(f2d_i(dv.y), sB1, bB), kOnemu);
+                const double cA = max_onemu(__fma_rn(f2d_i(dv.x), sA1, bA));
+                const double cB = max_onemu(__fma_rn(f2d_i(dv.y), sB1, bB));
                 W1 = make_float2(d2f_pos(cA * rA), d2f_pos(cB * rB));
               } else {
                 const double fA = f2d_i(dv.x) * sA1, fB = f2d_i(dv.y) * sB1;
@@ -378,12 +410,14 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
             const float2 F14 = make_float2(7.f / 12.f, 7.f / 12.f), F24 = make_float2(-1.f / 12.f, -1.f / 12.f);
             // land flags (1 = land)
             const float2 L0 = make_float2((mA & kIP) ? 0.f : 1.f, (mB & kIP) ? 0.f : 1.f);
+            const float qnan = __int_as_float(0x7fc00000);
+            const float2 M0 = make_float2((mA & kIP) ? 0.f : qnan, (mB & kIP) ? 0.f : qnan);  // NaN on land
             const bool ip1A = L1.x == 0.f, ip1B = L1.y == 0.f;
             const bool ip2B = L2.y == 0.f, ip2E = L2e == 0.f;  // column B and its east neighbour, row J-2
             const bool ip3A = L3.x == 0.f, ip3B = L3.y == 0.f;
-            const int jo = J - 3;
+            const int jo = J - kLead;  // the row stored at this step
             const bool rowout = jo >= j0 && jo < j1;
-            const bool stA = rowout && outA && ip3A, stB = rowout && outB && ip3B;
+            const bool stA = rowout && outA && (DIFF ? L4.x == 0.f : ip3A), stB = rowout && outB && (DIFF ? L4.y == 0.f : ip3B);
             const float2 nbig = make_float2(-kBig, -kBig), pbig = make_float2(kBig, kBig);
             // MPDATA (mod_tsadvc.F90:207-493), shared by the tracers:
             //  du1  divergence of the masked mass fluxes of row J-1 (the posdef part of
@@ -446,14 +480,14 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               // S1: low-order fluxes of row J (:686-720)
               const float2 fx0 = fma2(up0, west(f0[q]), mul2(un0, f0[q]));
               const float2 fy0 = fma2(vp0, s.f1, mul2(vn0, f0[q]));
-              const float2 fA0 = fma2(L0, nbig, f0[q]), fB0 = fma2(L0, pbig, f0[q]);  // exact at sea cells
+              const float2 fN0 = add2(f0[q], M0);  // exact at sea cells, NaN on land
               // S2: low-order solution of row J-1 (:778-791), extrema over sea neighbours
               const float2 c = s.f1;
-              const float2 aw = west(s.fA1), ae = east(s.fA1), bw = west(s.fB1), be = east(s.fB1);
-              const float fmxA = max3f(max3f(c.x, aw.x, ae.x), s.fA2.x, fA0.x);
-              const float fmxB = max3f(max3f(c.y, aw.y, ae.y), s.fA2.y, fA0.y);
-              const float fmnA = min3f(min3f(c.x, bw.x, be.x), s.fB2.x, fB0.x);
-              const float fmnB = min3f(min3f(c.y, bw.y, be.y), s.fB2.y, fB0.y);
+              const float2 fw = west(s.fN1), fe = east(s.fN1);
+              const float fmxA = max3f(max3f(c.x, fw.x, fe.x), s.fN2.x, fN0.x);
+              const float fmxB = max3f(max3f(c.y, fw.y, fe.y), s.fN2.y, fN0.y);
+              const float fmnA = min3f(min3f(c.x, fw.x, fe.x), s.fN2.x, fN0.x);
+              const float fmnB = min3f(min3f(c.y, fw.y, fe.y), s.fN2.y, fN0.y);
               const float2 fdv = mul2(comp_div2(east(s.fx1), s.fx1, fy0, s.fy1), DS1);
               const float2 t1 = fma2(c, W1, mul2(fdv, nR1));
               const float2 lo1 = make_float2(fmaxf(fmnA, fminf(fmxA, t1.x)), fmaxf(fmnB, fminf(fmxB, t1.y)));
@@ -537,10 +571,8 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               s.c3 = s.c2;
               s.c2 = s.c1;
               s.c1 = c0[q];
-              s.fA2 = s.fA1;
-              s.fB2 = s.fB1;
-              s.fA1 = fA0;
-              s.fB1 = fB0;
+              s.fN2 = s.fN1;
+              s.fN1 = fN0;
               s.f1 = f0[q];
             }
             } else {
@@ -553,14 +585,14 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               const float2 fy0 = fma2(vp0, s.f1, mul2(vn0, f0[q]));
               const float2 tx0 = mul2(ua0, sub2(f0[q], f0w));
               const float2 ty0 = mul2(va0, sub2(f0[q], s.f1));
-              const float2 fA0 = fma2(L0, nbig, f0[q]), fB0 = fma2(L0, pbig, f0[q]);
+              const float2 fN0 = add2(f0[q], M0);
               // P1/P2: extrema of row J-1 (:272-281) and its low-order solution (:345-353)
               const float2 c = s.f1;
-              const float2 aw = west(s.fA1), ae = east(s.fA1), bw = west(s.fB1), be = east(s.fB1);
-              const float2 mx1 = make_float2(max3f(max3f(c.x, aw.x, ae.x), s.fA2.x, fA0.x),
-                                             max3f(max3f(c.y, aw.y, ae.y), s.fA2.y, fA0.y));
-              const float2 mn1 = make_float2(min3f(min3f(c.x, bw.x, be.x), s.fB2.x, fB0.x),
-                                             min3f(min3f(c.y, bw.y, be.y), s.fB2.y, fB0.y));
+              const float2 fw = west(s.fN1), fe = east(s.fN1);
+              const float2 mx1 = make_float2(max3f(max3f(c.x, fw.x, fe.x), s.fN2.x, fN0.x),
+                                             max3f(max3f(c.y, fw.y, fe.y), s.fN2.y, fN0.y));
+              const float2 mn1 = make_float2(min3f(min3f(c.x, fw.x, fe.x), s.fN2.x, fN0.x),
+                                             min3f(min3f(c.y, fw.y, fe.y), s.fN2.y, fN0.y));
               const float2 fdf = mul2(comp_div2(east(s.fx1), s.fx1, fy0, s.fy1), DS1);
               const float2 Pq = make_float2(P[q], P[q]);
               const float2 t1 = fma2(Pq, Z1, fma2(c, W1, mul2(fdf, nR1)));
@@ -609,14 +641,40 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               s.ty1 = ty0;
               s.fx1 = fx0;
               s.fy1 = fy0;
-              s.fA2 = s.fA1;
-              s.fB2 = s.fB1;
-              s.fA1 = fA0;
-              s.fB1 = fB0;
+              s.fN2 = s.fN1;
+              s.fN1 = fN0;
               s.f1 = f0[q];
             }
             }
-            if (kLateStore && (stA || stB)) {
+            if constexpr (DIFF) {
+              // Laplacian diffusion of row J-4 (tsdff_2x/tsdff_1x, mod_tsadvc.F90:2262-2492) on the
+              // new values: face factors temdf2*aspux*scuy (0 where iu = 0) of row J-4 and
+              // temdf2*aspvy*scvx (0 where iv = 0) of row J-3 come from the grid table (its row J
+              // holds them), times the harmonic mean of max(dp,0) on either side; the update is
+              // -delt1/(scp2*max(dp,eps_har)) times the flux divergence, at sea cells only
+              const double2 e3 = ((const double2 *)(slot + RG::OFF_D3 + rr * RG::DROW))[lane];
+              const float4 g4 = ((const float4 *)(slot + RG::OFF_GD + rr * RG::DROW))[lane];
+              const float2 h3 = make_float2(fmaxf(d2f_i(e3.x), 0.f), fmaxf(d2f_i(e3.y), 0.f));
+              const float2 FU = mul2(make_float2(g4.x, g4.z), harmonic2(west(h4), h4));
+              const float2 FV = mul2(make_float2(g4.y, g4.w), harmonic2(h4, h3));
+              // delt1 is tsadvc's dt2, so delt1/scp2 = dt2*scp2i
+              const float2 FP = make_float2(L4.x == 0.f ? -DS4.x * rcp_approx(fmaxf(h4.x, 1.0e-20f)) : 0.f,
+                                            L4.y == 0.f ? -DS4.y * rcp_approx(fmaxf(h4.y, 1.0e-20f)) : 0.f);
+#pragma unroll
+              for (int q = 0; q < NQ; q++) {
+                const float2 dN = D1[q];
+                const float2 uw = mul2(FU, sub2(west(dN), dN));  // through the west face
+                const float2 vn = mul2(FV, sub2(dN, res[q]));    // through the north face
+                const float2 dvg = add2(sub2(east(uw), uw), sub2(vn, VF1[q]));
+                const float2 o = fma2(dvg, FP, dN);
+                if ((stA || stB) && q < nq) store_row(q, o.x, o.y);
+                VF1[q] = vn;
+                D1[q] = res[q];
+              }
+              h4 = h3;
+              DS4 = DS3;
+              L4 = L3;
+            } else if (kLateStore && (stA || stB)) {
 #pragma unroll
               for (int q = 0; q < NQ; q++)
                 if (q < nq) store_row(q, res[q].x, res[q].y);
@@ -698,7 +756,7 @@ cudaError_t launch_cell_words(const double *scp2i, const uint8_t *msk, double dt
 }
 
 cudaError_t launch_mix_col2(int scheme, const MixBasin *basins, const int4 *items, int nitems, int *head, int nsm,
-                            int nq, bool prep64, int *err, cudaStream_t s) {
+                            int nq, bool prep64, bool diff, int *err, cudaStream_t s) {
   auto pick = [&](auto kern, size_t smem) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -709,8 +767,11 @@ cudaError_t launch_mix_col2(int scheme, const MixBasin *basins, const int4 *item
     kern<<<nsm * per_sm, kWarps * 32, smem, s>>>(basins, items, nitems, head, err);
     return cudaGetLastError();
   };
-#define HYC_COL2(S, Q) (prep64 ? pick(mix_col2_kernel<S, Q, true>, Ring<S, Q>::SMEM) \
-                               : pick(mix_col2_kernel<S, Q, false>, Ring<S, Q>::SMEM))
+  if (diff && !prep64) return cudaErrorInvalidValue;  // the diffusion epilogue exists with the FP64 prep only
+#define HYC_COL2(S, Q)                                                                     \
+  (diff ? pick(mix_col2_kernel<S, Q, true, true>, Ring<S, Q, true>::SMEM)                  \
+        : prep64 ? pick(mix_col2_kernel<S, Q, true, false>, Ring<S, Q, false>::SMEM)        \
+                 : pick(mix_col2_kernel<S, Q, false, false>, Ring<S, Q, false>::SMEM))
   if (scheme == kFCT2) return nq >= 2 ? HYC_COL2(kFCT2, 2) : HYC_COL2(kFCT2, 1);
   if (scheme == kMPDATA) return nq >= 2 ? HYC_COL2(kMPDATA, 2) : HYC_COL2(kMPDATA, 1);
   if (scheme == kFCT4) return nq >= 2 ? HYC_COL2(kFCT4, 2) : HYC_COL2(kFCT4, 1);

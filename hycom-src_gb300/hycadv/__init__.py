@@ -51,7 +51,7 @@ EXPORTS = ("hyc_bigrid", "hyc_adv_init", "hyc_adv_finalize", "hyc_last_error", "
            "hyc_ens_last_error", "hyc_ens_set_option", "hyc_ens_get_option", "hyc_ens_set_posdef",
            "hyc_za_read", "hyc_za_parse_b", "hyc_za_check", "hyc_set_diffusion_grid", "hyc_tsdff",
            "hyc_asselin_save", "hyc_asselin_filter", "hyc_ens_get_async", "hyc_ens_wait",
-           "hyc_set_cnuity_grid", "hyc_cnuity", "hyc_selftest_wait")
+           "hyc_set_cnuity_grid", "hyc_cnuity", "hyc_selftest_wait", "hyc_ens_set_diffusion")
 ENS_WHAT = {"old": 0, "cur": 1, "uflx": 2, "vflx": 3, "dp": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
 TIMERS = {"tsadvc": 0, "xctilr": 1, "advect": 2, "copy": 3, "diag": 4, "tsdff": 5, "asselin": 6, "cnuity": 7}
@@ -143,6 +143,7 @@ def lib() -> C.CDLL:
         L.hyc_ens_set_option.argtypes = [vp, C.c_int32, C.c_int32]
         L.hyc_ens_get_option.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
         L.hyc_ens_set_posdef.argtypes = [vp, C.c_int32, C.c_int32, C.c_double]
+        L.hyc_ens_set_diffusion.argtypes = [vp, C.c_int32, C.c_double, vp, vp, vp, vp, C.c_int32]
         L.hyc_za_read.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, ip, vp, C.c_int32, dp, dp]
         L.hyc_za_parse_b.argtypes = [C.c_char_p, C.c_char_p, ip, ip, dp, dp]
         L.hyc_za_check.argtypes = [C.c_double] * 4
@@ -552,6 +553,21 @@ class Ensemble(_StreamFollower):
     def set_posdef(self, b: int, q: int, posdef: float):
         """MPDATA offset of tracer q of basin b (mod_tsadvc.F90:1755-1763)."""
         self._chk(lib().hyc_ens_set_posdef(self._h, b, q, float(posdef)))
+
+    def set_diffusion(self, b: int, temdf2: float, aspux=None, aspvy=None, scuy=None, scvx=None):
+        """Lateral diffusion of basin b's tracers after each step, fused into
+        the mixed form's step kernel (hyc_ens_set_diffusion); grid arrays in
+        the reference layout (numpy or CUDA tensors, all on the same side);
+        temdf2 = 0 turns it off."""
+        if temdf2 > 0:
+            arrs = [aspux, aspvy, scuy, scvx]
+            ptrs = [_ptr(a) for a in arrs]
+            if len({w for _, w in ptrs}) != 1:
+                raise ValueError("grid arrays must all be on the host or all on the device")
+            self._order(tuple(a for a in arrs if not isinstance(a, np.ndarray)))
+            self._chk(lib().hyc_ens_set_diffusion(self._h, b, float(temdf2), *[p for p, _ in ptrs], ptrs[0][1]))
+        else:  # 0 turns it off; a negative value is refused by the library
+            self._chk(lib().hyc_ens_set_diffusion(self._h, b, float(temdf2), None, None, None, None, HYC_HOST))
 
     def set_strip_tracers(self, n: int):
         """Mixed form: tracers advanced per pass of the strip kernel (1 or 2)."""

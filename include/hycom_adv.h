@@ -98,7 +98,8 @@ typedef struct hyc_tsadvc_params {
   int32_t btrmas;  /* barotropic mass flag (FCT2 becomes fct2c)        */
   int32_t ntracr;  /* number of tracers in the bound tracer array       */
   int32_t nhybrd;  /* number of hybrid layers                           */
-  int32_t isopyc;  /* isopycnic mode (nhybrd==0): unsupported, must be 0 */
+  int32_t isopyc;  /* isopycnic mode (nhybrd==0): layer-1 flux smoothing,
+                      mod_tsadvc.F90:1860-1897 (not with btrmas)        */
   int32_t hybrid;  /* nhybrd > 0                                        */
   int32_t mxlmy;   /* Mellor-Yamada mixed layer: also advect q2, q2l   */
   int32_t nstep;   /* model step; the salinity range diagnostic runs when
@@ -389,7 +390,7 @@ int hyc_advem_noalloc(int32_t idm, int32_t jdm, int32_t nbdy, int32_t advtyp, do
  *
  * Precision: HYC_PREC_FP64 (the plain form: FP64 state, bit-identical to
  * hyc_tsadvc) or HYC_PREC_MIXED (FP32 tracer state, fluxes, limiter and
- * update; FP64 dp, continuity and thickness division; see hyc_mixed.cu).
+ * update; FP64 dp, continuity and thickness division; see hyc_mixed_col2.cu).
  * The library keeps three leapfrog levels per basin and rotates them, so a
  * step never updates a level in place.
  * ---------------------------------------------------------------------- */
@@ -486,6 +487,23 @@ int hyc_ens_set_option(hyc_ens *ens, int32_t option, int32_t value);
  * (mod_tsadvc.F90:1755-1763); FCT ignores it.  Synchronous.
  */
 int hyc_ens_set_posdef(hyc_ens *ens, int32_t basin, int32_t tracer, double posdef);
+/*
+ * Lateral diffusion of basin b's tracers at the end of each step, fused
+ * into the step kernel's epilogue (FP32-mixed form with the FP64 thickness
+ * prep): the diffusion block of tsadvc (mod_tsadvc.F90:2138-2230) for
+ * hybrid layers with temdfc = 1 -- tsdff_2x / tsdff_1x (:2262-2492) on
+ * every tracer of the new level, face factors temdf2*aspux*scuy and
+ * temdf2*aspvy*scvx (where iu / iv) times the harmonic mean of max(dp,0)
+ * (dp = HYC_E_DP, the new thickness; onetamas = 1), the update
+ * -delt1/(scp2*max(dp,eps_har)) times the flux divergence at sea cells.
+ * The new values are written once, diffused.  th3d is not formed (the
+ * ensemble's tracers are generic).  aspux, aspvy, scuy, scvx: ld1*ld2
+ * doubles in the reference layout, halo included, host or device (where);
+ * temdf2 = 0 turns it off for the basin.  The FP64 form returns
+ * HYC_ERR_UNSUPPORTED (its diffusion is hyc_tsdff).  Synchronous.
+ */
+int hyc_ens_set_diffusion(hyc_ens *ens, int32_t basin, double temdf2, const double *aspux, const double *aspvy,
+                          const double *scuy, const double *scvx, int32_t where);
 int hyc_ens_get_option(hyc_ens *ens, int32_t option, int32_t *value);
 int hyc_ens_enable_timers(hyc_ens *ens, int32_t on);
 const char *hyc_ens_last_error(const hyc_ens *ens);

@@ -59,8 +59,10 @@ def _put(ens, i, d):
         ens.put(i, "cur", lv[m - 1].contiguous(), s0=q * kdm, ns=kdm)
 
 
-def _oracle_new(d, wl, k0, k1):
-    """The oracle's new level (t+1) of every tracer for layers k0..k1-1."""
+def _oracle_new(d, wl, k0, k1, dparams=None):
+    """The oracle's new level (t+1) of every tracer for layers k0..k1-1;
+    with dparams (temdf2 and the grid arrays), tsadvc's diffusion block after
+    the advection."""
     from oracle import oracle
 
     b = d["b"]
@@ -76,11 +78,14 @@ def _oracle_new(d, wl, k0, k1):
     g.tsadvc(m, n, temp=temp, saln=saln, th3d=np.zeros_like(temp), uflx=h(d["uflx"][k0:k1]),
              vflx=h(d["vflx"][k0:k1]), dp=dp, delt1=wl["delt1"], advtyp=2, tracer=tracer,
              trcflg=np.zeros(max(ntr - 2, 1), np.int32), nstep=1)
+    if dparams is not None:
+        g.tsdff(m, n, temp=temp, saln=saln, th3d=np.zeros_like(temp), dp=dp, oneta=np.ones((2, b.ld2, b.ld1)),
+                delt1=wl["delt1"], tracer=tracer, **dparams)
     out = [temp[n - 1], saln[n - 1]] + ([tracer[q, n - 1] for q in range(ntr - 2)] if ntr > 2 else [])
     return out
 
 
-def _compare(ens, i, d, wl, exact, label):
+def _compare(ens, i, d, wl, exact, label, dparams=None):
     """Per tracer (max rel err, rms rel err) of the ensemble's new level against
     the oracle, over interior sea cells, layer runs of CHUNK."""
     import torch
@@ -94,7 +99,7 @@ def _compare(ens, i, d, wl, exact, label):
     buf = torch.empty((CHUNK, b.ld2, b.ld1), dtype=torch.float64)
     for k0 in range(0, kdm, CHUNK):
         k1 = min(kdm, k0 + CHUNK)
-        want = _oracle_new(d, wl, k0, k1)
+        want = _oracle_new(d, wl, k0, k1, dparams)
         for q in range(ntr):
             got = buf[:k1 - k0]
             ens.get(i, "cur", got, s0=q * kdm + k0, ns=k1 - k0)
@@ -153,3 +158,29 @@ def test_c3_extreme_members_against_oracle(cuda):
             print(f"c3 {prec} {s['idm']}x{s['jdm']}x{s['kdm']} ntr {s['ntr']}: max rel err {mx.max():.2e}")
             assert mx.max() < 1e-6
         ens.close()
+
+
+def test_c1_fused_diffusion_against_oracle(cuda):
+    """The precision form with the diffusion epilogue on the 4500x3298 basin
+    (T and S, 8 layers): within 1e-6 of the oracle's tsadvc followed by its
+    diffusion block (mod_tsadvc.F90:2138-2230) on a uniform grid."""
+    import torch
+
+    import bench
+    import hycadv
+
+    torch.cuda.empty_cache()
+    wl = dict(bench.WORKLOADS["c1"])
+    d = _make(dict(nx=wl["nx"], ny=wl["ny"], kdm=CHUNK, ntr=2, seed=wl["seed"]), wl, cuda, True)
+    dx = np.sqrt(d["b"].metrics()[0])
+    grid = dict(aspux=np.ones_like(dx), aspvy=np.ones_like(dx), scuy=dx, scvx=dx)
+    ens = hycadv.Ensemble([d["spec"]], precision="mixed")
+    ens.set_diffusion(0, bench.TEMDF2, **grid)
+    _put(ens, 0, d)
+    ens.step(2, wl["delt1"], 1)
+    torch.cuda.synchronize()
+    mx, rms = _compare(ens, 0, d, wl, False, "c1 diffusion", dparams=dict(temdf2=bench.TEMDF2, **grid))
+    ens.close()
+    for q in range(2):
+        print(f"c1 with diffusion, tracer {q}: max rel err {mx[q]:.2e}, rms rel err {rms[q]:.2e}")
+        assert mx[q] < 1e-6, (q, mx[q])
