@@ -179,7 +179,8 @@ __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(fminf(a.x,
 // NaN where ip = 0: max.f32 and min.f32 return the other operand when one
 // is NaN, so one copy serves the maxima and the minima (the centre operand
 // is the unmasked field, so no extremum is NaN).  The extrema of fmxlo and
-// fmnlo carry -BIG (maxima) or +BIG (minima) masked copies.
+// fmnlo carry -BIG (maxima) or +BIG (minima) masked copies, and so does
+// MPDATA's field (measured faster there).
 struct St2 {
   float2 f1;                 // fld at J-1
   float2 fN1, fN2;           // fld at J-1, J-2, NaN at land cells
@@ -197,7 +198,7 @@ struct St2 {
 // posdef offset enters through the mass-flux divergence only)
 struct StM {
   float2 f1;                  // fld at J-1
-  float2 fN1, fN2;            // fld at J-1, J-2, NaN at land cells
+  float2 fA1, fB1, fA2, fB2;  // fld at J-1, J-2 masked for maxima (A) / minima (B)
   float2 fx1, fy1;            // low-order x (west face) / y (south face) fluxes of row J-1, f part
   float2 tx1, ty1;            // .5|u|(f-f_w) of row J-1 (x), .5|v|(f-f_s) of the south face of J-1
   float2 fg2;                 // flxdiv (with posdef) of row J-2
@@ -585,14 +586,14 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               const float2 fy0 = fma2(vp0, s.f1, mul2(vn0, f0[q]));
               const float2 tx0 = mul2(ua0, sub2(f0[q], f0w));
               const float2 ty0 = mul2(va0, sub2(f0[q], s.f1));
-              const float2 fN0 = add2(f0[q], M0);
+              const float2 fA0 = fma2(L0, nbig, f0[q]), fB0 = fma2(L0, pbig, f0[q]);
               // P1/P2: extrema of row J-1 (:272-281) and its low-order solution (:345-353)
               const float2 c = s.f1;
-              const float2 fw = west(s.fN1), fe = east(s.fN1);
-              const float2 mx1 = make_float2(max3f(max3f(c.x, fw.x, fe.x), s.fN2.x, fN0.x),
-                                             max3f(max3f(c.y, fw.y, fe.y), s.fN2.y, fN0.y));
-              const float2 mn1 = make_float2(min3f(min3f(c.x, fw.x, fe.x), s.fN2.x, fN0.x),
-                                             min3f(min3f(c.y, fw.y, fe.y), s.fN2.y, fN0.y));
+              const float2 aw = west(s.fA1), ae = east(s.fA1), bw = west(s.fB1), be = east(s.fB1);
+              const float2 mx1 = make_float2(max3f(max3f(c.x, aw.x, ae.x), s.fA2.x, fA0.x),
+                                             max3f(max3f(c.y, aw.y, ae.y), s.fA2.y, fA0.y));
+              const float2 mn1 = make_float2(min3f(min3f(c.x, bw.x, be.x), s.fB2.x, fB0.x),
+                                             min3f(min3f(c.y, bw.y, be.y), s.fB2.y, fB0.y));
               const float2 fdf = mul2(comp_div2(east(s.fx1), s.fx1, fy0, s.fy1), DS1);
               const float2 Pq = make_float2(P[q], P[q]);
               const float2 t1 = fma2(Pq, Z1, fma2(c, W1, mul2(fdf, nR1)));
@@ -641,8 +642,10 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               s.ty1 = ty0;
               s.fx1 = fx0;
               s.fy1 = fy0;
-              s.fN2 = s.fN1;
-              s.fN1 = fN0;
+              s.fA2 = s.fA1;
+              s.fB2 = s.fB1;
+              s.fA1 = fA0;
+              s.fB1 = fB0;
               s.f1 = f0[q];
             }
             }
