@@ -17,11 +17,11 @@ namespace hyc {
 struct MixBasin {
   int ii, jj, nbdy, ld1, ld2;
   long long slice;
-  int kdm, ntr;
+  int kdm, ntr;  // ntr: tracers this table's launch advances, from q0 on
   int images;  // periodic-x halo images to write (0 when closed)
   int seg;     // rows per strip segment
   int kchunk;  // layers per work item
-  int pad;
+  int q0;      // first tracer of this table's launch
   float *fnew;  // ntr*kdm slices, level t+1
   float posdef[kMaxFields];  // MPDATA offset of each tracer (mod_tsadvc.F90:1755-1763)
   // TMA maps (box 64 x 4 rows, device memory): levels t-1 and t (3-D, ld1 x

@@ -59,13 +59,17 @@ struct hyc_ens {
   int *d_err = nullptr;            // device error flag (bounded waits that gave up)
   // device tables, one per rotation
   MixBasin *d_mix[3] = {nullptr, nullptr, nullptr};
+  // the one-tracer launch of the strip kernel that advances an odd tracer
+  // count's last tracer when the main launch takes the tracers in pairs
+  MixBasin *d_mixt[3] = {nullptr, nullptr, nullptr};
   TileArgs *d_targs[3] = {nullptr, nullptr, nullptr};
   std::vector<TileArgs> h_targs[3];  // host copies (FP64 PCM/MPDATA run the plain tile kernel per basin)
   double tbl_dt2 = -1.0;
-  int4 *d_items = nullptr;
-  int nitems = 0;
+  int4 *d_items = nullptr;  // the main launch's items, then the one-tracer launch's
+  int nitems = 0, nitems_t = 0;
+  int items_nq = 0;         // tracers per pass the strip items were built for
   int items_tx = 0, items_ty = 0, items_layers = -1;
-  int *d_head = nullptr;  // one queue counter per step slot
+  int *d_head = nullptr;  // two queue counters per step slot (main and one-tracer launch)
   int nhead = 0;
   double *d_partial = nullptr;
   int npartial = 0;
@@ -152,6 +156,7 @@ void free_all(hyc_ens *e) {
   }
   for (int r = 0; r < 3; r++) {
     cudaFree(e->d_mix[r]);
+    cudaFree(e->d_mixt[r]);
     cudaFree(e->d_targs[r]);
   }
   cudaFree(e->d_items);
@@ -245,6 +250,8 @@ int build_tables(hyc_ens *e, double dt2) {
         m.fnew = (float *)b.lev[ln];
         m.seg = e->shape.ty;
         m.kchunk = col2_kchunk(e, b);
+        m.q0 = 0;
+        if (e->items_nq == 2 && b.ntr > 1) m.ntr = b.ntr & ~1;  // pairs; an odd last tracer is the other launch's
         for (int q = 0; q < b.ntr && q < hyc::kMaxFields; q++) m.posdef[q] = (float)b.posdef[q];
         const CUtensorMap *c = e->d_cmaps + i * kMaps;
         m.c2_old = c + lo;
@@ -255,7 +262,13 @@ int build_tables(hyc_ens *e, double dt2) {
         m.c2_cg = c + 6;
         m.c2_gd = c + 7;
       }
+      std::vector<MixBasin> tt(t);  // the one-tracer launch: each basin's last tracer
+      for (int i = 0; i < nb; i++) {
+        tt[i].q0 = e->b[i].ntr - 1;
+        tt[i].ntr = 1;
+      }
       ECK(cudaMemcpy(e->d_mix[r], t.data(), nb * sizeof(MixBasin), cudaMemcpyHostToDevice), "mix table");
+      ECK(cudaMemcpy(e->d_mixt[r], tt.data(), nb * sizeof(MixBasin), cudaMemcpyHostToDevice), "mix table");
     } else {
       std::vector<TileArgs> t(nb);
       for (int i = 0; i < nb; i++) {
@@ -348,14 +361,18 @@ int build_tables(hyc_ens *e, double dt2) {
 }
 
 // queue of work items, largest first (longest-processing-time order)
+// tracers per pass of the strip kernel's main launch
+int strip_pass(const hyc_ens *e) { return std::min(e->strip_nq, e->maxntr); }
+
 int build_items(hyc_ens *e) {
   const bool per_layer = e->prec != HYC_PREC_MIXED;
-  if (e->d_items && e->items_tx == e->shape.tx && e->items_ty == e->shape.ty) return HYC_OK;
+  const int nqm = strip_pass(e);
+  if (e->d_items && e->items_tx == e->shape.tx && e->items_ty == e->shape.ty && e->items_nq == nqm) return HYC_OK;
   struct W {
     long long work;
     int4 it;
   };
-  std::vector<W> w;
+  std::vector<W> w, wt;  // main launch, one-tracer launch
   for (int i = 0; i < (int)e->b.size(); i++) {
     const EBasin &b = e->b[i];
     const int ntx = (b.idm + e->shape.tx - 1) / e->shape.tx, nty = (b.jdm + e->shape.ty - 1) / e->shape.ty;
@@ -363,12 +380,19 @@ int build_items(hyc_ens *e) {
       // the layer chunks of a segment are queued together: the per-cell
       // words of the segment's rows are then read from DRAM about once
       // and from L2 by the other chunks
+      // with pairs of tracers per pass, an odd count's last tracer goes to the
+      // one-tracer launch instead of a pass that advances it twice
       const int nstrip = (b.nbdy + b.idm - 4 + hyc::kCol2Strip - 1) / hyc::kCol2Strip;
       const int kc = col2_kchunk(e, b), nkc = (b.kdm + kc - 1) / kc;
+      const int trm = nqm == 2 ? (b.ntr & ~1) : b.ntr;
+      const bool tail = nqm == 2 && (b.ntr & 1);
       for (int sg = 0; sg < nty; sg++)
         for (int kq = 0; kq < nkc; kq++)
-          for (int st = 0; st < nstrip; st++)
-            w.push_back({(long long)(std::min(b.kdm, (kq + 1) * kc) - kq * kc) * b.ntr, make_int4(i, st, sg, kq)});
+          for (int st = 0; st < nstrip; st++) {
+            const long long lay = std::min(b.kdm, (kq + 1) * kc) - kq * kc;
+            if (trm > 0) w.push_back({lay * trm, make_int4(i, st, sg, kq)});
+            if (tail) wt.push_back({lay, make_int4(i, st, sg, kq)});
+          }
       continue;
     }
     for (int t = 0; t < ntx * nty; t++) {
@@ -380,16 +404,21 @@ int build_items(hyc_ens *e) {
     }
   }
   std::stable_sort(w.begin(), w.end(), [](const W &a, const W &c) { return a.work > c.work; });
+  std::stable_sort(wt.begin(), wt.end(), [](const W &a, const W &c) { return a.work > c.work; });
   ECK(cudaStreamSynchronize(e->stream), "items sync");
-  std::vector<int4> it(w.size());
-  for (size_t i = 0; i < w.size(); i++) it[i] = w[i].it;
+  std::vector<int4> it;
+  it.reserve(w.size() + wt.size());
+  for (const auto &x : w) it.push_back(x.it);
+  for (const auto &x : wt) it.push_back(x.it);
   cudaFree(e->d_items);
   e->d_items = nullptr;
   ECK(cudaMalloc(&e->d_items, std::max<size_t>(1, it.size()) * sizeof(int4)), "items");
   ECK(cudaMemcpy(e->d_items, it.data(), it.size() * sizeof(int4), cudaMemcpyHostToDevice), "items copy");
-  e->nitems = (int)it.size();
+  e->nitems = (int)w.size();
+  e->nitems_t = (int)wt.size();
   e->items_tx = e->shape.tx;
   e->items_ty = e->shape.ty;
+  e->items_nq = nqm;
   e->tbl_dt2 = -1.0;  // ntx/nty in the tables depend on the shape
   return HYC_OK;
 }
@@ -398,7 +427,7 @@ int ensure_heads(hyc_ens *e, int n) {
   if (e->nhead >= n) return HYC_OK;
   cudaFree(e->d_head);
   e->d_head = nullptr;
-  ECK(cudaMalloc(&e->d_head, n * sizeof(int)), "queue heads");
+  ECK(cudaMalloc(&e->d_head, 2 * n * sizeof(int)), "queue heads");
   e->nhead = n;
   return HYC_OK;
 }
@@ -417,12 +446,19 @@ int prime(hyc_ens *e) {
 
 // one step's launches (queue reset + step kernel) for rotation r, head slot h
 int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
-  ECK(cudaMemsetAsync(e->d_head + h, 0, sizeof(int), st), "queue reset");
-  cudaError_t c;
-  if (e->prec == HYC_PREC_MIXED)
-    c = hyc::launch_mix_col2(advtyp, e->d_mix[r], e->d_items, e->nitems, e->d_head + h, e->nsm,
-                             std::min(e->strip_nq, e->maxntr), e->prep64, e->diff, e->d_err, st);
-  else if (e->prec != HYC_PREC_MIXED && (advtyp == 0 || advtyp == 1)) {
+  ECK(cudaMemsetAsync(e->d_head + 2 * h, 0, 2 * sizeof(int), st), "queue reset");
+  cudaError_t c = cudaSuccess;
+  int launches = 1;
+  if (e->prec == HYC_PREC_MIXED) {
+    if (e->nitems > 0)
+      c = hyc::launch_mix_col2(advtyp, e->d_mix[r], e->d_items, e->nitems, e->d_head + 2 * h, e->nsm, strip_pass(e),
+                               e->prep64, e->diff, e->d_err, st);
+    if (c == cudaSuccess && e->nitems_t > 0) {  // the odd counts' last tracers
+      c = hyc::launch_mix_col2(advtyp, e->d_mixt[r], e->d_items + e->nitems, e->nitems_t, e->d_head + 2 * h + 1,
+                               e->nsm, 1, e->prep64, e->diff, e->d_err, st);
+      launches = (e->nitems > 0) + 1;
+    }
+  } else if (e->prec != HYC_PREC_MIXED && (advtyp == 0 || advtyp == 1)) {
     // FP64 PCM/MPDATA: the plain form's tile kernel per basin, then the periodic halo
     c = cudaSuccess;
     for (size_t i = 0; i < e->b.size() && c == cudaSuccess; i++) {
@@ -434,9 +470,10 @@ int enqueue_step(hyc_ens *e, int advtyp, int r, int h, cudaStream_t st) {
     }
   }
   else
-    c = hyc::launch_fct_queue(advtyp, e->shape, e->d_targs[r], e->d_items, e->nitems, e->d_head + h, e->nsm, st);
+    c = hyc::launch_fct_queue(advtyp, e->shape, e->d_targs[r], e->d_items, e->nitems, e->d_head + 2 * h, e->nsm,
+                              st);
   if (c != cudaSuccess) return efail(e, HYC_ERR_CUDA, "step kernel: %s", cudaGetErrorString(c));
-  e->stats.launches += 1;
+  e->stats.launches += launches;
   return HYC_OK;
 }
 
@@ -538,7 +575,8 @@ int hyc_ens_create(hyc_ens **out, int32_t nbasin, const hyc_basin_spec *specs, i
     if (!cp) return bail(efail(nullptr, HYC_ERR_CUDA, "basin %d: upload failed", i));
   }
   for (int r = 0; r < 3; r++) {
-    bool ok = precision == HYC_PREC_MIXED ? cudaMalloc(&e->d_mix[r], nbasin * sizeof(MixBasin)) == cudaSuccess
+    bool ok = precision == HYC_PREC_MIXED ? cudaMalloc(&e->d_mix[r], nbasin * sizeof(MixBasin)) == cudaSuccess &&
+                                                cudaMalloc(&e->d_mixt[r], nbasin * sizeof(MixBasin)) == cudaSuccess
                                           : cudaMalloc(&e->d_targs[r], nbasin * sizeof(TileArgs)) == cudaSuccess;
     if (!ok) return bail(efail(nullptr, HYC_ERR_NOMEM, "tables"));
   }

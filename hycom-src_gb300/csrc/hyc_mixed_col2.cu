@@ -2,7 +2,8 @@
 // 64-column strip north through the rows, two columns per lane, with the
 // rows streamed into a per-warp shared-memory ring by TMA.
 //
-// Work item: (basin, strip, segment of rows, chunk of layers), all tracers.  The
+// Work item: (basin, strip, segment of rows, chunk of layers), all the
+// launch's tracers of the basin (its table entry's q0 .. q0+ntr-1).  The
 // strip starts at padded column s = 56*w (a multiple of 4, so every TMA box
 // starts on a 16-byte boundary), lane l owns columns s+2l and s+2l+1, and
 // the 56 columns s+4 .. s+59 are updated (the scheme reaches 3 cells).
@@ -248,7 +249,8 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
     if (it >= nitems) break;
     const int4 w = items[it];
     const MixBasin &B = basins[w.x];
-    const int ii = B.ii, jj = B.jj, nb = B.nbdy, ld1 = B.ld1, kdm = B.kdm, ntr = B.ntr, images = B.images;
+    const int ii = B.ii, jj = B.jj, nb = B.nbdy, ld1 = B.ld1, kdm = B.kdm, images = B.images;
+    const int q0 = B.q0, ntr = B.ntr;  // this launch's tracers: q0 .. q0+ntr-1
     float *const fnew = B.fnew;
     const long long sl = B.slice;
     const int s0 = 56 * w.y;  // strip start (padded column)
@@ -275,7 +277,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
       tma::expect_tx(b, RG::TX_BYTES);
 #pragma unroll
       for (int q = 0; q < NQ; q++) {
-        const int qq = min(qp * NQ + q, ntr - 1);
+        const int qq = q0 + min(qp * NQ + q, ntr - 1);
         tma::load3(slot + RG::OFF_FO + q * kRB * RG::FROW, B.c2_old, b, s0, y, qq * kdm + k);
         if (!MP) tma::load3(slot + RG::OFF_FC + q * kRB * RG::FROW, B.c2_cur, b, s0, y, qq * kdm + k);
       }
@@ -299,13 +301,14 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
         const int nq = min(NQ, ntr - qb);
         float *fn[NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; q++) fn[q] = fnew + ((long long)min(qb + (q < nq ? q : 0), ntr - 1) * kdm + k) * sl;
+        for (int q = 0; q < NQ; q++)
+          fn[q] = fnew + ((long long)(q0 + min(qb + (q < nq ? q : 0), ntr - 1)) * kdm + k) * sl;
         St S[NQ];
         float P[NQ];  // posdef of each tracer of the pass (MPDATA)
 #pragma unroll
         for (int q = 0; q < NQ; q++) {
           S[q] = St{};
-          P[q] = B.posdef[min(qb + q, ntr - 1)];
+          P[q] = B.posdef[q0 + min(qb + q, ntr - 1)];
         }
         const float2 z2 = make_float2(0.f, 0.f);
         float2 u1 = z2, u1m = z2, v1 = z2, R2 = z2, nR3 = z2, QF2 = z2, DS1 = z2, DS2 = z2, DS3 = z2, QS1 = z2;
