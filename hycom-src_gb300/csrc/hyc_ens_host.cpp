@@ -486,7 +486,8 @@ bool scheme_ok(const hyc_ens *e, int advtyp) {
 
 bool shape_ok(const hyc_ens *e, hyc::TileShape t) {
   if (e->prec == HYC_PREC_MIXED)
-    return is_col2(t) && (t.ty == 32 || t.ty == 64 || t.ty == 128 || t.ty == 256 || t.ty == 512);
+    return is_col2(t) && (t.ty == 32 || t.ty == 64 || t.ty == 128 || t.ty == 256 || t.ty == 512 || t.ty == 1024 ||
+                           t.ty == 2048);
   return (t.tx == 32 && t.ty == 16) || (t.tx == 16 && t.ty == 16);
 }
 
@@ -1046,7 +1047,8 @@ int hyc_ens_tune(hyc_ens *e, int32_t advtyp, double delt1, int32_t *tx, int32_t 
   if (e->diff && !e->prep64)
     return efail(e, HYC_ERR_UNSUPPORTED, "the diffusion epilogue needs the FP64 thickness prep (HYC_OPT_PREP64)");
   Dev g(e->device);
-  static const hyc::TileShape cands[] = {{32, 16}, {16, 16}, {56, 32}, {56, 64}, {56, 128}, {56, 256}, {56, 512}};
+  static const hyc::TileShape cands[] = {{32, 16},  {16, 16},  {56, 32},   {56, 64},  {56, 128},
+                                         {56, 256}, {56, 512}, {56, 1024}, {56, 2048}};
   hyc::TileShape best = e->shape;
   float best_ms = 1e30f;
   const hyc::TileShape keep = e->shape;

@@ -439,7 +439,7 @@ int hyc_ens_get_slices(hyc_ens *ens, int32_t basin, int32_t what, int32_t s0, in
                        int32_t where);
 /* Tile shape of the step kernel; hyc_ens_tune picks one.  Mixed form:
  * tx = 56, the strip kernel (64-column strips streamed by TMA, 56 columns
- * updated), ty = rows per segment, 32/64/128/256/512.  FP64 form: 32 x 16
+ * updated), ty = rows per segment, 32 to 2048 (powers of 2).  FP64 form: 32 x 16
  * or 16 x 16 cell tiles. */
 int hyc_ens_set_tile(hyc_ens *ens, int32_t tx, int32_t ty);
 /*
