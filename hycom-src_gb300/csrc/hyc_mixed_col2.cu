@@ -67,8 +67,7 @@ struct Ring {
   static constexpr int OFF_V = OFF_U + kRB * FROW;
   static constexpr int OFF_DP = OFF_V + kRB * FROW;   // dp, FP64
   static constexpr int OFF_CG = OFF_DP + kRB * DROW;  // per-cell word, FP64
-  static constexpr int OFF_D3 = OFF_CG + kRB * DROW;  // DIFF: dp three rows south, FP64
-  static constexpr int OFF_GD = OFF_D3 + (DIFF ? kRB * DROW : 0);  // DIFF: diffusion face factors (FP32 pairs)
+  static constexpr int OFF_GD = OFF_CG + kRB * DROW;  // DIFF: diffusion face factors (FP32 pairs)
   static constexpr int TX_BYTES = OFF_GD + (DIFF ? kRB * DROW : 0);
   static constexpr int SLOT = (TX_BYTES + 127) / 128 * 128;
   static constexpr int WARP = kNS * SLOT;
@@ -286,7 +285,6 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
       tma::load3(slot + RG::OFF_DP, B.c2_dp, b, s0, y, k);
       tma::load3(slot + RG::OFF_CG, B.c2_cg, b, s0, y, 0);
       if (DIFF) {
-        tma::load3(slot + RG::OFF_D3, B.c2_dp, b, s0, y - 3, k);  // rows before the grid start read as 0
         tma::load3(slot + RG::OFF_GD, B.c2_gd, b, s0, y, 0);
       }
     };
@@ -324,6 +322,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
 #pragma unroll
         for (int q = 0; q < NQ; q++) D1[q] = VF1[q] = z2;
         float2 h4 = z2, DS4 = z2, L4 = z2;
+        float2 hq1 = z2, hq2 = z2;  // DIFF: max(dp,0) of rows J-2, J-3 (FP32, from the thickness prep)
         for (int blk = 0; blk < nblk; blk++, t++) {
           const uint32_t g = tg + t;
           if (!__all_sync(kFull, tma::wait(bar + (g % kNS), (g / kNS) & 1u, err))) {
@@ -357,6 +356,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
 
             // ---- thickness factors of row J-1 (mod_tsadvc.F90:1905-1942)
             float2 W1, R1, QF1, Wm1, H1;  // Wm1 = W-1 and H1 = fco+fcn (MPDATA only)
+            float2 hc1 = z2;              // DIFF: max(dp,0) of row J-1
             float2 dv;                    // FP64 prep: the divergence of the face fluxes of row J-1
             bool unA = false, unB = false;  // FP64 prep, MPDATA: fco = dp + div*dt2*scp2i (no clip)
             if (PREP64) {
@@ -384,6 +384,7 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               }
               R1 = make_float2(d2f_pos(rA), d2f_pos(rB));
               QF1 = mul2(sub2(hf, onemu2), QS1);  // fcn*scp2/dt2
+              if (DIFF) hc1 = sub2(hf, onemu2);
             } else {
               const float2 fdv = mul2(comp_div2(east(u1), u1, v0, v1), DS1);
               const float2 d = make_float2(d2f_i(dA1), d2f_i(dB1));
@@ -656,11 +657,11 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
               // Laplacian diffusion of row J-4 (tsdff_2x/tsdff_1x, mod_tsadvc.F90:2262-2492) on the
               // new values: face factors temdf2*aspux*scuy (0 where iu = 0) of row J-4 and
               // temdf2*aspvy*scvx (0 where iv = 0) of row J-3 come from the grid table (its row J
-              // holds them), times the harmonic mean of max(dp,0) on either side; the update is
+              // holds them), times the harmonic mean of max(dp,0) on either side (kept in FP32
+              // from the thickness prep of rows J-3 and J-4); the update is
               // -delt1/(scp2*max(dp,eps_har)) times the flux divergence, at sea cells only
-              const double2 e3 = ((const double2 *)(slot + RG::OFF_D3 + rr * RG::DROW))[lane];
               const float4 g4 = ((const float4 *)(slot + RG::OFF_GD + rr * RG::DROW))[lane];
-              const float2 h3 = make_float2(fmaxf(d2f_i(e3.x), 0.f), fmaxf(d2f_i(e3.y), 0.f));
+              const float2 h3 = hq2;
               const float2 FU = mul2(make_float2(g4.x, g4.z), harmonic2(west(h4), h4));
               const float2 FV = mul2(make_float2(g4.y, g4.w), harmonic2(h4, h3));
               // delt1 is tsadvc's dt2, so delt1/scp2 = dt2*scp2i
@@ -678,6 +679,8 @@ __global__ void __launch_bounds__(kWarps * 32, NQ == 1 ? 3 : 2)
                 D1[q] = res[q];
               }
               h4 = h3;
+              hq2 = hq1;
+              hq1 = hc1;
               DS4 = DS3;
               L4 = L3;
             } else if (kLateStore && (stA || stB)) {
