@@ -36,6 +36,13 @@
 // conversions between FP32 and FP64 run on the integer pipes: on GB300 an
 // F2F conversion issues on the FP64 pipe, at about 1/60 of the FP32 rate.
 // Without PREP64 the factors are formed in compensated FP32.
+//
+// DIFF: tsadvc's lateral diffusion (mod_tsadvc.F90:2138-2230) runs on the
+// new values before they are stored -- at row J the epilogue diffuses row
+// J-4 against the new rows J-5 (its south-face flux, kept) and J-3 -- with
+// the face factors from a per-cell grid table streamed like the cell words
+// (row r of the table holds the u-factors of row r-4 and the v-factors of
+// row r-3).  Advection and diffusion are then one pass over the fields.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
